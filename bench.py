@@ -1,0 +1,390 @@
+#!/usr/bin/env python
+"""MTTKRP throughput on the 100M-nonzero power-law tensor.
+
+Workload (one "step" = MTTKRP of every mode, 0, 1, 2, on one GPU):
+  3rd-order COO tensor 4,000,000 x 2,000,000 x 25,000 with exactly 100,000,000
+  unique nonzeros; modes 0 and 1 truncated Zipf(1.2), mode 2 uniform; values
+  lognormal(0,1) float32; rank 32 float32 factors U[0,1).  Seeded synthetic
+  data from the library generator (sptgbGenerate).
+
+  value   GB/s by the reference's algorithmic byte count per MTTKRP,
+          nnz*(4N+4) + sum_m I_m*R*4 (src/sptensor/mttkrp_cuda_onekernel.cu:94-97),
+          with tensor copies and factors resident in HBM (sptgbCoo*).
+  e2e     the same metric through the drop-in C entry point sptCudaMTTKRP with
+          host buffers: every call copies the tensor and factors to the GPU,
+          sorts by the output mode when needed and copies the result back.
+  roofline  the segmented MTTKRP launch (k_zero_shared + k_mttkrp_seg), per
+          launch duration from CUDA events on the launching stream.
+  cpu_baseline  the oracle port of sptOmpMTTKRP_Reduce (all host threads) on
+          a 10M-nonzero sample tensor of the same shape and distributions.
+--impl reference times that CPU implementation alone (the reference's own
+library when it was built here, else the port), per step all three modes of
+the sample tensor.  With torchrun each rank runs its own replica (the path
+does not shard); value is the sum over ranks over the slowest rank's time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+DIMS = [4_000_000, 2_000_000, 25_000]
+ZIPF = [1.2, 1.2, None]
+RANK = 32
+SEED = 20261203
+METRIC = "MTTKRP GB/s (algorithmic bytes, all 3 modes, 100M-nnz power-law COO, rank 32)"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=300)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--nnz", type=int, default=100_000_000)
+    p.add_argument("--cpu-sample", type=int, default=10_000_000)
+    p.add_argument("--e2e-steps", type=int, default=3)
+    p.add_argument("--skip-cpu", action="store_true")
+    return p.parse_args()
+
+
+def spec_for(count, seed=SEED):
+    import sptol_gb300 as S
+    s = S.GenSpec()
+    s.seed = seed
+    s.nmodes = 3
+    for m, d in enumerate(DIMS):
+        s.ndims[m] = d
+        if ZIPF[m]:
+            s.coord_dist[m] = S.DIST_ZIPF
+            s.zipf_s[m] = ZIPF[m]
+        else:
+            s.coord_dist[m] = S.DIST_UNIFORM
+    s.count = count
+    s.merge_duplicates = 0
+    s.value_dist = S.VAL_LOGNORMAL
+    return s
+
+
+def algo_bytes(ndims, nnz, rank):
+    N = len(ndims)
+    return nnz * (4 * N + 4) + sum(d * rank * 4 for d in ndims)
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_per_launch():
+    """DRAM bytes per MTTKRP launch from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "mttkrp_coo_c2.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return int(float(line.split(":")[1]))
+    except Exception:
+        pass
+    return None
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons with nvidia-smi while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=" + self.Q, "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.gpu)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def reduce_max(value, world):
+    """Max of a float over ranks (identity for a single process)."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def cpu_port_mttkrp(t, mats, threads, reps):
+    """sptOmpMTTKRP_Reduce restated (oracle) on the sample: seconds per step."""
+    import oracle as O
+    inds, vals = t.arrays()
+    facs = [m.array()[: t.ndims[i]] for i, m in enumerate(mats[:3])]
+    best = []
+    for r in range(reps + 1):
+        t0 = time.perf_counter()
+        for mode in range(3):
+            O.mttkrp(t.ndims, inds, vals, facs, RANK, mode, precision="omp", tk=threads)
+        if r > 0:
+            best.append(time.perf_counter() - t0)
+    return float(np.mean(best))
+
+
+def cpu_reference_mttkrp(t, mats, threads, reps):
+    """The reference's own sptOmpMTTKRP_Reduce (when built here)."""
+    import oracle as O
+    inds, vals = t.arrays()
+    facs = [m.array()[: t.ndims[i]] for i, m in enumerate(mats[:3])]
+    tot = 0.0
+    for mode in range(3):
+        _, s = O.ref_mttkrp(t.ndims, inds, vals, facs, RANK, mode, which=1, tk=threads, reps=reps)
+        tot += s
+    return tot
+
+
+def cpu_leg(sample_nnz, reps, prefer_reference):
+    import oracle as O
+    import sptol_gb300 as S
+    O.build(with_ref=False)
+    threads = os.cpu_count() or 1
+    t = S.Tensor.generate(spec_for(sample_nnz, seed=SEED + 1))
+    mats = S.new_factors(DIMS, RANK, seed=2)
+    kind = "port"
+    if prefer_reference and os.path.exists(O.REF_PATH):
+        secs = cpu_reference_mttkrp(t, mats, threads, reps)
+        kind = "reference"
+    else:
+        secs = cpu_port_mttkrp(t, mats, threads, reps)
+    gbs = 3 * algo_bytes(DIMS, t.nnz, RANK) / secs / 1e9
+    sample = ("%d-nnz tensor of the same shape and distributions, all 3 modes, %d reps after 1 warm-up, "
+              "sptOmpMTTKRP_Reduce with %d threads" % (t.nnz, reps, threads))
+    return {"value": round(gbs, 3), "unit": "GB/s", "cores": threads, "kind": kind, "sample": sample,
+            "seconds_per_step": secs, "nnz_per_s": 3 * t.nnz / secs}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    steps, warm = max(1, args.steps if args.steps <= 20 else 5), args.warmup
+    import oracle as O
+    import sptol_gb300 as S
+    O.build(with_ref=False)
+    threads = os.cpu_count() or 1
+    t = S.Tensor.generate(spec_for(args.cpu_sample, seed=SEED + 1))
+    mats = S.new_factors(DIMS, RANK, seed=2)
+    kind = "reference" if os.path.exists(O.REF_PATH) else "port"
+    f = cpu_reference_mttkrp if kind == "reference" else cpu_port_mttkrp
+    for _ in range(max(0, min(warm, 1))):
+        f(t, mats, threads, 0)
+    secs = f(t, mats, threads, steps)
+    gbs = 3 * algo_bytes(DIMS, t.nnz, RANK) / secs / 1e9
+    line = {
+        "metric": METRIC, "value": round(gbs, 3), "unit": "GB/s", "n_gpus": args.gpus, "steps": steps,
+        "warmup": warm, "ms_per_step": secs * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+        "config": {"workload": "mttkrp_powerlaw_coo_4Mx2Mx25K_rank32_sample", "nnz": t.nnz,
+                   "dims": DIMS, "zipf": ZIPF, "values": "lognormal(0,1)", "rank": RANK},
+        "cpu_baseline": {"value": round(gbs, 3), "unit": "GB/s", "cores": threads, "kind": kind,
+                         "sample": "%d-nnz tensor of the workload's shape and distributions, 3 modes per step, "
+                                   "sptOmpMTTKRP_Reduce, %d threads" % (t.nnz, threads)},
+        "e2e": {"value": round(gbs, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, world, rank, local):
+    import torch
+    import sptol_gb300 as S
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    L = S.lib()
+    L.sptgbInit(local)
+    os.environ.setdefault("SPTGB_QUIET", "1")
+    gen_t0 = time.time()
+    t = S.Tensor.generate(spec_for(args.nnz))
+    gen_s = time.time() - gen_t0
+    ndims = t.ndims
+    nnz = t.nnz
+    stride = ((RANK - 1) // 8 + 1) * 8
+    mats = S.new_factors(ndims, RANK, seed=1)
+    dfac = [torch.from_numpy(mats[m].array()[: ndims[m]].copy()).cuda() for m in range(3)]
+    dout = torch.zeros((max(ndims), stride), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+    prep_t0 = time.time()
+    coo = S.DeviceCoo(t, stream=sh)
+    for m in range(3):
+        coo.prepare(m, stream=sh)
+    torch.cuda.synchronize()
+    prep_s = time.time() - prep_t0
+    ptrs = [f.data_ptr() for f in dfac]
+    orders = [[m] + [(m + i) % 3 for i in (1, 2)] for m in range(3)]
+
+    def launch(mode):
+        coo.mttkrp(mode, orders[mode], ptrs, RANK, stride, dout.data_ptr(), stream=sh)
+
+    for _ in range(args.warmup):
+        for m in range(3):
+            launch(m)
+    torch.cuda.synchronize()
+    K = args.steps
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(3 * K)]
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    clocks = Clocks(local)
+    clocks.start()
+    time.sleep(0.3)
+    barrier(world)
+    torch.cuda.synchronize()
+    n0 = S.launch_count()
+    t_start.record(stream)
+    i = 0
+    for _ in range(K):
+        for m in range(3):
+            evs[i][0].record(stream)
+            launch(m)
+            evs[i][1].record(stream)
+            i += 1
+    t_end.record(stream)
+    torch.cuda.synchronize()
+    n1 = S.launch_count()
+    barrier(world)
+    timed_ms = t_start.elapsed_time(t_end)
+    if len(clocks.rows) < 5:
+        # the timed region was shorter than the sampling period: keep the same
+        # kernels running for about a second more so the clock record covers them
+        t1 = time.time()
+        while time.time() - t1 < 1.5:
+            for m in range(3):
+                launch(m)
+            torch.cuda.synchronize()
+    clocks.stop()
+    per_launch = [evs[j][0].elapsed_time(evs[j][1]) for j in range(3 * K)]
+    per_mode = [float(np.mean(per_launch[m::3])) for m in range(3)]
+    ms_max = reduce_max(timed_ms, world)
+    bytes_step = 3 * algo_bytes(ndims, nnz, RANK)
+    value = world * K * bytes_step / (ms_max / 1e3) / 1e9
+    peak, peak_kind = peaks()
+    launch_ms = float(np.mean(per_launch))
+    achieved = algo_bytes(ndims, nnz, RANK) / (launch_ms / 1e3) / 1e9
+    traffic = traffic_per_launch()
+
+    # e2e through the drop-in host-buffer API
+    h2d = 0
+    d2h = 0
+    for m in range(3):
+        h2d += nnz * 16 + sum(ndims[p] * stride * 4 for p in orders[m][1:])
+        d2h += ndims[m] * stride * 4
+    ke = max(1, args.e2e_steps)
+    S.mttkrp(t, mats, 0, entry="sptCudaMTTKRP")
+    barrier(world)
+    e0 = time.perf_counter()
+    for _ in range(ke):
+        for m in range(3):
+            S.mttkrp(t, mats, m, mats_order=orders[m], entry="sptCudaMTTKRP")
+    e_s = reduce_max((time.perf_counter() - e0) / ke, world)
+    e2e = world * bytes_step / e_s / 1e9
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.skip_cpu:
+        cpu = cpu_leg(args.cpu_sample, 3, prefer_reference=False)
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": world, "steps": K,
+            "warmup": args.warmup, "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "mttkrp_powerlaw_coo_4Mx2Mx25K_100Mnnz_rank32", "dims": ndims, "nnz": nnz,
+                       "zipf": ZIPF, "values": "lognormal(0,1)", "rank": RANK, "modes_per_step": 3,
+                       "l2": "inputs larger than L2 (1.6 GB nonzero stream per launch)",
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": peak_kind,
+                         "kernel": "k_zero_shared + k_mttkrp_seg (one MTTKRP launch)",
+                         "ms_per_launch_by_mode": [round(x, 4) for x in per_mode]},
+            "e2e": {"value": round(e2e, 2), "unit": "GB/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "entry": "sptCudaMTTKRP (host buffers)", "ms_per_step": e_s * 1e3},
+            "gpu_launches": int(n1 - n0),
+            "clocks": clocks.summary(),
+            "nnz_per_s": round(world * K * 3 * nnz / (ms_max / 1e3), 1),
+            "setup_s": {"generate": round(gen_s, 2), "upload_and_sort_3_modes": round(prep_s, 2)},
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    coo.free()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_init()
+    if args.impl == "reference":
+        if world > 1 and rank != 0:
+            return
+        run_reference(args, world, rank)
+        return
+    run_ours(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,286 @@
+/*
+ * ParTI.h -- drop-in public header of the GB300-native sparse MTTKRP / CP-ALS
+ * library.
+ *
+ * Everything a caller of ParTI!'s MTTKRP and CP-ALS path links against is
+ * declared here with the same names, argument meaning and struct layouts as
+ * ParTI! built with 32-bit indices, 32-bit values and 8-bit element indices
+ * (reference: include/includes/types.h:30-94, include/includes/structs.h,
+ * include/includes/macros.h:44-52, CMakeLists.txt:24-26).  The compute behind
+ * every declared MTTKRP / sort / HiCOO / CP-ALS entry point runs on the GPU;
+ * there is no CPU implementation of those operations in this library.
+ *
+ * Struct layouts are byte-identical to the reference so that objects built by
+ * code compiled against ParTI!'s own header can be handed to this library.
+ */
+#ifndef PARTI_H
+#define PARTI_H
+
+#include <stddef.h>
+#include <stdio.h>
+#include <stdint.h>
+#include <inttypes.h>
+#include <stdbool.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- types --
+ * Widths fixed at index 32 / value 32 / element 8 (types.h:30-94). */
+typedef uint32_t sptIndex;
+typedef uint32_t sptBlockIndex;
+typedef float    sptValue;
+typedef uint8_t  sptElementIndex;
+typedef uint16_t sptBlockMatrixIndex;
+typedef sptBlockIndex sptBlockNnzIndex;
+typedef uint64_t sptNnzIndex;
+#if defined(__SIZEOF_INT128__)
+typedef unsigned __int128 sptMortonIndex;
+#endif
+
+#define PARTI_INDEX_TYPEWIDTH 32
+#define PARTI_VALUE_TYPEWIDTH 32
+#define PARTI_ELEMENT_INDEX_TYPEWIDTH 8
+#define PARTI_INDEX_MAX UINT32_MAX
+#define PARTI_PRI_INDEX PRIu32
+#define PARTI_PRI_NNZ_INDEX PRIu64
+#define PARTI_PRI_VALUE "f"
+
+/* --------------------------------------------------------------- errors --
+ * Same codes as SptError (macros.h:44-52).  CUDA failures are reported as
+ * SPTERR_CUDA_ERROR + cudaError_t, as spt_CheckCudaError does
+ * (src/error/error.h:81-86). */
+typedef enum {
+    SPTERR_NO_ERROR       = 0,
+    SPTERR_UNKNOWN        = 1,
+    SPTERR_SHAPE_MISMATCH = 2,
+    SPTERR_VALUE_ERROR    = 3,
+    SPTERR_ZERO_DIVISION  = 4,
+    SPTERR_NO_MORE        = 99,
+    SPTERR_OS_ERROR       = 0x10000,
+    SPTERR_CUDA_ERROR     = 0x20000,
+} SptError;
+
+/* ----------------------------------------------------------- containers --
+ * structs.h:23-203, same member order and types. */
+typedef struct { sptNnzIndex len; sptNnzIndex cap; sptValue *data; } sptValueVector;
+typedef struct { sptNnzIndex len; sptNnzIndex cap; sptIndex *data; } sptIndexVector;
+typedef struct { sptNnzIndex len; sptNnzIndex cap; sptElementIndex *data; } sptElementIndexVector;
+typedef struct { sptNnzIndex len; sptNnzIndex cap; sptBlockIndex *data; } sptBlockIndexVector;
+typedef struct { sptNnzIndex len; sptNnzIndex cap; sptNnzIndex *data; } sptNnzIndexVector;
+
+/* Dense row-major matrix; stride = ncols rounded up to 8 (matrix.c:37-56). */
+typedef struct {
+    sptIndex nrows;
+    sptIndex ncols;
+    sptIndex cap;
+    sptIndex stride;
+    sptValue *values;
+} sptMatrix;
+
+/* Dense matrix with a small column count (structs.h:76-82). */
+typedef struct {
+    sptIndex        nrows;
+    sptElementIndex ncols;
+    sptIndex        cap;
+    sptElementIndex stride;
+    sptValue        *values;
+} sptRankMatrix;
+
+/* COO sparse tensor (structs.h:113-120): inds[m].data[x] is the mode-m
+ * coordinate of nonzero x, values.data[x] its value. */
+typedef struct {
+    sptIndex nmodes;
+    sptIndex *sortorder;
+    sptIndex *ndims;
+    sptNnzIndex nnz;
+    sptIndexVector *inds;
+    sptValueVector values;
+} sptSparseTensor;
+
+/* HiCOO sparse tensor (structs.h:126-156). */
+typedef struct {
+    sptIndex            nmodes;
+    sptIndex            *sortorder;
+    sptIndex            *ndims;
+    sptNnzIndex         nnz;
+    sptElementIndex     sb_bits;
+    sptElementIndex     sk_bits;
+    sptElementIndex     sc_bits;
+    sptNnzIndexVector   kptr;
+    sptIndexVector      **kschr;
+    sptIndex            *nkiters;
+    sptNnzIndexVector   cptr;
+    sptIndexVector      **kschr_balanced;
+    sptIndexVector      **kschr_balanced_pos;
+    sptIndex            *nkpars;
+    sptIndexVector      *kschr_rest;
+    sptNnzIndexVector   knnzs;
+    sptNnzIndexVector   bptr;
+    sptBlockIndexVector *binds;
+    sptElementIndexVector *einds;
+    sptValueVector      values;
+} sptSparseTensorHiCOO;
+
+/* Kruskal tensor, the CP-ALS result (structs.h:196-203). */
+typedef struct {
+    sptIndex nmodes;
+    sptIndex rank;
+    sptIndex *ndims;
+    sptValue *lambda;
+    double fit;
+    sptMatrix **factors;
+} sptKruskalTensor;
+
+typedef struct {
+    sptIndex nmodes;
+    sptElementIndex rank;
+    sptIndex *ndims;
+    sptValue *lambda;
+    double fit;
+    sptRankMatrix **factors;
+} sptRankKruskalTensor;
+
+typedef struct { sptIndex key; sptIndex value; } sptKeyValuePair;
+
+/* Opaque timer (macros.h:38); this library's timers are CUDA events on the
+ * library stream when use_cuda != 0, CLOCK_MONOTONIC otherwise. */
+typedef struct sptTagTimer *sptTimer;
+
+/* ------------------------------------------------------ error reporting --
+ * Thread-local last error, as src/error/error.c:28-116. */
+int  sptGetLastError(const char **module, const char **file, unsigned *line, const char **reason);
+void sptClearLastError(void);
+
+/* ------------------------------------------------------------- timers -- */
+int    sptNewTimer(sptTimer *timer, int use_cuda);
+int    sptStartTimer(sptTimer timer);
+int    sptStopTimer(sptTimer timer);
+double sptElapsedTime(const sptTimer timer);
+double sptPrintElapsedTime(const sptTimer timer, const char *name);
+double sptPrintAverageElapsedTime(const sptTimer timer, const int niters, const char *name);
+int    sptFreeTimer(sptTimer timer);
+int    sptCudaSetDevice(int device);
+int    sptCudaGetLastError(void);
+
+/* ------------------------------------------------------------- vectors --
+ * include/includes/vectors.h: same growth rule (cap += cap/2). */
+sptNnzIndex sptMaxNnzIndexArray(sptNnzIndex const *indices, sptNnzIndex const size);
+sptIndex    sptMaxIndexArray(sptIndex const *indices, sptNnzIndex const size);
+void        sptPairArraySort(sptKeyValuePair *kvarray, sptIndex const length);
+
+int  sptNewValueVector(sptValueVector *vec, uint64_t len, uint64_t cap);
+int  sptConstantValueVector(sptValueVector *const vec, sptValue const val);
+int  sptCopyValueVector(sptValueVector *dest, const sptValueVector *src, int const nt);
+int  sptAppendValueVector(sptValueVector *vec, sptValue const value);
+int  sptResizeValueVector(sptValueVector *vec, sptNnzIndex const size);
+void sptFreeValueVector(sptValueVector *vec);
+
+int  sptNewIndexVector(sptIndexVector *vec, uint64_t len, uint64_t cap);
+int  sptConstantIndexVector(sptIndexVector *const vec, sptIndex const num);
+int  sptCopyIndexVector(sptIndexVector *dest, const sptIndexVector *src, int const nt);
+int  sptAppendIndexVector(sptIndexVector *vec, sptIndex const value);
+int  sptResizeIndexVector(sptIndexVector *vec, sptNnzIndex const size);
+void sptFreeIndexVector(sptIndexVector *vec);
+
+int  sptNewElementIndexVector(sptElementIndexVector *vec, uint64_t len, uint64_t cap);
+int  sptAppendElementIndexVector(sptElementIndexVector *vec, sptElementIndex const value);
+int  sptResizeElementIndexVector(sptElementIndexVector *vec, sptNnzIndex const size);
+void sptFreeElementIndexVector(sptElementIndexVector *vec);
+
+int  sptNewBlockIndexVector(sptBlockIndexVector *vec, uint64_t len, uint64_t cap);
+int  sptAppendBlockIndexVector(sptBlockIndexVector *vec, sptBlockIndex const value);
+int  sptResizeBlockIndexVector(sptBlockIndexVector *vec, sptNnzIndex const size);
+void sptFreeBlockIndexVector(sptBlockIndexVector *vec);
+
+int  sptNewNnzIndexVector(sptNnzIndexVector *vec, uint64_t len, uint64_t cap);
+int  sptAppendNnzIndexVector(sptNnzIndexVector *vec, sptNnzIndex const value);
+int  sptResizeNnzIndexVector(sptNnzIndexVector *vec, sptNnzIndex const size);
+void sptFreeNnzIndexVector(sptNnzIndexVector *vec);
+
+/* ------------------------------------------------------- dense matrices --
+ * include/includes/matrices.h (containers; the CP-ALS reductions run on the
+ * GPU inside sptCpdAls). */
+int  sptNewMatrix(sptMatrix *mtx, sptIndex const nrows, sptIndex const ncols);
+int  sptRandomizeMatrix(sptMatrix *mtx, sptIndex const nrows, sptIndex const ncols);
+int  sptIdentityMatrix(sptMatrix *mtx);
+int  sptConstantMatrix(sptMatrix *const mtx, sptValue const val);
+int  sptCopyMatrix(sptMatrix *dest, const sptMatrix *src);
+void sptFreeMatrix(sptMatrix *mtx);
+sptValue sptRandomValue(void);
+
+/* ---------------------------------------------------- COO sparse tensor --
+ * include/includes/sptensors.h. */
+int    sptNewSparseTensor(sptSparseTensor *tsr, sptIndex nmodes, const sptIndex ndims[]);
+int    sptCopySparseTensor(sptSparseTensor *dest, const sptSparseTensor *src, int const nt);
+void   sptFreeSparseTensor(sptSparseTensor *tsr);
+double SparseTensorFrobeniusNormSquared(sptSparseTensor const *const spten);
+
+void sptGetBestModeOrder(sptIndex *mode_order, sptIndex const mode, sptIndex const *ndims, sptIndex const nmodes);
+void sptGetWorstModeOrder(sptIndex *mode_order, sptIndex const mode, sptIndex const *ndims, sptIndex const nmodes);
+
+/* Device sorts, bit-exact with the reference's orders on unique coordinates
+ * (src/sptensor/sort.c:410-585).  tk is accepted and ignored. */
+void sptSparseTensorSortIndex(sptSparseTensor *tsr, int force, int tk);
+void sptSparseTensorSortIndexAtMode(sptSparseTensor *tsr, sptIndex const mode, int force, int tk);
+void sptSparseTensorSortIndexCustomOrder(sptSparseTensor *tsr, sptIndex const *mode_order, int force, int tk);
+void sptSparseTensorSortIndexRowBlock(sptSparseTensor *tsr, int force, const sptNnzIndex begin,
+                                      const sptNnzIndex end, const sptElementIndex sk_bits, int const tk);
+void sptSparseTensorSortIndexMorton(sptSparseTensor *tsr, int force, const sptNnzIndex begin,
+                                    const sptNnzIndex end, const sptElementIndex sb_bits, int tk);
+int  sptSparseTensorMixedOrder(sptSparseTensor *tsr, const sptElementIndex sb_bits,
+                               const sptElementIndex sk_bits, int const tk);
+
+/* ------------------------------------------------------ HiCOO container -- */
+int  sptNewSparseTensorHiCOO(sptSparseTensorHiCOO *hitsr, const sptIndex nmodes, const sptIndex ndims[],
+                             const sptNnzIndex nnz, const sptElementIndex sb_bits,
+                             const sptElementIndex sk_bits, const sptElementIndex sc_bits);
+void sptFreeSparseTensorHiCOO(sptSparseTensorHiCOO *hitsr);
+/* COO -> HiCOO on the GPU; sorts tsr in place exactly as the reference does
+ * (src/sptensor/hicoo/convert.c:300-497). */
+int  sptSparseTensorToHiCOO(sptSparseTensorHiCOO *hitsr, sptNnzIndex *max_nnzb, sptSparseTensor *tsr,
+                            const sptElementIndex sb_bits, const sptElementIndex sk_bits, int const tk);
+int  sptSetKernelPointers(sptNnzIndexVector *kptr, sptSparseTensor *tsr, const sptElementIndex sk_bits);
+double sptSparseTensorFrobeniusNormSquaredHiCOO(sptSparseTensorHiCOO const *const hitsr);
+
+/* --------------------------------------------------------------- MTTKRP --
+ * mats[0..nmodes-1] are the factor matrices, mats[nmodes] receives the
+ * result rows [0, ndims[mode]); mats_order[1..nmodes-1] lists the factors
+ * multiplied (src/sptensor/mttkrp.c:39-115).  All variants run on the GPU;
+ * thread counts, reduction copies and impl_num are accepted and ignored. */
+int sptMTTKRP(sptSparseTensor const *const X, sptMatrix *mats[], sptIndex const mats_order[], sptIndex const mode);
+int sptOmpMTTKRP(sptSparseTensor const *const X, sptMatrix *mats[], sptIndex const mats_order[],
+                 sptIndex const mode, const int tk);
+int sptOmpMTTKRP_Reduce(sptSparseTensor const *const X, sptMatrix *mats[], sptMatrix *copy_mats[],
+                        sptIndex const mats_order[], sptIndex const mode, const int tk);
+int sptCudaMTTKRP(sptSparseTensor const *const X, sptMatrix *mats[], sptIndex *const mats_order,
+                  sptIndex const mode, sptIndex const impl_num);
+int sptCudaMTTKRPOneKernel(sptSparseTensor const *const X, sptMatrix **const mats, sptIndex *const mats_order,
+                           sptIndex const mode, sptIndex const impl_num);
+int sptMTTKRPHiCOO(sptSparseTensorHiCOO const *const hitsr, sptMatrix *mats[], sptIndex const mats_order[],
+                   sptIndex const mode);
+int sptOmpMTTKRPHiCOO(sptSparseTensorHiCOO const *const hitsr, sptMatrix *mats[], sptIndex const mats_order[],
+                      sptIndex const mode, const int nt);
+
+/* ------------------------------------------------------ Kruskal / CP-ALS -- */
+int  sptNewKruskalTensor(sptKruskalTensor *ktsr, sptIndex nmodes, const sptIndex ndims[], sptIndex rank);
+void sptFreeKruskalTensor(sptKruskalTensor *ktsr);
+
+/* One CP-ALS run from caller-initialised factors mats[0..nmodes-1] (and a
+ * scratch mats[nmodes] with max_dim rows); returns the last fit
+ * (src/sptensor/cpd.c:32-137). */
+double CpdAlsStep(sptSparseTensor const *const spten, sptIndex const rank, sptIndex const niters,
+                  double const tol, sptMatrix **mats, sptValue *const lambda);
+int sptCpdAls(sptSparseTensor const *const spten, sptIndex const rank, sptIndex const niters,
+              double const tol, sptKruskalTensor *ktensor);
+int sptOmpCpdAls(sptSparseTensor const *const spten, sptIndex const rank, sptIndex const niters,
+                 double const tol, const int tk, const int use_reduce, sptKruskalTensor *ktensor);
+int sptCudaCpdAls(sptSparseTensor const *const spten, sptIndex const rank, sptIndex const niters,
+                  double const tol, sptKruskalTensor *ktensor);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PARTI_H */

@@ -1,0 +1,95 @@
+/*
+ * sptgb.h -- GB300 extension API of the sparse MTTKRP / CP-ALS library.
+ *
+ * ParTI.h keeps the reference's host-buffer calling convention: every call
+ * moves its inputs to the GPU and its result back.  The functions here let a
+ * caller keep a tensor, its per-mode segmented copies and the factor
+ * matrices resident in HBM and call the same kernels on device pointers and a
+ * caller-chosen CUDA stream (passed as void* so that this header does not
+ * need the CUDA headers).  Nothing here has a counterpart in the reference.
+ */
+#ifndef SPTGB_H
+#define SPTGB_H
+
+#include "ParTI.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------ library -- */
+const char *sptgbVersion(void);
+/* Selects the device and creates the library stream; called lazily by every
+ * entry point, so calling it is optional. */
+int   sptgbInit(int device);
+/* The stream the ParTI.h entry points run on (a cudaStream_t). */
+void *sptgbStream(void);
+/* Kernels launched by this library since it was loaded. */
+uint64_t sptgbLaunchCount(void);
+/* Seed for sptRandomizeMatrix and for the factor initialisation of
+ * sptCpdAls (the reference seeds with time(NULL), matrix.c:69). */
+void  sptgbSetSeed(uint64_t seed);
+
+/* ------------------------------------------- device-resident COO tensor --
+ * A COO tensor uploaded once.  sptgbCooPrepareMode builds, on the device,
+ * the copy sorted by `mode` (mode first, then the remaining modes in
+ * ascending order: sptSparseTensorSortIndexCustomOrder's order) together
+ * with its segment data; sptgbCooMTTKRP then runs the segmented kernel on
+ * it.  d_mats[m] (m < nmodes) are device factor matrices of ndims[m] rows
+ * and `stride` floats per row; d_out receives ndims[mode] rows. */
+typedef struct sptgbCoo sptgbCoo;
+int  sptgbCooCreate(sptgbCoo **out, const sptSparseTensor *X, void *stream);
+int  sptgbCooPrepareMode(sptgbCoo *t, sptIndex mode, void *stream);
+int  sptgbCooMTTKRP(sptgbCoo *t, sptIndex mode, const sptIndex *mats_order,
+                    const float *const *d_mats, sptIndex rank, sptIndex stride,
+                    float *d_out, void *stream);
+/* BF16 factor storage, FP32 accumulation: d_mats_bf16[m] hold bf16 rows of
+ * `stride` elements (uint16_t bit patterns). */
+int  sptgbCooMTTKRPBf16(sptgbCoo *t, sptIndex mode, const sptIndex *mats_order,
+                        const uint16_t *const *d_mats_bf16, sptIndex rank, sptIndex stride,
+                        float *d_out, void *stream);
+sptNnzIndex sptgbCooNnz(const sptgbCoo *t);
+size_t      sptgbCooDeviceBytes(const sptgbCoo *t);
+/* Time of the last sptgbCooMTTKRP kernel sequence on its stream (ms),
+ * measured with CUDA events when timing is enabled. */
+void  sptgbCooSetTiming(sptgbCoo *t, int enable);
+float sptgbCooLastKernelMs(const sptgbCoo *t);
+void  sptgbCooFree(sptgbCoo *t);
+
+/* ----------------------------------------------------- synthetic tensors --
+ * Seeded generator shared by the tests and the benchmark (SplitMix64
+ * counter streams; inverse-CDF truncated Zipf; Box-Muller normals). */
+enum { SPTGB_DIST_UNIFORM = 0, SPTGB_DIST_ZIPF = 1 };
+enum { SPTGB_VAL_U01 = 0, SPTGB_VAL_UPM1 = 1, SPTGB_VAL_LOGNORMAL = 2, SPTGB_VAL_PLANTED = 3 };
+typedef struct {
+    uint64_t seed;
+    sptIndex nmodes;
+    sptIndex ndims[8];
+    int      coord_dist[8];   /* SPTGB_DIST_* per mode */
+    double   zipf_s[8];       /* Zipf exponent per mode */
+    uint64_t count;           /* draws (merge=1) or exact unique nnz (merge=0) */
+    int      merge_duplicates;/* 1: duplicate draws summed; 0: deduplicate and top up */
+    int      value_dist;      /* SPTGB_VAL_* */
+    sptIndex planted_rank;    /* SPTGB_VAL_PLANTED: rank of the planted model */
+    uint64_t planted_seed;    /* seed of the planted factors, U[0,1) */
+    double   noise_sigma;     /* Gaussian noise added to planted values */
+} sptgbGenSpec;
+/* Fills X (which must be uninitialised) with the generated tensor, sorted
+ * lexicographically (mode 0 most significant). */
+int sptgbGenerate(sptSparseTensor *X, const sptgbGenSpec *spec);
+/* U[lo,hi) fill of rows x ncols (padding columns set to 0), seeded by
+ * (seed, stream_id). */
+int sptgbFillMatrix(sptMatrix *mtx, uint64_t seed, uint64_t stream_id, float lo, float hi);
+
+/* --------------------------------------------------- CP-ALS with traces --
+ * CpdAlsStep semantics from caller factors, returning the fit after every
+ * iteration in fits[0..niters) (NaN past an early stop) and the iteration
+ * count.  Fits are computed with the full symmetric Gram matrices. */
+int sptgbCpdAls(sptSparseTensor const *spten, sptIndex rank, sptIndex niters, double tol,
+                sptMatrix **mats, sptValue *lambda, double *fits, sptIndex *iters_done);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPTGB_H */

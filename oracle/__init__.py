@@ -1,0 +1,356 @@
+"""ORACLE -- test infrastructure only.
+
+Loads the CPU restatement of ParTI!'s MTTKRP / CP-ALS path (orc.c ->
+_build/liborc.so) and, where the reference sources exist, the reference
+itself (_ref/libparti_ref.so, built from its own sources by the Makefile).
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline arm use this
+package; the library under sptol_gb300/ never imports it.
+
+Arrays: coordinates are [N, nnz] uint32, values [nnz] float32, factor
+matrices float32 [ndims[m], stride] with stride = rank rounded up to 8.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORC_PATH = os.path.join(HERE, "_build", "liborc.so")
+REF_PATH = os.path.join(HERE, "_ref", "libparti_ref.so")
+REF_SRC = "/root/reference"
+
+u32p = C.POINTER(C.c_uint32)
+u64p = C.POINTER(C.c_uint64)
+f32p = C.POINTER(C.c_float)
+f64p = C.POINTER(C.c_double)
+u8p = C.POINTER(C.c_uint8)
+
+_ORC = None
+_REF = None
+
+
+def build(with_ref=None):
+    """Builds liborc.so, and the reference library when its sources exist."""
+    subprocess.run(["make", "-s", "-C", HERE, "orc"], check=True)
+    if with_ref is None:
+        with_ref = os.path.isdir(os.path.join(REF_SRC, "src"))
+    if with_ref:
+        subprocess.run(["make", "-s", "-j8", "-C", HERE, "ref", "REF=" + REF_SRC], check=True)
+
+
+def stride_of(rank):
+    return ((rank - 1) // 8 + 1) * 8
+
+
+class HiCOOOut(C.Structure):
+    _fields_ = [("nb", C.c_uint64), ("nk", C.c_uint64), ("ncptr", C.c_uint64), ("max_nnzb", C.c_uint64),
+                ("bptr", u64p), ("kptr", u64p), ("cptr", u64p), ("binds", u32p), ("einds", u8p),
+                ("nkiters", u32p), ("kschr_len", u32p), ("kschr", u32p)]
+
+
+def orc():
+    global _ORC
+    if _ORC is None:
+        if not os.path.exists(ORC_PATH):
+            build(with_ref=False)
+        L = C.CDLL(ORC_PATH)
+        L.orc_sort_lex.argtypes = [C.c_uint32, C.c_uint64, C.POINTER(u32p), u32p, u64p]
+        L.orc_sort_hicoo.argtypes = [C.c_uint32, C.c_uint64, C.POINTER(u32p), C.c_int, u64p]
+        L.orc_hicoo_build.argtypes = [C.c_uint32, u32p, C.c_uint64, C.POINTER(u32p), C.c_int, C.c_int,
+                                      C.POINTER(HiCOOOut)]
+        mt = [C.c_uint32, C.c_uint64, C.POINTER(u32p), f32p, C.POINTER(f32p), C.c_uint32, C.c_uint32, u32p,
+              C.c_uint32, C.c_uint32]
+        L.orc_mttkrp_f32.argtypes = mt + [f32p]
+        L.orc_mttkrp_f64.argtypes = mt + [f64p]
+        L.orc_omp_mttkrp_reduce.argtypes = mt + [f32p, C.c_int, f32p]
+        L.orc_mttkrp_hicoo_f32.argtypes = [C.c_uint32, C.c_uint64, u64p, C.POINTER(u32p), C.POINTER(u8p), f32p,
+                                           C.c_int, C.POINTER(f32p), C.c_uint32, C.c_uint32, u32p, C.c_uint32,
+                                           C.c_uint32, f32p]
+        L.orc_cpd_als_f64.argtypes = [C.c_uint32, u32p, C.c_uint64, C.POINTER(u32p), f32p, C.c_uint32, C.c_uint32,
+                                      C.c_double, C.POINTER(f32p), C.c_uint32, f32p, f64p, u32p]
+        L.orc_fit_exact.argtypes = [C.c_uint32, u32p, C.c_uint64, C.POINTER(u32p), f32p, C.c_uint32,
+                                    C.POINTER(f32p), C.c_uint32, f32p]
+        L.orc_fit_exact.restype = C.c_double
+        _ORC = L
+    return _ORC
+
+
+def ref_available():
+    return os.path.exists(REF_PATH) or os.path.isdir(os.path.join(REF_SRC, "src"))
+
+
+def ref():
+    """The reference library with its LAPACK calls forwarded to scipy's."""
+    global _REF
+    if _REF is None:
+        if not os.path.exists(REF_PATH):
+            build(with_ref=True)
+        L = C.CDLL(REF_PATH)
+        import scipy.linalg.cython_blas as cb
+        import scipy.linalg.cython_lapack as cl
+        get = C.pythonapi.PyCapsule_GetPointer
+        get.restype = C.c_void_p
+        get.argtypes = [C.py_object, C.c_char_p]
+        gname = C.pythonapi.PyCapsule_GetName
+        gname.restype = C.c_char_p
+        gname.argtypes = [C.py_object]
+
+        def fp(mod, name):
+            cap = mod.__pyx_capi__[name]
+            return get(cap, gname(cap))
+
+        L.ref_set_lapack.argtypes = [C.c_void_p] * 4
+        L.ref_set_lapack(fp(cb, "ssyrk"), fp(cl, "spotrf"), fp(cl, "spotrs"), fp(cl, "sgesv"))
+        L.ref_sort.argtypes = [C.c_uint32, u32p, C.c_uint64, C.POINTER(u32p), f32p, u32p]
+        L.ref_mttkrp.argtypes = [C.c_uint32, u32p, C.c_uint64, C.POINTER(u32p), f32p, C.c_uint32, C.POINTER(f32p),
+                                 C.c_uint32, u32p, C.c_uint32, f32p, C.c_int, C.c_int, C.c_int, f64p]
+        L.ref_hicoo.argtypes = [C.c_uint32, u32p, C.c_uint64, C.POINTER(u32p), f32p, C.c_int, C.c_int,
+                                C.POINTER(HiCOOOut)]
+        L.ref_mttkrp_hicoo.argtypes = [C.c_uint32, u32p, C.c_uint64, C.POINTER(u32p), f32p, C.c_int, C.c_int,
+                                       C.c_uint32, C.POINTER(f32p), C.c_uint32, u32p, C.c_uint32, f32p]
+        L.ref_cpd_trace.argtypes = [C.c_uint32, u32p, C.c_uint64, C.POINTER(u32p), f32p, C.c_uint32, C.c_uint32,
+                                    C.POINTER(f32p), C.c_uint32, C.POINTER(f32p), f32p, f64p, C.POINTER(f32p), f32p,
+                                    f64p]
+        _REF = L
+    return _REF
+
+
+# ----------------------------------------------------------------- helpers --
+def _u32(a):
+    a = np.ascontiguousarray(a, dtype=np.uint32)
+    return a, a.ctypes.data_as(u32p)
+
+
+def _rows(arrs, ptype, dtype):
+    arrs = [np.ascontiguousarray(a, dtype=dtype) for a in arrs]
+    p = (ptype * len(arrs))(*[a.ctypes.data_as(ptype) for a in arrs])
+    return arrs, p
+
+
+def _default_order(N, mode):
+    return [mode] + [(mode + i) % N for i in range(1, N)]
+
+
+def sort_lex(inds, order=None):
+    """Permutation sorting the nonzeros lexicographically in `order`."""
+    N, n = inds.shape
+    order = list(range(N)) if order is None else order
+    keep, ip = _rows(list(inds), u32p, np.uint32)
+    o, op = _u32(order)
+    perm = np.zeros(n, np.uint64)
+    orc().orc_sort_lex(N, n, ip, op, perm.ctypes.data_as(u64p))
+    return perm.astype(np.int64)
+
+
+def sort_hicoo(inds, sk_bits):
+    N, n = inds.shape
+    keep, ip = _rows(list(inds), u32p, np.uint32)
+    perm = np.zeros(n, np.uint64)
+    orc().orc_sort_hicoo(N, n, ip, sk_bits, perm.ctypes.data_as(u64p))
+    return perm.astype(np.int64)
+
+
+def _hicoo_alloc(N, n, ndims, sk_bits):
+    nrows = sum((d + (1 << sk_bits) - 1) >> sk_bits for d in ndims)
+    bufs = {
+        "bptr": np.zeros(n + 1, np.uint64), "kptr": np.zeros(n + 1, np.uint64),
+        "cptr": np.zeros(2 * n + 2, np.uint64), "binds": np.zeros(N * n, np.uint32),
+        "einds": np.zeros(N * n, np.uint8), "nkiters": np.zeros(N, np.uint32),
+        "kschr_len": np.zeros(nrows, np.uint32), "kschr": np.zeros(N * n, np.uint32),
+    }
+    o = HiCOOOut()
+    for k in ("bptr", "kptr", "cptr"):
+        setattr(o, k, bufs[k].ctypes.data_as(u64p))
+    for k in ("binds", "nkiters", "kschr_len", "kschr"):
+        setattr(o, k, bufs[k].ctypes.data_as(u32p))
+    o.einds = bufs["einds"].ctypes.data_as(u8p)
+    return bufs, o
+
+
+def _hicoo_trim(bufs, o, N, n):
+    nb, nk = int(o.nb), int(o.nk)
+    return {
+        "kptr": bufs["kptr"][: nk + 1].copy(), "cptr": bufs["cptr"][: int(o.ncptr)].copy(),
+        "bptr": bufs["bptr"][: nb + 1].copy(), "binds": bufs["binds"][: N * nb].reshape(N, nb).copy(),
+        "einds": bufs["einds"].reshape(N, n).copy(), "nkiters": bufs["nkiters"].copy(),
+        "kschr_len": bufs["kschr_len"].copy(), "kschr": bufs["kschr"][: N * nk].copy(),
+        "max_nnzb": int(o.max_nnzb),
+    }
+
+
+def hicoo_build(ndims, inds_sorted, sb_bits, sk_bits):
+    """HiCOO arrays from a COO already in HiCOO order (orc_sort_hicoo)."""
+    N, n = inds_sorted.shape
+    keep, ip = _rows(list(inds_sorted), u32p, np.uint32)
+    nd, ndp = _u32(ndims)
+    bufs, o = _hicoo_alloc(N, n, ndims, sk_bits)
+    orc().orc_hicoo_build(N, ndp, n, ip, sb_bits, sk_bits, C.byref(o))
+    return _hicoo_trim(bufs, o, N, n)
+
+
+def mttkrp(ndims, inds, vals, mats, rank, mode, order=None, precision="f32", tk=None):
+    """Sequential FP32 (reference order), FP64, or OpenMP-reduce FP32 MTTKRP."""
+    N, n = inds.shape
+    order = _default_order(N, mode) if order is None else order
+    stride = stride_of(rank)
+    keep, ip = _rows(list(inds), u32p, np.uint32)
+    mkeep, mp = _rows(mats, f32p, np.float32)
+    v = np.ascontiguousarray(vals, np.float32)
+    o, op = _u32(order)
+    rows = ndims[mode]
+    L = orc()
+    args = [N, n, ip, v.ctypes.data_as(f32p), mp, stride, rank, op, mode, rows]
+    if precision == "f64":
+        out = np.zeros((rows, stride), np.float64)
+        L.orc_mttkrp_f64(*args, out.ctypes.data_as(f64p))
+    elif precision == "omp":
+        tk = tk or os.cpu_count()
+        out = np.zeros((rows, stride), np.float32)
+        copies = np.zeros(tk * rows * stride, np.float32)
+        L.orc_omp_mttkrp_reduce(*args, out.ctypes.data_as(f32p), tk, copies.ctypes.data_as(f32p))
+    else:
+        out = np.zeros((rows, stride), np.float32)
+        L.orc_mttkrp_f32(*args, out.ctypes.data_as(f32p))
+    return out[:, :rank]
+
+
+def mttkrp_hicoo(ndims, h, vals, sb_bits, mats, rank, mode, order=None):
+    N = len(ndims)
+    order = _default_order(N, mode) if order is None else order
+    stride = stride_of(rank)
+    bk, bp = _rows(list(h["binds"]), u32p, np.uint32)
+    ek, ep = _rows(list(h["einds"]), u8p, np.uint8)
+    mkeep, mp = _rows(mats, f32p, np.float32)
+    v = np.ascontiguousarray(vals, np.float32)
+    bptr = np.ascontiguousarray(h["bptr"], np.uint64)
+    o, op = _u32(order)
+    out = np.zeros((ndims[mode], stride), np.float32)
+    orc().orc_mttkrp_hicoo_f32(N, len(bptr) - 1, bptr.ctypes.data_as(u64p), bp, ep, v.ctypes.data_as(f32p), sb_bits,
+                               mp, stride, rank, op, mode, ndims[mode], out.ctypes.data_as(f32p))
+    return out[:, :rank]
+
+
+def cpd_als(ndims, inds, vals, rank, niters, tol, init):
+    """FP64 CP-ALS restatement; init: list of [ndims[m], rank] float arrays."""
+    N, n = inds.shape
+    stride = stride_of(rank)
+    facs = []
+    for a in init:
+        f = np.zeros((a.shape[0], stride), np.float32)
+        f[:, :rank] = a
+        facs.append(f)
+    keep, ip = _rows(list(inds), u32p, np.uint32)
+    fkeep, fp = _rows(facs, f32p, np.float32)
+    nd, ndp = _u32(ndims)
+    v = np.ascontiguousarray(vals, np.float32)
+    lam = np.zeros(rank, np.float32)
+    fits = np.full(niters, np.nan)
+    done = C.c_uint32()
+    orc().orc_cpd_als_f64(N, ndp, n, ip, v.ctypes.data_as(f32p), rank, niters, tol, fp, stride,
+                          lam.ctypes.data_as(f32p), fits.ctypes.data_as(f64p), C.byref(done))
+    return [f[:, :rank].copy() for f in fkeep], lam, fits, int(done.value)
+
+
+def fit_exact(ndims, inds, vals, factors, lam):
+    N, n = inds.shape
+    rank = factors[0].shape[1]
+    stride = stride_of(rank)
+    facs = []
+    for a in factors:
+        f = np.zeros((a.shape[0], stride), np.float32)
+        f[:, :rank] = a
+        facs.append(f)
+    keep, ip = _rows(list(inds), u32p, np.uint32)
+    fkeep, fp = _rows(facs, f32p, np.float32)
+    nd, ndp = _u32(ndims)
+    v = np.ascontiguousarray(vals, np.float32)
+    l = np.ascontiguousarray(lam, np.float32)
+    return float(orc().orc_fit_exact(N, ndp, n, ip, v.ctypes.data_as(f32p), rank, fp, stride,
+                                     l.ctypes.data_as(f32p)))
+
+
+# ------------------------------------------------------- the reference --
+def ref_sort(ndims, inds, vals, order=None):
+    N, n = inds.shape
+    ik, ip = _rows([r.copy() for r in inds], u32p, np.uint32)
+    v = np.ascontiguousarray(vals, np.float32).copy()
+    nd, ndp = _u32(ndims)
+    op = None
+    if order is not None:
+        o, op = _u32(order)
+    ref().ref_sort(N, ndp, n, ip, v.ctypes.data_as(f32p), op)
+    return np.stack(ik), v
+
+
+def ref_mttkrp(ndims, inds, vals, mats, rank, mode, order=None, which=0, tk=1, reps=0):
+    N, n = inds.shape
+    order = _default_order(N, mode) if order is None else order
+    stride = stride_of(rank)
+    ik, ip = _rows(list(inds), u32p, np.uint32)
+    mk, mp = _rows(mats, f32p, np.float32)
+    v = np.ascontiguousarray(vals, np.float32)
+    nd, ndp = _u32(ndims)
+    o, op = _u32(order)
+    out = np.zeros((ndims[mode], stride), np.float32)
+    secs = C.c_double()
+    r = ref().ref_mttkrp(N, ndp, n, ip, v.ctypes.data_as(f32p), rank, mp, stride, op, mode,
+                         out.ctypes.data_as(f32p), which, tk, reps, C.byref(secs))
+    assert r == 0
+    return out[:, :rank], secs.value
+
+
+def ref_hicoo(ndims, inds, vals, sb_bits, sk_bits):
+    N, n = inds.shape
+    ik, ip = _rows([r.copy() for r in inds], u32p, np.uint32)
+    v = np.ascontiguousarray(vals, np.float32).copy()
+    nd, ndp = _u32(ndims)
+    bufs, o = _hicoo_alloc(N, n, ndims, sk_bits)
+    ref().ref_hicoo(N, ndp, n, ip, v.ctypes.data_as(f32p), sb_bits, sk_bits, C.byref(o))
+    return np.stack(ik), v, _hicoo_trim(bufs, o, N, n)
+
+
+def ref_mttkrp_hicoo(ndims, inds, vals, sb_bits, sk_bits, mats, rank, mode, order=None):
+    N, n = inds.shape
+    order = _default_order(N, mode) if order is None else order
+    stride = stride_of(rank)
+    ik, ip = _rows([r.copy() for r in inds], u32p, np.uint32)
+    mk, mp = _rows(mats, f32p, np.float32)
+    v = np.ascontiguousarray(vals, np.float32)
+    nd, ndp = _u32(ndims)
+    o, op = _u32(order)
+    out = np.zeros((ndims[mode], stride), np.float32)
+    ref().ref_mttkrp_hicoo(N, ndp, n, ip, v.ctypes.data_as(f32p), sb_bits, sk_bits, rank, mp, stride, op, mode,
+                           out.ctypes.data_as(f32p))
+    return out[:, :rank]
+
+
+def ref_cpd_trace(ndims, inds, vals, rank, niters, init):
+    N, n = inds.shape
+    stride = stride_of(rank)
+
+    def padded():
+        out = []
+        for a in init:
+            f = np.zeros((a.shape[0], stride), np.float32)
+            f[:, :rank] = a
+            out.append(f)
+        return out
+
+    ik, ip = _rows(list(inds), u32p, np.uint32)
+    v = np.ascontiguousarray(vals, np.float32)
+    nd, ndp = _u32(ndims)
+    ink, inp = _rows(padded(), f32p, np.float32)
+    lk, lp = _rows(padded(), f32p, np.float32)
+    sk, sp = _rows(padded(), f32p, np.float32)
+    lam_loop = np.zeros(rank, np.float32)
+    lam_step = np.zeros(rank, np.float32)
+    fits = np.zeros(niters)
+    step_fit = C.c_double()
+    ref().ref_cpd_trace(N, ndp, n, ip, v.ctypes.data_as(f32p), rank, niters, inp, stride, lp,
+                        lam_loop.ctypes.data_as(f32p), fits.ctypes.data_as(f64p), sp, lam_step.ctypes.data_as(f32p),
+                        C.byref(step_fit))
+    return {
+        "loop_factors": [f[:, :rank].copy() for f in lk], "loop_lambda": lam_loop, "fits": fits,
+        "step_factors": [f[:, :rank].copy() for f in sk], "step_lambda": lam_step, "step_fit": step_fit.value,
+    }

@@ -1,0 +1,579 @@
+/*
+ * ORACLE -- TEST INFRASTRUCTURE ONLY.
+ *
+ * CPU restatement of ParTI!'s sparse MTTKRP / CP-ALS path, used by tests/,
+ * __graft_entry__.smoke() and bench.py's CPU-baseline arm as the checker.
+ * The library (libParTI.so) never links, loads or calls this code.
+ *
+ * Every function restates one reference routine, cited by file:line of the
+ * ParTI! sources.  Parity pinning: tests/golden/ holds outputs of the
+ * reference itself (compiled from its own sources by oracle/Makefile, target
+ * `ref`), and tests/test_oracle_golden.py checks these functions against them.
+ *
+ * Interfaces use flat arrays: inds[m] points at the nnz mode-m coordinates,
+ * factor matrices are row-major with `stride` floats per row.
+ */
+#include <math.h>
+#include <omp.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define ORC_MAX_MODES 8
+
+/* ------------------------------------------------------------- sorting --
+ * Merge sort of a permutation under a comparison; the reference's orders are
+ * total on unique coordinates, so any correct sort yields its permutation. */
+typedef int (*orc_cmp)(const void *ctx, uint64_t a, uint64_t b);
+
+static void msort(uint64_t *p, uint64_t *tmp, uint64_t n, orc_cmp cmp, const void *ctx) {
+    if (n < 2) return;
+    const uint64_t h = n / 2;
+    msort(p, tmp, h, cmp, ctx);
+    msort(p + h, tmp, n - h, cmp, ctx);
+    uint64_t i = 0, j = h, k = 0;
+    while (i < h && j < n) tmp[k++] = cmp(ctx, p[j], p[i]) < 0 ? p[j++] : p[i++];
+    while (i < h) tmp[k++] = p[i++];
+    while (j < n) tmp[k++] = p[j++];
+    memcpy(p, tmp, n * sizeof *p);
+}
+
+typedef struct {
+    uint32_t nmodes;
+    const uint32_t *const *inds;
+    const uint32_t *order;
+    int sk_bits;
+} sort_ctx;
+
+/* sort.c:629-646 (with the mode order of SortIndexCustomOrder, :523-552). */
+static int cmp_lex(const void *c, uint64_t a, uint64_t b) {
+    const sort_ctx *s = (const sort_ctx *)c;
+    for (uint32_t i = 0; i < s->nmodes; ++i) {
+        const uint32_t m = s->order[i];
+        const uint32_t x = s->inds[m][a], y = s->inds[m][b];
+        if (x < y) return -1;
+        if (x > y) return 1;
+    }
+    return 0;
+}
+
+int orc_sort_lex(uint32_t nmodes, uint64_t nnz, const uint32_t *const *inds, const uint32_t *order, uint64_t *perm) {
+    uint64_t *tmp = (uint64_t *)malloc((nnz ? nnz : 1) * sizeof *tmp);
+    if (!tmp) return 1;
+    for (uint64_t i = 0; i < nnz; ++i) perm[i] = i;
+    sort_ctx c = {nmodes, inds, order, 0};
+    msort(perm, tmp, nnz, cmp_lex, &c);
+    free(tmp);
+    return 0;
+}
+
+/* Byte-spread tables of sort.c:55-164 as a computation: bit i of the byte
+ * goes to bit 3i (z), 3i+1 (y), 3i+2 (x). */
+static uint32_t spread3(uint32_t byte) {
+    uint32_t r = 0;
+    for (int i = 0; i < 8; ++i) r |= ((byte >> i) & 1u) << (3 * i);
+    return r;
+}
+
+/* sort.c:754-795: the 128-bit key built byte by byte from the top; the
+ * highest byte's contribution is shifted past bit 127. */
+static unsigned __int128 morton3(uint32_t x, uint32_t y, uint32_t z) {
+    unsigned __int128 k;
+    k = (unsigned __int128)((spread3((z >> 24) & 0xFF)) | (spread3((y >> 24) & 0xFF) << 1) |
+                            (spread3((x >> 24) & 0xFF) << 2));
+    k = (k << 72) | (spread3((z >> 16) & 0xFF) | (spread3((y >> 16) & 0xFF) << 1) | (spread3((x >> 16) & 0xFF) << 2));
+    k = (k << 48) | (spread3((z >> 8) & 0xFF) | (spread3((y >> 8) & 0xFF) << 1) | (spread3((x >> 8) & 0xFF) << 2));
+    k = (k << 24) | (spread3(z & 0xFF) | (spread3(y & 0xFF) << 1) | (spread3(x & 0xFF) << 2));
+    return k;
+}
+
+/* sort.c:852-917: every coordinate bit i to bit 4i; key = w | z<<1 | y<<2 | x<<3. */
+static unsigned __int128 spread4(uint32_t v) {
+    unsigned __int128 r = 0;
+    for (int i = 0; i < 32; ++i) r |= (unsigned __int128)((v >> i) & 1u) << (4 * i);
+    return r;
+}
+static unsigned __int128 morton4(uint32_t x, uint32_t y, uint32_t z, uint32_t w) {
+    return spread4(w) | (spread4(z) << 1) | (spread4(y) << 2) | (spread4(x) << 3);
+}
+
+/* Row-block compare (sort.c:713-737) then Morton compare (sort.c:748-995):
+ * the order left by spt_PreprocessSparseTensor (hicoo/convert.c:160-226). */
+static int cmp_hicoo(const void *c, uint64_t a, uint64_t b) {
+    const sort_ctx *s = (const sort_ctx *)c;
+    for (uint32_t m = 0; m < s->nmodes; ++m) {
+        const uint32_t x = s->inds[m][a] >> s->sk_bits, y = s->inds[m][b] >> s->sk_bits;
+        if (x < y) return -1;
+        if (x > y) return 1;
+    }
+    unsigned __int128 ka = 0, kb = 0;
+    if (s->nmodes == 3) {
+        ka = morton3(s->inds[0][a], s->inds[1][a], s->inds[2][a]);
+        kb = morton3(s->inds[0][b], s->inds[1][b], s->inds[2][b]);
+    } else if (s->nmodes == 4) {
+        ka = morton4(s->inds[0][a], s->inds[1][a], s->inds[2][a], s->inds[3][a]);
+        kb = morton4(s->inds[0][b], s->inds[1][b], s->inds[2][b], s->inds[3][b]);
+    }
+    return ka < kb ? -1 : (ka > kb ? 1 : 0);
+}
+
+int orc_sort_hicoo(uint32_t nmodes, uint64_t nnz, const uint32_t *const *inds, int sk_bits, uint64_t *perm) {
+    uint64_t *tmp = (uint64_t *)malloc((nnz ? nnz : 1) * sizeof *tmp);
+    if (!tmp) return 1;
+    for (uint64_t i = 0; i < nnz; ++i) perm[i] = i;
+    sort_ctx c = {nmodes, inds, NULL, sk_bits};
+    msort(perm, tmp, nnz, cmp_hicoo, &c);
+    free(tmp);
+    return 0;
+}
+
+/* ---------------------------------------------------------- HiCOO build --
+ * hicoo/convert.c:103-146 (kschr), :237-288 (kernel pointers), :300-497
+ * (blocks, chunks, elements), on a COO already in HiCOO order.  Outputs
+ * (caller-sized: nb <= nnz, nk <= nnz, ncptr <= nb + nk + 1, kschr
+ * nmodes * nk entries, kschr_len sum over modes of ceil(ndims/2^sk)). */
+typedef struct {
+    uint64_t nb, nk, ncptr, max_nnzb;
+    uint64_t *bptr, *kptr, *cptr;
+    uint32_t *binds;   /* [nmodes][nb] */
+    uint8_t *einds;    /* [nmodes][nnz] */
+    uint32_t *nkiters; /* [nmodes] */
+    uint32_t *kschr_len;
+    uint32_t *kschr;
+} orc_hicoo;
+
+int orc_hicoo_build(uint32_t nmodes, const uint32_t *ndims, uint64_t nnz, const uint32_t *const *inds, int sb_bits,
+                    int sk_bits, orc_hicoo *h) {
+    const uint64_t sc = 1ull << 14;
+    if (nnz == 0) return 1;
+    /* kernel starts (convert.c:237-288) */
+    uint64_t *kstart = (uint64_t *)malloc((nnz + 1) * sizeof *kstart);
+    uint64_t nk = 0;
+    for (uint64_t z = 0; z < nnz; ++z) {
+        int diff = (z == 0);
+        for (uint32_t m = 0; m < nmodes && z; ++m) diff |= (inds[m][z] >> sk_bits) != (inds[m][z - 1] >> sk_bits);
+        if (diff) kstart[nk++] = z;
+    }
+    kstart[nk] = nnz;
+    /* kschr (convert.c:117-143) */
+    uint32_t *row_off = (uint32_t *)calloc(ORC_MAX_MODES, sizeof(uint32_t));
+    uint64_t tot_rows = 0;
+    for (uint32_t m = 0; m < nmodes; ++m) {
+        row_off[m] = (uint32_t)tot_rows;
+        tot_rows += ((uint64_t)ndims[m] + (1ull << sk_bits) - 1) >> sk_bits;
+    }
+    memset(h->kschr_len, 0, tot_rows * sizeof(uint32_t));
+    for (uint64_t k = 0; k < nk; ++k)
+        for (uint32_t m = 0; m < nmodes; ++m) h->kschr_len[row_off[m] + (inds[m][kstart[k]] >> sk_bits)]++;
+    /* entries in kernel order within each kernel row */
+    uint64_t *fill = (uint64_t *)calloc(tot_rows + 1, sizeof(uint64_t));
+    for (uint64_t r = 0; r < tot_rows; ++r) fill[r + 1] = fill[r] + h->kschr_len[r];
+    for (uint64_t k = 0; k < nk; ++k)
+        for (uint32_t m = 0; m < nmodes; ++m) {
+            const uint64_t r = row_off[m] + (inds[m][kstart[k]] >> sk_bits);
+            h->kschr[fill[r]++] = (uint32_t)k;
+        }
+    for (uint32_t m = 0; m < nmodes; ++m) {
+        uint32_t mx = 0;
+        const uint64_t kn = ((uint64_t)ndims[m] + (1ull << sk_bits) - 1) >> sk_bits;
+        for (uint64_t i = 0; i < kn; ++i)
+            if (h->kschr_len[row_off[m] + i] > mx) mx = h->kschr_len[row_off[m] + i];
+        h->nkiters[m] = mx;
+    }
+    /* element / block / chunk emission (convert.c:372-472) */
+    uint64_t nb = 1, ne = 0, chunk = 0, nc = 0;
+    uint32_t prior[ORC_MAX_MODES];
+    for (uint32_t m = 0; m < nmodes; ++m) {
+        prior[m] = inds[m][0] >> sb_bits;
+        h->binds[(uint64_t)m * nnz + 0] = prior[m];
+    }
+    h->bptr[0] = 0;
+    uint64_t nbptr = 1;
+    for (uint64_t k = 0; k < nk; ++k) {
+        const uint64_t nb_tmp = k == 0 ? 0 : nb;
+        h->kptr[k] = nb_tmp;
+        h->cptr[nc++] = nb_tmp;
+        chunk = 0;
+        for (uint64_t z = kstart[k]; z < kstart[k + 1]; ++z) {
+            int same = 1;
+            uint32_t blk[ORC_MAX_MODES];
+            for (uint32_t m = 0; m < nmodes; ++m) {
+                blk[m] = inds[m][z] >> sb_bits;
+                h->einds[(uint64_t)m * nnz + z] = (uint8_t)(inds[m][z] - (blk[m] << sb_bits));
+                same &= blk[m] == prior[m];
+            }
+            if (same) {
+                ++ne;
+            } else {
+                h->bptr[nbptr++] = (uint64_t)(uint32_t)z;
+                for (uint32_t m = 0; m < nmodes; ++m) {
+                    h->binds[(uint64_t)m * nnz + nb] = blk[m];
+                    prior[m] = blk[m];
+                }
+                if (chunk + ne >= sc) {
+                    h->cptr[nc++] = nb;
+                    chunk = 0;
+                } else {
+                    chunk += ne;
+                }
+                ++nb;
+                ne = 1;
+            }
+        }
+    }
+    h->kptr[nk] = nbptr;
+    h->cptr[nc++] = nbptr;
+    h->bptr[nbptr] = nnz;
+    h->nb = nb;
+    h->nk = nk;
+    h->ncptr = nc;
+    uint64_t mx = h->bptr[1] - h->bptr[0];
+    for (uint64_t b = 0; b < nb; ++b)
+        if (h->bptr[b + 1] - h->bptr[b] > mx) mx = h->bptr[b + 1] - h->bptr[b];
+    h->max_nnzb = mx;
+    /* binds were written with a row length of nnz; compact to nb */
+    for (uint32_t m = 1; m < nmodes; ++m) memmove(h->binds + (uint64_t)m * nb, h->binds + (uint64_t)m * nnz, nb * 4);
+    free(kstart);
+    free(row_off);
+    free(fill);
+    return 0;
+}
+
+/* ------------------------------------------------------------- MTTKRP --
+ * mttkrp.c:39-115 (order >= 4) and :118-177 (3-D): per nonzero the product
+ * entry * F[o1][i1] * F[o2][i2] ... (left to right), added to the output
+ * row in nonzero order, FP32. */
+void orc_mttkrp_f32(uint32_t nmodes, uint64_t nnz, const uint32_t *const *inds, const float *vals,
+                    const float *const *mats, uint32_t stride, uint32_t R, const uint32_t *mats_order, uint32_t mode,
+                    uint32_t out_rows, float *out) {
+    memset(out, 0, (size_t)out_rows * stride * sizeof(float));
+    float scratch[1024];
+    for (uint64_t x = 0; x < nnz; ++x) {
+        const float entry = vals[x];
+        const uint32_t o1 = mats_order[1];
+        const float *r1 = mats[o1] + (size_t)inds[o1][x] * stride;
+        for (uint32_t r = 0; r < R; ++r) scratch[r] = entry * r1[r];
+        for (uint32_t i = 2; i < nmodes; ++i) {
+            const uint32_t oi = mats_order[i];
+            const float *ri = mats[oi] + (size_t)inds[oi][x] * stride;
+            for (uint32_t r = 0; r < R; ++r) scratch[r] *= ri[r];
+        }
+        float *o = out + (size_t)inds[mode][x] * stride;
+        for (uint32_t r = 0; r < R; ++r) o[r] += scratch[r];
+    }
+}
+
+/* Same loop in FP64 (products and sums), the precision reference. */
+void orc_mttkrp_f64(uint32_t nmodes, uint64_t nnz, const uint32_t *const *inds, const float *vals,
+                    const float *const *mats, uint32_t stride, uint32_t R, const uint32_t *mats_order, uint32_t mode,
+                    uint32_t out_rows, double *out) {
+    memset(out, 0, (size_t)out_rows * stride * sizeof(double));
+    double scratch[1024];
+    for (uint64_t x = 0; x < nnz; ++x) {
+        const double entry = vals[x];
+        const uint32_t o1 = mats_order[1];
+        const float *r1 = mats[o1] + (size_t)inds[o1][x] * stride;
+        for (uint32_t r = 0; r < R; ++r) scratch[r] = entry * (double)r1[r];
+        for (uint32_t i = 2; i < nmodes; ++i) {
+            const uint32_t oi = mats_order[i];
+            const float *ri = mats[oi] + (size_t)inds[oi][x] * stride;
+            for (uint32_t r = 0; r < R; ++r) scratch[r] *= (double)ri[r];
+        }
+        double *o = out + (size_t)inds[mode][x] * stride;
+        for (uint32_t r = 0; r < R; ++r) o[r] += scratch[r];
+    }
+}
+
+/* mttkrp_omp.c:401-476: privatised per-thread outputs, static schedule over
+ * nonzeros, then a row-parallel reduction over threads. */
+void orc_omp_mttkrp_reduce(uint32_t nmodes, uint64_t nnz, const uint32_t *const *inds, const float *vals,
+                           const float *const *mats, uint32_t stride, uint32_t R, const uint32_t *mats_order,
+                           uint32_t mode, uint32_t out_rows, float *out, int tk, float *copies) {
+    memset(out, 0, (size_t)out_rows * stride * sizeof(float));
+    const size_t csz = (size_t)out_rows * stride;
+    memset(copies, 0, (size_t)tk * csz * sizeof(float));
+#pragma omp parallel for schedule(static) num_threads(tk)
+    for (uint64_t x = 0; x < nnz; ++x) {
+        float *cp = copies + (size_t)omp_get_thread_num() * csz;
+        float scratch[1024];
+        const float entry = vals[x];
+        const uint32_t o1 = mats_order[1];
+        const float *r1 = mats[o1] + (size_t)inds[o1][x] * stride;
+        for (uint32_t r = 0; r < R; ++r) scratch[r] = entry * r1[r];
+        for (uint32_t i = 2; i < nmodes; ++i) {
+            const uint32_t oi = mats_order[i];
+            const float *ri = mats[oi] + (size_t)inds[oi][x] * stride;
+            for (uint32_t r = 0; r < R; ++r) scratch[r] *= ri[r];
+        }
+        float *o = cp + (size_t)inds[mode][x] * stride;
+        for (uint32_t r = 0; r < R; ++r) o[r] += scratch[r];
+    }
+#pragma omp parallel for schedule(static) num_threads(tk)
+    for (uint32_t i = 0; i < out_rows; ++i)
+        for (int t = 0; t < tk; ++t)
+            for (uint32_t r = 0; r < R; ++r) out[(size_t)i * stride + r] += copies[(size_t)t * csz + (size_t)i * stride + r];
+}
+
+/* hicoo/mttkrp.c:53-144: kernels -> blocks -> elements, coordinates
+ * (binds << sb_bits) + einds. */
+void orc_mttkrp_hicoo_f32(uint32_t nmodes, uint64_t nb, const uint64_t *bptr, const uint32_t *const *binds,
+                          const uint8_t *const *einds, const float *vals, int sb_bits, const float *const *mats,
+                          uint32_t stride, uint32_t R, const uint32_t *mats_order, uint32_t mode, uint32_t out_rows,
+                          float *out) {
+    memset(out, 0, (size_t)out_rows * stride * sizeof(float));
+    float scratch[1024];
+    uint32_t c[ORC_MAX_MODES];
+    for (uint64_t b = 0; b < nb; ++b) {
+        for (uint64_t z = bptr[b]; z < bptr[b + 1]; ++z) {
+            for (uint32_t m = 0; m < nmodes; ++m) c[m] = (binds[m][b] << sb_bits) + einds[m][z];
+            const float entry = vals[z];
+            const uint32_t o1 = mats_order[1];
+            const float *r1 = mats[o1] + (size_t)c[o1] * stride;
+            for (uint32_t r = 0; r < R; ++r) scratch[r] = entry * r1[r];
+            for (uint32_t i = 2; i < nmodes; ++i) {
+                const uint32_t oi = mats_order[i];
+                const float *ri = mats[oi] + (size_t)c[oi] * stride;
+                for (uint32_t r = 0; r < R; ++r) scratch[r] *= ri[r];
+            }
+            float *o = out + (size_t)c[mode] * stride;
+            for (uint32_t r = 0; r < R; ++r) o[r] += scratch[r];
+        }
+    }
+}
+
+/* -------------------------------------------------------------- CP-ALS --
+ * cpd.c:32-137 restated in FP64 with a correct fit:
+ *   Grams A^T A (full), per iteration and mode: MTTKRP, solve with the
+ *   Hadamard of the other Grams (Cholesky; Gaussian elimination with partial
+ *   pivoting when not positive definite, as matrix_solver.c:48-80 falls back
+ *   from spotrf_ to sgesv_), 2-norm at iteration 0 else max-norm clamped to
+ *   >= 1 (matrix.c:390-554), new Gram; then
+ *   fit = 1 - r / ||X|| with r = sqrt(res) if res > 0 else res,
+ *   res = ||X||^2 + ||K||^2 - 2 <X,K> (ktensor.c:102-120), ||K||^2 from full
+ *   symmetric Grams, <X,K> from the last mode's MTTKRP (ktensor.c:173-257);
+ *   GetFinalLambda (matrix.c:557-573) at the end.
+ * Factors enter and leave as FP32 arrays of ndims[m] x stride. */
+static int solve_rows_f64(double *H, int R, double *X, uint64_t nrows, int ld) {
+    /* Cholesky H = L L^T in place (lower). */
+    double *L = (double *)malloc((size_t)R * R * sizeof(double));
+    memcpy(L, H, (size_t)R * R * sizeof(double));
+    int spd = 1;
+    for (int k = 0; k < R && spd; ++k) {
+        double d = L[k * R + k];
+        for (int j = 0; j < k; ++j) d -= L[k * R + j] * L[k * R + j];
+        if (!(d > 0.0)) {
+            spd = 0;
+            break;
+        }
+        L[k * R + k] = sqrt(d);
+        for (int i = k + 1; i < R; ++i) {
+            double s = L[i * R + k];
+            for (int j = 0; j < k; ++j) s -= L[i * R + j] * L[k * R + j];
+            L[i * R + k] = s / L[k * R + k];
+        }
+    }
+    if (spd) {
+        for (uint64_t i = 0; i < nrows; ++i) {
+            double *x = X + i * ld;
+            for (int r = 0; r < R; ++r) {
+                double s = x[r];
+                for (int j = 0; j < r; ++j) s -= L[r * R + j] * x[j];
+                x[r] = s / L[r * R + r];
+            }
+            for (int r = R - 1; r >= 0; --r) {
+                double s = x[r];
+                for (int j = r + 1; j < R; ++j) s -= L[j * R + r] * x[j];
+                x[r] = s / L[r * R + r];
+            }
+        }
+        free(L);
+        return 0;
+    }
+    /* LU with partial pivoting of H, solve H x = m per row. */
+    int *piv = (int *)malloc(R * sizeof(int));
+    memcpy(L, H, (size_t)R * R * sizeof(double));
+    for (int k = 0; k < R; ++k) {
+        int p = k;
+        for (int i = k + 1; i < R; ++i)
+            if (fabs(L[i * R + k]) > fabs(L[p * R + k])) p = i;
+        piv[k] = p;
+        if (p != k)
+            for (int j = 0; j < R; ++j) {
+                double t = L[k * R + j];
+                L[k * R + j] = L[p * R + j];
+                L[p * R + j] = t;
+            }
+        if (L[k * R + k] != 0.0)
+            for (int i = k + 1; i < R; ++i) {
+                L[i * R + k] /= L[k * R + k];
+                for (int j = k + 1; j < R; ++j) L[i * R + j] -= L[i * R + k] * L[k * R + j];
+            }
+    }
+    for (uint64_t i = 0; i < nrows; ++i) {
+        double *x = X + i * ld;
+        for (int k = 0; k < R; ++k) {
+            double t = x[k];
+            x[k] = x[piv[k]];
+            x[piv[k]] = t;
+        }
+        for (int r = 0; r < R; ++r)
+            for (int j = 0; j < r; ++j) x[r] -= L[r * R + j] * x[j];
+        for (int r = R - 1; r >= 0; --r) {
+            for (int j = r + 1; j < R; ++j) x[r] -= L[r * R + j] * x[j];
+            x[r] /= L[r * R + r];
+        }
+    }
+    free(piv);
+    free(L);
+    return 1;
+}
+
+static void gram_f64(const double *A, uint64_t nrows, int R, int ld, double *G) {
+    memset(G, 0, (size_t)R * R * sizeof(double));
+    for (uint64_t i = 0; i < nrows; ++i)
+        for (int p = 0; p < R; ++p)
+            for (int q = p; q < R; ++q) G[p * R + q] += A[i * ld + p] * A[i * ld + q];
+    for (int p = 0; p < R; ++p)
+        for (int q = 0; q < p; ++q) G[p * R + q] = G[q * R + p];
+}
+
+int orc_cpd_als_f64(uint32_t nmodes, const uint32_t *ndims, uint64_t nnz, const uint32_t *const *inds,
+                    const float *vals, uint32_t R, uint32_t niters, double tol, float *const *factors, uint32_t stride,
+                    float *lambda_out, double *fits, uint32_t *iters_done) {
+    double *A[ORC_MAX_MODES], *G[ORC_MAX_MODES];
+    uint32_t maxd = 0;
+    for (uint32_t m = 0; m < nmodes; ++m) {
+        A[m] = (double *)malloc((size_t)ndims[m] * R * sizeof(double));
+        for (uint64_t i = 0; i < ndims[m]; ++i)
+            for (uint32_t r = 0; r < R; ++r) A[m][i * R + r] = factors[m][i * stride + r];
+        G[m] = (double *)malloc((size_t)R * R * sizeof(double));
+        gram_f64(A[m], ndims[m], (int)R, (int)R, G[m]);
+        if (ndims[m] > maxd) maxd = ndims[m];
+    }
+    double *M = (double *)malloc((size_t)maxd * R * sizeof(double));
+    double *H = (double *)malloc((size_t)R * R * sizeof(double));
+    double *lam = (double *)malloc(R * sizeof(double));
+    double *sc = (double *)malloc(1024 * sizeof(double));
+    double normX2 = 0.0;
+    for (uint64_t x = 0; x < nnz; ++x) normX2 += (double)vals[x] * vals[x];
+    double oldfit = 0.0;
+    uint32_t done = 0;
+    for (uint32_t it = 0; it < niters; ++it) {
+        for (uint32_t m = 0; m < nmodes; ++m) {
+            uint32_t order[ORC_MAX_MODES];
+            order[0] = m;
+            for (uint32_t i = 1; i < nmodes; ++i) order[i] = (m + i) % nmodes;
+            memset(M, 0, (size_t)ndims[m] * R * sizeof(double));
+            for (uint64_t x = 0; x < nnz; ++x) {
+                for (uint32_t r = 0; r < R; ++r) sc[r] = vals[x] * A[order[1]][(size_t)inds[order[1]][x] * R + r];
+                for (uint32_t i = 2; i < nmodes; ++i)
+                    for (uint32_t r = 0; r < R; ++r) sc[r] *= A[order[i]][(size_t)inds[order[i]][x] * R + r];
+                double *o = M + (size_t)inds[m][x] * R;
+                for (uint32_t r = 0; r < R; ++r) o[r] += sc[r];
+            }
+            for (uint32_t e = 0; e < R * R; ++e) {
+                double v = 1.0;
+                for (uint32_t k = 1; k < nmodes; ++k) v *= G[(m + k) % nmodes][e];
+                H[e] = v;
+            }
+            memcpy(A[m], M, (size_t)ndims[m] * R * sizeof(double));
+            solve_rows_f64(H, (int)R, A[m], ndims[m], (int)R);
+            for (uint32_t r = 0; r < R; ++r) lam[r] = 0.0;
+            if (it == 0) {
+                for (uint64_t i = 0; i < ndims[m]; ++i)
+                    for (uint32_t r = 0; r < R; ++r) lam[r] += A[m][i * R + r] * A[m][i * R + r];
+                for (uint32_t r = 0; r < R; ++r) lam[r] = sqrt(lam[r]);
+            } else {
+                for (uint64_t i = 0; i < ndims[m]; ++i)
+                    for (uint32_t r = 0; r < R; ++r)
+                        if (A[m][i * R + r] > lam[r]) lam[r] = A[m][i * R + r];
+                for (uint32_t r = 0; r < R; ++r)
+                    if (lam[r] < 1.0) lam[r] = 1.0;
+            }
+            for (uint64_t i = 0; i < ndims[m]; ++i)
+                for (uint32_t r = 0; r < R; ++r) A[m][i * R + r] /= lam[r];
+            gram_f64(A[m], ndims[m], (int)R, (int)R, G[m]);
+        }
+        /* fit (ktensor.c:102-257) with full Grams */
+        double normK = 0.0;
+        for (uint32_t p = 0; p < R; ++p)
+            for (uint32_t q = 0; q < R; ++q) {
+                double h = 1.0;
+                for (uint32_t m = 0; m < nmodes; ++m) h *= G[m][p * R + q];
+                normK += h * lam[p] * lam[q];
+            }
+        normK = fabs(normK);
+        const uint32_t last = nmodes - 1;
+        double inner = 0.0;
+        for (uint32_t r = 0; r < R; ++r) {
+            double acc = 0.0;
+            for (uint64_t i = 0; i < ndims[last]; ++i) acc += A[last][i * R + r] * M[i * R + r];
+            inner += acc * lam[r];
+        }
+        double res = normX2 + normK - 2.0 * inner;
+        if (res > 0.0) res = sqrt(res);
+        const double fit = 1.0 - res / sqrt(normX2);
+        fits[it] = fit;
+        done = it + 1;
+        if (it > 0 && fabs(fit - oldfit) < tol) break;
+        oldfit = fit;
+    }
+    /* GetFinalLambda */
+    for (uint32_t m = 0; m < nmodes; ++m) {
+        for (uint32_t r = 0; r < R; ++r) {
+            double s = 0.0;
+            for (uint64_t i = 0; i < ndims[m]; ++i) s += A[m][i * R + r] * A[m][i * R + r];
+            s = sqrt(s);
+            lam[r] *= s;
+            for (uint64_t i = 0; i < ndims[m]; ++i) A[m][i * R + r] /= s;
+        }
+    }
+    for (uint32_t m = 0; m < nmodes; ++m)
+        for (uint64_t i = 0; i < ndims[m]; ++i)
+            for (uint32_t r = 0; r < R; ++r) factors[m][i * stride + r] = (float)A[m][i * R + r];
+    for (uint32_t r = 0; r < R; ++r) lambda_out[r] = (float)lam[r];
+    *iters_done = done;
+    for (uint32_t m = 0; m < nmodes; ++m) {
+        free(A[m]);
+        free(G[m]);
+    }
+    free(M);
+    free(H);
+    free(lam);
+    free(sc);
+    return 0;
+}
+
+/* The corrected fit of a Kruskal model against the tensor, in FP64, with
+ * <X,K> summed exactly over the nonzeros. */
+double orc_fit_exact(uint32_t nmodes, const uint32_t *ndims, uint64_t nnz, const uint32_t *const *inds,
+                     const float *vals, uint32_t R, const float *const *factors, uint32_t stride, const float *lambda) {
+    double normX2 = 0.0, inner = 0.0, normK = 0.0;
+    for (uint64_t x = 0; x < nnz; ++x) {
+        normX2 += (double)vals[x] * vals[x];
+        double s = 0.0;
+        for (uint32_t r = 0; r < R; ++r) {
+            double p = lambda[r];
+            for (uint32_t m = 0; m < nmodes; ++m) p *= factors[m][(size_t)inds[m][x] * stride + r];
+            s += p;
+        }
+        inner += vals[x] * s;
+    }
+    double *G = (double *)calloc((size_t)R * R, sizeof(double));
+    for (uint32_t p = 0; p < R * R; ++p) G[p] = 1.0;
+    for (uint32_t m = 0; m < nmodes; ++m)
+        for (uint32_t p = 0; p < R; ++p)
+            for (uint32_t q = 0; q < R; ++q) {
+                double g = 0.0;
+                for (uint64_t i = 0; i < ndims[m]; ++i)
+                    g += (double)factors[m][i * stride + p] * factors[m][i * stride + q];
+                G[p * R + q] *= g;
+            }
+    for (uint32_t p = 0; p < R; ++p)
+        for (uint32_t q = 0; q < R; ++q) normK += G[p * R + q] * lambda[p] * lambda[q];
+    free(G);
+    normK = fabs(normK);
+    double res = normX2 + normK - 2.0 * inner;
+    if (res > 0.0) res = sqrt(res);
+    return 1.0 - res / sqrt(normX2);
+}

@@ -1,0 +1,265 @@
+/*
+ * ORACLE -- TEST INFRASTRUCTURE ONLY.
+ *
+ * Flat-array entry points over the reference library itself, compiled by
+ * oracle/Makefile (target `ref`) together with ParTI!'s own sources into
+ * oracle/_ref/libparti_ref.so.  Used only where the reference sources exist:
+ * to generate tests/golden/ and to time the reference's OpenMP MTTKRP beside
+ * the oracle port.  Every call goes through the reference's public API.
+ */
+#define _GNU_SOURCE
+#include <ParTI.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+#include "clapack.h"
+
+static void build_tensor(sptSparseTensor *X, uint32_t nmodes, const uint32_t *ndims, uint64_t nnz,
+                         uint32_t *const *inds, const float *vals) {
+    sptNewSparseTensor(X, nmodes, ndims);
+    for (uint32_t m = 0; m < nmodes; ++m) {
+        sptResizeIndexVector(&X->inds[m], nnz);
+        memcpy(X->inds[m].data, inds[m], nnz * sizeof(uint32_t));
+    }
+    sptResizeValueVector(&X->values, nnz);
+    memcpy(X->values.data, vals, nnz * sizeof(float));
+    X->nnz = nnz;
+}
+
+static sptMatrix **build_mats(uint32_t nmodes, const uint32_t *ndims, uint32_t R, float *const *mats, uint32_t stride) {
+    sptMatrix **U = (sptMatrix **)malloc((nmodes + 1) * sizeof(*U));
+    uint32_t maxd = 0;
+    for (uint32_t m = 0; m < nmodes; ++m) {
+        U[m] = (sptMatrix *)malloc(sizeof(sptMatrix));
+        sptNewMatrix(U[m], ndims[m], R);
+        if (U[m]->stride != stride) abort();
+        memcpy(U[m]->values, mats[m], (size_t)ndims[m] * stride * sizeof(float));
+        if (ndims[m] > maxd) maxd = ndims[m];
+    }
+    U[nmodes] = (sptMatrix *)malloc(sizeof(sptMatrix));
+    sptNewMatrix(U[nmodes], maxd, R);
+    sptConstantMatrix(U[nmodes], 0);
+    return U;
+}
+
+static void free_mats(sptMatrix **U, uint32_t nmodes) {
+    for (uint32_t m = 0; m <= nmodes; ++m) {
+        sptFreeMatrix(U[m]);
+        free(U[m]);
+    }
+    free(U);
+}
+
+static double now_s(void) {
+    struct timespec t;
+    clock_gettime(CLOCK_MONOTONIC, &t);
+    return t.tv_sec + 1e-9 * t.tv_nsec;
+}
+
+/* order == NULL: sptSparseTensorSortIndex; else SortIndexCustomOrder. */
+int ref_sort(uint32_t nmodes, const uint32_t *ndims, uint64_t nnz, uint32_t *const *inds, float *vals,
+             const uint32_t *order) {
+    sptSparseTensor X;
+    build_tensor(&X, nmodes, ndims, nnz, inds, vals);
+    if (order) sptSparseTensorSortIndexCustomOrder(&X, order, 1, 1);
+    else sptSparseTensorSortIndex(&X, 1, 1);
+    for (uint32_t m = 0; m < nmodes; ++m) memcpy(inds[m], X.inds[m].data, nnz * 4);
+    memcpy(vals, X.values.data, nnz * 4);
+    sptFreeSparseTensor(&X);
+    return 0;
+}
+
+/* which: 0 sptMTTKRP, 1 sptOmpMTTKRP_Reduce, 2 sptOmpMTTKRP.  Returns the
+ * time of `reps` calls (after one warm-up call) in *seconds. */
+int ref_mttkrp(uint32_t nmodes, const uint32_t *ndims, uint64_t nnz, uint32_t *const *inds, const float *vals,
+               uint32_t R, float *const *mats, uint32_t stride, const uint32_t *mats_order, uint32_t mode, float *out,
+               int which, int tk, int reps, double *seconds) {
+    sptSparseTensor X;
+    build_tensor(&X, nmodes, ndims, nnz, inds, vals);
+    sptMatrix **U = build_mats(nmodes, ndims, R, mats, stride);
+    U[nmodes]->nrows = ndims[mode];
+    sptMatrix **copies = NULL;
+    if (which == 1) {
+        copies = (sptMatrix **)malloc(tk * sizeof(*copies));
+        for (int t = 0; t < tk; ++t) {
+            copies[t] = (sptMatrix *)malloc(sizeof(sptMatrix));
+            sptNewMatrix(copies[t], ndims[mode], R);
+        }
+    }
+    int r = 0;
+    double t0 = 0;
+    for (int k = 0; k <= reps; ++k) {
+        if (k == 1) t0 = now_s();
+        if (which == 0) r = sptMTTKRP(&X, U, (sptIndex *)mats_order, mode);
+        else if (which == 1) r = sptOmpMTTKRP_Reduce(&X, U, copies, (sptIndex *)mats_order, mode, tk);
+        else r = sptOmpMTTKRP(&X, U, (sptIndex *)mats_order, mode, tk);
+    }
+    if (seconds) *seconds = reps ? (now_s() - t0) / reps : 0.0;
+    memcpy(out, U[nmodes]->values, (size_t)ndims[mode] * stride * 4);
+    if (copies) {
+        for (int t = 0; t < tk; ++t) {
+            sptFreeMatrix(copies[t]);
+            free(copies[t]);
+        }
+        free(copies);
+    }
+    free_mats(U, nmodes);
+    sptFreeSparseTensor(&X);
+    return r;
+}
+
+typedef struct {
+    uint64_t nb, nk, ncptr, max_nnzb;
+    uint64_t *bptr, *kptr, *cptr;
+    uint32_t *binds;
+    uint8_t *einds;
+    uint32_t *nkiters;
+    uint32_t *kschr_len;
+    uint32_t *kschr;
+} ref_hicoo_out;
+
+/* sptSparseTensorToHiCOO with tk = 1; inds/vals receive the sorted COO. */
+int ref_hicoo(uint32_t nmodes, const uint32_t *ndims, uint64_t nnz, uint32_t *const *inds, float *vals, int sb_bits,
+              int sk_bits, ref_hicoo_out *o) {
+    sptSparseTensor X;
+    build_tensor(&X, nmodes, ndims, nnz, inds, vals);
+    sptSparseTensorHiCOO H;
+    sptNnzIndex mx = 0;
+    int r = sptSparseTensorToHiCOO(&H, &mx, &X, (sptElementIndex)sb_bits, (sptElementIndex)sk_bits, 1);
+    for (uint32_t m = 0; m < nmodes; ++m) memcpy(inds[m], X.inds[m].data, nnz * 4);
+    memcpy(vals, X.values.data, nnz * 4);
+    o->nb = H.bptr.len - 1;
+    o->nk = H.kptr.len - 1;
+    o->ncptr = H.cptr.len;
+    o->max_nnzb = mx;
+    memcpy(o->bptr, H.bptr.data, H.bptr.len * 8);
+    memcpy(o->kptr, H.kptr.data, H.kptr.len * 8);
+    memcpy(o->cptr, H.cptr.data, H.cptr.len * 8);
+    for (uint32_t m = 0; m < nmodes; ++m) {
+        memcpy(o->binds + (size_t)m * o->nb, H.binds[m].data, o->nb * 4);
+        memcpy(o->einds + (size_t)m * nnz, H.einds[m].data, nnz);
+        o->nkiters[m] = H.nkiters[m];
+    }
+    uint64_t row = 0, ent = 0;
+    const uint64_t sk = 1ull << sk_bits;
+    for (uint32_t m = 0; m < nmodes; ++m) {
+        const uint64_t kn = (ndims[m] + sk - 1) / sk;
+        for (uint64_t i = 0; i < kn; ++i) {
+            o->kschr_len[row++] = (uint32_t)H.kschr[m][i].len;
+            for (uint64_t e = 0; e < H.kschr[m][i].len; ++e) o->kschr[ent++] = H.kschr[m][i].data[e];
+        }
+    }
+    sptFreeSparseTensorHiCOO(&H);
+    sptFreeSparseTensor(&X);
+    return r;
+}
+
+int ref_mttkrp_hicoo(uint32_t nmodes, const uint32_t *ndims, uint64_t nnz, uint32_t *const *inds, const float *vals,
+                     int sb_bits, int sk_bits, uint32_t R, float *const *mats, uint32_t stride,
+                     const uint32_t *mats_order, uint32_t mode, float *out) {
+    sptSparseTensor X;
+    build_tensor(&X, nmodes, ndims, nnz, inds, vals);
+    sptSparseTensorHiCOO H;
+    sptNnzIndex mx = 0;
+    sptSparseTensorToHiCOO(&H, &mx, &X, (sptElementIndex)sb_bits, (sptElementIndex)sk_bits, 1);
+    sptMatrix **U = build_mats(nmodes, ndims, R, mats, stride);
+    U[nmodes]->nrows = ndims[mode];
+    int r = sptMTTKRPHiCOO(&H, U, (sptIndex *)mats_order, mode);
+    memcpy(out, U[nmodes]->values, (size_t)ndims[mode] * stride * 4);
+    free_mats(U, nmodes);
+    sptFreeSparseTensorHiCOO(&H);
+    sptFreeSparseTensor(&X);
+    return r;
+}
+
+/* Fit of the model against the tensor in FP64 from the full symmetric Gram
+ * matrices and <X,K> summed over the nonzeros; the reference's own fit reads
+ * a Gram triangle its ssyrk_ call never writes. */
+static double corrected_fit(const sptSparseTensor *X, sptMatrix **U, const sptValue *lambda, uint32_t R) {
+    const uint32_t N = X->nmodes;
+    double nx = 0, inner = 0, nk = 0;
+    for (uint64_t x = 0; x < X->nnz; ++x) {
+        const double v = X->values.data[x];
+        nx += v * v;
+        double s = 0;
+        for (uint32_t r = 0; r < R; ++r) {
+            double p = lambda[r];
+            for (uint32_t m = 0; m < N; ++m) p *= U[m]->values[(size_t)X->inds[m].data[x] * U[m]->stride + r];
+            s += p;
+        }
+        inner += v * s;
+    }
+    for (uint32_t p = 0; p < R; ++p)
+        for (uint32_t q = 0; q < R; ++q) {
+            double h = 1;
+            for (uint32_t m = 0; m < N; ++m) {
+                double g = 0;
+                for (uint32_t i = 0; i < U[m]->nrows; ++i)
+                    g += (double)U[m]->values[(size_t)i * U[m]->stride + p] * U[m]->values[(size_t)i * U[m]->stride + q];
+                h *= g;
+            }
+            nk += h * lambda[p] * lambda[q];
+        }
+    nk = fabs(nk);
+    double res = nx + nk - 2 * inner;
+    if (res > 0) res = sqrt(res);
+    return 1 - res / sqrt(nx);
+}
+
+/* The CP-ALS loop of cpd.c:76-127 driven through the reference's exported
+ * pieces (sptMTTKRP, sptMatrixSolveNormals, sptMatrix2Norm/MaxNorm, ssyrk_,
+ * GetFinalLambda) from caller factors, recording the corrected fit after
+ * every iteration; then CpdAlsStep itself from the same factors, so that the
+ * caller can check both end in the same factors bit for bit. */
+int ref_cpd_trace(uint32_t nmodes, const uint32_t *ndims, uint64_t nnz, uint32_t *const *inds, const float *vals,
+                  uint32_t R, uint32_t niters, float *const *init, uint32_t stride, float *const *final_loop,
+                  float *lambda_loop, double *fits, float *const *final_step, float *lambda_step, double *step_fit) {
+    sptSparseTensor X;
+    build_tensor(&X, nmodes, ndims, nnz, inds, vals);
+    sptMatrix **U = build_mats(nmodes, ndims, R, init, stride);
+    sptMatrix **ata = (sptMatrix **)malloc((nmodes + 1) * sizeof(*ata));
+    for (uint32_t m = 0; m <= nmodes; ++m) {
+        ata[m] = (sptMatrix *)malloc(sizeof(sptMatrix));
+        sptNewMatrix(ata[m], R, R);
+    }
+    char uplo = 'L', notrans = 'N';
+    float alpha = 1, beta = 0;
+    int br = (int)R, bs = (int)stride;
+    for (uint32_t m = 0; m < nmodes; ++m) {
+        int nr = (int)U[m]->nrows;
+        ssyrk_(&uplo, &notrans, &br, &nr, &alpha, U[m]->values, &bs, &beta, ata[m]->values, &bs);
+    }
+    sptIndex *order = (sptIndex *)malloc(nmodes * sizeof(sptIndex));
+    for (uint32_t it = 0; it < niters; ++it) {
+        for (uint32_t m = 0; m < nmodes; ++m) {
+            U[nmodes]->nrows = U[m]->nrows;
+            order[0] = m;
+            for (uint32_t i = 1; i < nmodes; ++i) order[i] = (m + i) % nmodes;
+            sptMTTKRP(&X, U, order, m);
+            memcpy(U[m]->values, U[nmodes]->values, (size_t)U[m]->nrows * stride * sizeof(float));
+            sptMatrixSolveNormals(m, nmodes, ata, U[m]);
+            if (it == 0) sptMatrix2Norm(U[m], lambda_loop);
+            else sptMatrixMaxNorm(U[m], lambda_loop);
+            int nr = (int)U[m]->nrows;
+            ssyrk_(&uplo, &notrans, &br, &nr, &alpha, U[m]->values, &bs, &beta, ata[m]->values, &bs);
+        }
+        fits[it] = corrected_fit(&X, U, lambda_loop, R);
+    }
+    GetFinalLambda(R, nmodes, U, lambda_loop);
+    for (uint32_t m = 0; m < nmodes; ++m) memcpy(final_loop[m], U[m]->values, (size_t)ndims[m] * stride * 4);
+    free_mats(U, nmodes);
+
+    sptMatrix **V = build_mats(nmodes, ndims, R, init, stride);
+    *step_fit = CpdAlsStep(&X, R, niters, 0.0, V, lambda_step);
+    for (uint32_t m = 0; m < nmodes; ++m) memcpy(final_step[m], V[m]->values, (size_t)ndims[m] * stride * 4);
+    free_mats(V, nmodes);
+    for (uint32_t m = 0; m <= nmodes; ++m) {
+        sptFreeMatrix(ata[m]);
+        free(ata[m]);
+    }
+    free(ata);
+    free(order);
+    sptFreeSparseTensor(&X);
+    return 0;
+}

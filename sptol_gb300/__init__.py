@@ -1,0 +1,454 @@
+"""Host-side mirror of ParTI!'s MTTKRP / CP-ALS C API over libParTI.so.
+
+The C library (include/ParTI.h, include/sptgb.h) is the product; this module
+only binds it with ctypes so that Python callers (tests, the benchmark) use
+exactly the entry points a C caller would: sptMTTKRP, sptCudaMTTKRP,
+sptSparseTensorSortIndex, sptSparseTensorToHiCOO, sptMTTKRPHiCOO, sptCpdAls /
+CpdAlsStep, plus the device-resident extension API.  Struct definitions mirror
+include/ParTI.h field by field.  There is no Python or CPU implementation of
+any operation here: a missing library raises ImportError.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+__all__ = [
+    "lib", "Tensor", "Matrix", "HiCOO", "GenSpec", "mttkrp", "mttkrp_hicoo", "cpd_als",
+    "new_factors", "SptError", "DIST_UNIFORM", "DIST_ZIPF", "VAL_U01", "VAL_UPM1", "VAL_LOGNORMAL",
+    "VAL_PLANTED", "DeviceCoo",
+]
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libParTI.so")
+
+DIST_UNIFORM, DIST_ZIPF = 0, 1
+VAL_U01, VAL_UPM1, VAL_LOGNORMAL, VAL_PLANTED = 0, 1, 2, 3
+MAX_MODES = 8
+
+u32p = C.POINTER(C.c_uint32)
+u64p = C.POINTER(C.c_uint64)
+f32p = C.POINTER(C.c_float)
+u8p = C.POINTER(C.c_uint8)
+
+
+class SptError(RuntimeError):
+    def __init__(self, code, where):
+        self.code = code
+        super().__init__("%s failed with SptError 0x%x%s" % (where, code, _last_reason()))
+
+
+class IndexVector(C.Structure):
+    _fields_ = [("len", C.c_uint64), ("cap", C.c_uint64), ("data", u32p)]
+
+
+class ValueVector(C.Structure):
+    _fields_ = [("len", C.c_uint64), ("cap", C.c_uint64), ("data", f32p)]
+
+
+class ElementIndexVector(C.Structure):
+    _fields_ = [("len", C.c_uint64), ("cap", C.c_uint64), ("data", u8p)]
+
+
+class BlockIndexVector(C.Structure):
+    _fields_ = [("len", C.c_uint64), ("cap", C.c_uint64), ("data", u32p)]
+
+
+class NnzIndexVector(C.Structure):
+    _fields_ = [("len", C.c_uint64), ("cap", C.c_uint64), ("data", u64p)]
+
+
+class SparseTensorS(C.Structure):
+    _fields_ = [("nmodes", C.c_uint32), ("sortorder", u32p), ("ndims", u32p), ("nnz", C.c_uint64),
+                ("inds", C.POINTER(IndexVector)), ("values", ValueVector)]
+
+
+class MatrixS(C.Structure):
+    _fields_ = [("nrows", C.c_uint32), ("ncols", C.c_uint32), ("cap", C.c_uint32), ("stride", C.c_uint32),
+                ("values", f32p)]
+
+
+class HiCOOS(C.Structure):
+    _fields_ = [("nmodes", C.c_uint32), ("sortorder", u32p), ("ndims", u32p), ("nnz", C.c_uint64),
+                ("sb_bits", C.c_uint8), ("sk_bits", C.c_uint8), ("sc_bits", C.c_uint8),
+                ("kptr", NnzIndexVector), ("kschr", C.POINTER(C.POINTER(IndexVector))), ("nkiters", u32p),
+                ("cptr", NnzIndexVector), ("kschr_balanced", C.POINTER(C.POINTER(IndexVector))),
+                ("kschr_balanced_pos", C.POINTER(C.POINTER(IndexVector))), ("nkpars", u32p),
+                ("kschr_rest", C.POINTER(IndexVector)), ("knnzs", NnzIndexVector), ("bptr", NnzIndexVector),
+                ("binds", C.POINTER(BlockIndexVector)), ("einds", C.POINTER(ElementIndexVector)),
+                ("values", ValueVector)]
+
+
+class KruskalS(C.Structure):
+    _fields_ = [("nmodes", C.c_uint32), ("rank", C.c_uint32), ("ndims", u32p), ("lambda_", f32p),
+                ("fit", C.c_double), ("factors", C.POINTER(C.POINTER(MatrixS)))]
+
+
+class GenSpec(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("nmodes", C.c_uint32), ("ndims", C.c_uint32 * 8),
+                ("coord_dist", C.c_int * 8), ("zipf_s", C.c_double * 8), ("count", C.c_uint64),
+                ("merge_duplicates", C.c_int), ("value_dist", C.c_int), ("planted_rank", C.c_uint32),
+                ("planted_seed", C.c_uint64), ("noise_sigma", C.c_double)]
+
+
+_LIB = None
+
+
+def _declare(L):
+    T = C.POINTER(SparseTensorS)
+    M = C.POINTER(MatrixS)
+    MM = C.POINTER(M)
+    H = C.POINTER(HiCOOS)
+    sig = {
+        "sptGetLastError": (C.c_int, [C.POINTER(C.c_char_p), C.POINTER(C.c_char_p), C.POINTER(C.c_uint),
+                                      C.POINTER(C.c_char_p)]),
+        "sptClearLastError": (None, []),
+        "sptNewSparseTensor": (C.c_int, [T, C.c_uint32, u32p]),
+        "sptFreeSparseTensor": (None, [T]),
+        "sptResizeIndexVector": (C.c_int, [C.POINTER(IndexVector), C.c_uint64]),
+        "sptResizeValueVector": (C.c_int, [C.POINTER(ValueVector), C.c_uint64]),
+        "sptNewMatrix": (C.c_int, [M, C.c_uint32, C.c_uint32]),
+        "sptFreeMatrix": (None, [M]),
+        "sptMTTKRP": (C.c_int, [T, MM, u32p, C.c_uint32]),
+        "sptOmpMTTKRP": (C.c_int, [T, MM, u32p, C.c_uint32, C.c_int]),
+        "sptCudaMTTKRP": (C.c_int, [T, MM, u32p, C.c_uint32, C.c_uint32]),
+        "sptSparseTensorSortIndex": (None, [T, C.c_int, C.c_int]),
+        "sptSparseTensorSortIndexCustomOrder": (None, [T, u32p, C.c_int, C.c_int]),
+        "sptSparseTensorSortIndexAtMode": (None, [T, C.c_uint32, C.c_int, C.c_int]),
+        "sptSparseTensorSortIndexMorton": (None, [T, C.c_int, C.c_uint64, C.c_uint64, C.c_uint8, C.c_int]),
+        "sptSparseTensorSortIndexRowBlock": (None, [T, C.c_int, C.c_uint64, C.c_uint64, C.c_uint8, C.c_int]),
+        "sptSparseTensorMixedOrder": (C.c_int, [T, C.c_uint8, C.c_uint8, C.c_int]),
+        "sptSparseTensorToHiCOO": (C.c_int, [H, u64p, T, C.c_uint8, C.c_uint8, C.c_int]),
+        "sptFreeSparseTensorHiCOO": (None, [H]),
+        "sptMTTKRPHiCOO": (C.c_int, [H, MM, u32p, C.c_uint32]),
+        "CpdAlsStep": (C.c_double, [T, C.c_uint32, C.c_uint32, C.c_double, MM, f32p]),
+        "sptCpdAls": (C.c_int, [T, C.c_uint32, C.c_uint32, C.c_double, C.POINTER(KruskalS)]),
+        "sptNewKruskalTensor": (C.c_int, [C.POINTER(KruskalS), C.c_uint32, u32p, C.c_uint32]),
+        "sptFreeKruskalTensor": (None, [C.POINTER(KruskalS)]),
+        "SparseTensorFrobeniusNormSquared": (C.c_double, [T]),
+        "sptgbVersion": (C.c_char_p, []),
+        "sptgbInit": (C.c_int, [C.c_int]),
+        "sptgbStream": (C.c_void_p, []),
+        "sptgbLaunchCount": (C.c_uint64, []),
+        "sptgbSetSeed": (None, [C.c_uint64]),
+        "sptgbGenerate": (C.c_int, [T, C.POINTER(GenSpec)]),
+        "sptgbFillMatrix": (C.c_int, [M, C.c_uint64, C.c_uint64, C.c_float, C.c_float]),
+        "sptgbCpdAls": (C.c_int, [T, C.c_uint32, C.c_uint32, C.c_double, MM, f32p, C.POINTER(C.c_double),
+                                  u32p]),
+        "sptgbCooCreate": (C.c_int, [C.POINTER(C.c_void_p), T, C.c_void_p]),
+        "sptgbCooPrepareMode": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p]),
+        "sptgbCooMTTKRP": (C.c_int, [C.c_void_p, C.c_uint32, u32p, C.POINTER(C.c_void_p), C.c_uint32,
+                                     C.c_uint32, C.c_void_p, C.c_void_p]),
+        "sptgbCooMTTKRPBf16": (C.c_int, [C.c_void_p, C.c_uint32, u32p, C.POINTER(C.c_void_p), C.c_uint32,
+                                         C.c_uint32, C.c_void_p, C.c_void_p]),
+        "sptgbCooNnz": (C.c_uint64, [C.c_void_p]),
+        "sptgbCooDeviceBytes": (C.c_size_t, [C.c_void_p]),
+        "sptgbCooSetTiming": (None, [C.c_void_p, C.c_int]),
+        "sptgbCooLastKernelMs": (C.c_float, [C.c_void_p]),
+        "sptgbCooFree": (None, [C.c_void_p]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+
+
+def lib():
+    """Loads libParTI.so (built in-tree by sptol_gb300.build)."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libParTI.so is not built (%s); run sptol_gb300/build.py" % LIB_PATH)
+        _LIB = C.CDLL(LIB_PATH)
+        _declare(_LIB)
+    return _LIB
+
+
+def _last_reason():
+    L = _LIB
+    if L is None:
+        return ""
+    r = C.c_char_p()
+    L.sptGetLastError(None, None, None, C.byref(r))
+    return (": " + r.value.decode()) if r.value else ""
+
+
+def _check(code, where):
+    if code != 0:
+        raise SptError(code, where)
+
+
+def _u32(a):
+    a = np.ascontiguousarray(a, dtype=np.uint32)
+    return a, a.ctypes.data_as(u32p)
+
+
+class Tensor:
+    """An sptSparseTensor allocated by the library."""
+
+    def __init__(self):
+        self.s = SparseTensorS()
+        self._owned = False
+
+    @classmethod
+    def from_arrays(cls, ndims, inds, vals):
+        inds = np.asarray(inds)
+        vals = np.ascontiguousarray(vals, dtype=np.float32)
+        L = lib()
+        t = cls()
+        nd, ndp = _u32(ndims)
+        N = len(nd)
+        _check(L.sptNewSparseTensor(C.byref(t.s), N, ndp), "sptNewSparseTensor")
+        t._owned = True
+        n = int(vals.shape[0])
+        for m in range(N):
+            _check(L.sptResizeIndexVector(C.byref(t.s.inds[m]), n), "sptResizeIndexVector")
+            if n:
+                C.memmove(t.s.inds[m].data, np.ascontiguousarray(inds[m], dtype=np.uint32).ctypes.data, 4 * n)
+        _check(L.sptResizeValueVector(C.byref(t.s.values), n), "sptResizeValueVector")
+        if n:
+            C.memmove(t.s.values.data, vals.ctypes.data, 4 * n)
+        t.s.nnz = n
+        return t
+
+    @classmethod
+    def generate(cls, spec):
+        t = cls()
+        _check(lib().sptgbGenerate(C.byref(t.s), C.byref(spec)), "sptgbGenerate")
+        t._owned = True
+        return t
+
+    @property
+    def nmodes(self):
+        return int(self.s.nmodes)
+
+    @property
+    def nnz(self):
+        return int(self.s.nnz)
+
+    @property
+    def ndims(self):
+        return [int(self.s.ndims[m]) for m in range(self.nmodes)]
+
+    @property
+    def sortorder(self):
+        return [int(self.s.sortorder[m]) for m in range(self.nmodes)]
+
+    def inds(self, m):
+        if self.nnz == 0:
+            return np.zeros(0, np.uint32)
+        return np.ctypeslib.as_array(self.s.inds[m].data, shape=(self.nnz,))
+
+    def vals(self):
+        if self.nnz == 0:
+            return np.zeros(0, np.float32)
+        return np.ctypeslib.as_array(self.s.values.data, shape=(self.nnz,))
+
+    def arrays(self):
+        """Copies: (inds [N, nnz] uint32, vals [nnz] float32)."""
+        return np.stack([self.inds(m).copy() for m in range(self.nmodes)]), self.vals().copy()
+
+    def ptr(self):
+        return C.byref(self.s)
+
+    def free(self):
+        if self._owned:
+            lib().sptFreeSparseTensor(C.byref(self.s))
+            self._owned = False
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class Matrix:
+    """An sptMatrix allocated by sptNewMatrix (row-major, stride = ncols rounded up to 8)."""
+
+    def __init__(self, nrows, ncols):
+        self.s = MatrixS()
+        _check(lib().sptNewMatrix(C.byref(self.s), nrows, ncols), "sptNewMatrix")
+        self._owned = True
+        self.array()[:] = 0
+
+    @classmethod
+    def from_array(cls, a, stride_like=None):
+        a = np.asarray(a, dtype=np.float32)
+        m = cls(a.shape[0], a.shape[1])
+        m.array()[:, : a.shape[1]] = a
+        return m
+
+    def array(self):
+        """Full (cap x stride) view including padding columns."""
+        s = self.s
+        return np.ctypeslib.as_array(s.values, shape=(int(s.cap), int(s.stride)))
+
+    def view(self):
+        """(nrows x ncols) view."""
+        return self.array()[: int(self.s.nrows), : int(self.s.ncols)]
+
+    def free(self):
+        if self._owned:
+            lib().sptFreeMatrix(C.byref(self.s))
+            self._owned = False
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def new_factors(ndims, rank, seed=0, lo=0.0, hi=1.0):
+    """Factor matrices U[lo, hi) from the library's seeded filler, plus the
+    scratch output mats[N] sized to the largest mode."""
+    L = lib()
+    mats = []
+    for m, d in enumerate(ndims):
+        M = Matrix(d, rank)
+        _check(L.sptgbFillMatrix(C.byref(M.s), seed, m, lo, hi), "sptgbFillMatrix")
+        mats.append(M)
+    mats.append(Matrix(max(ndims), rank))
+    return mats
+
+
+def _mat_array(mats):
+    arr = (C.POINTER(MatrixS) * len(mats))()
+    for i, m in enumerate(mats):
+        arr[i] = C.pointer(m.s)
+    return arr
+
+
+def mttkrp(tensor, mats, mode, mats_order=None, entry="sptMTTKRP"):
+    """Runs the drop-in entry point `entry`; returns mats[N] rows [0, ndims[mode])."""
+    L = lib()
+    N = tensor.nmodes
+    if mats_order is None:
+        mats_order = [mode] + [(mode + i) % N for i in range(1, N)]
+    order, op = _u32(mats_order)
+    mats[N].s.nrows = tensor.ndims[mode]
+    arr = _mat_array(mats)
+    if entry == "sptMTTKRP":
+        r = L.sptMTTKRP(tensor.ptr(), arr, op, mode)
+    elif entry == "sptCudaMTTKRP":
+        r = L.sptCudaMTTKRP(tensor.ptr(), arr, op, mode, 15)
+    elif entry == "sptOmpMTTKRP":
+        r = L.sptOmpMTTKRP(tensor.ptr(), arr, op, mode, 1)
+    else:
+        raise ValueError(entry)
+    _check(r, entry)
+    return mats[N].array()[: tensor.ndims[mode], : int(mats[N].s.ncols)].copy()
+
+
+class HiCOO:
+    def __init__(self, tensor, sb_bits, sk_bits):
+        self.s = HiCOOS()
+        mx = C.c_uint64()
+        _check(lib().sptSparseTensorToHiCOO(C.byref(self.s), C.byref(mx), tensor.ptr(), sb_bits, sk_bits, 1),
+               "sptSparseTensorToHiCOO")
+        self.max_nnzb = int(mx.value)
+        self._owned = True
+
+    def arrays(self):
+        s = self.s
+        N = int(s.nmodes)
+
+        def vec(v):
+            n = int(v.len)
+            if n == 0:
+                return np.zeros(0, dtype=np.dtype(v.data._type_))
+            return np.ctypeslib.as_array(v.data, shape=(n,)).copy()
+
+        sk = 1 << int(s.sk_bits)
+        out = {
+            "kptr": vec(s.kptr), "cptr": vec(s.cptr), "bptr": vec(s.bptr),
+            "binds": [vec(s.binds[m]) for m in range(N)],
+            "einds": [vec(s.einds[m]) for m in range(N)],
+            "values": vec(s.values),
+            "nkiters": [int(s.nkiters[m]) for m in range(N)],
+            "kschr": [[vec(s.kschr[m][i]) for i in range((int(s.ndims[m]) + sk - 1) // sk)] for m in range(N)],
+        }
+        return out
+
+    def ptr(self):
+        return C.byref(self.s)
+
+    def free(self):
+        if self._owned:
+            lib().sptFreeSparseTensorHiCOO(C.byref(self.s))
+            self._owned = False
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def mttkrp_hicoo(h, mats, mode, mats_order=None):
+    L = lib()
+    N = int(h.s.nmodes)
+    if mats_order is None:
+        mats_order = [mode] + [(mode + i) % N for i in range(1, N)]
+    order, op = _u32(mats_order)
+    nd = int(h.s.ndims[mode])
+    mats[N].s.nrows = nd
+    _check(L.sptMTTKRPHiCOO(h.ptr(), _mat_array(mats), op, mode), "sptMTTKRPHiCOO")
+    return mats[N].array()[:nd, : int(mats[N].s.ncols)].copy()
+
+
+def cpd_als(tensor, rank, niters, tol, init):
+    """CP-ALS from caller factors `init` (list of N arrays ndims[m] x rank).
+    Returns (factors, lambda, fits per iteration, iterations run)."""
+    L = lib()
+    N = tensor.nmodes
+    mats = [Matrix.from_array(a) for a in init] + [Matrix(max(tensor.ndims), rank)]
+    lam = np.zeros(rank, np.float32)
+    fits = np.zeros(niters, np.float64)
+    done = C.c_uint32()
+    _check(L.sptgbCpdAls(tensor.ptr(), rank, niters, tol, _mat_array(mats), lam.ctypes.data_as(f32p),
+                         fits.ctypes.data_as(C.POINTER(C.c_double)), C.byref(done)), "sptgbCpdAls")
+    return [mats[m].view().copy() for m in range(N)], lam, fits, int(done.value)
+
+
+class DeviceCoo:
+    """sptgbCoo handle: a device-resident tensor with per-mode segmented copies."""
+
+    def __init__(self, tensor, stream=None):
+        self.h = C.c_void_p()
+        _check(lib().sptgbCooCreate(C.byref(self.h), tensor.ptr(), stream), "sptgbCooCreate")
+        self.nmodes = tensor.nmodes
+
+    def prepare(self, mode, stream=None):
+        _check(lib().sptgbCooPrepareMode(self.h, mode, stream), "sptgbCooPrepareMode")
+
+    def mttkrp(self, mode, mats_order, dev_ptrs, rank, stride, out_ptr, stream=None, bf16=False):
+        order, op = _u32(mats_order)
+        arr = (C.c_void_p * len(dev_ptrs))(*dev_ptrs)
+        f = lib().sptgbCooMTTKRPBf16 if bf16 else lib().sptgbCooMTTKRP
+        _check(f(self.h, mode, op, arr, rank, stride, out_ptr, stream), "sptgbCooMTTKRP")
+
+    def set_timing(self, on):
+        lib().sptgbCooSetTiming(self.h, 1 if on else 0)
+
+    def last_ms(self):
+        return float(lib().sptgbCooLastKernelMs(self.h))
+
+    def nbytes(self):
+        return int(lib().sptgbCooDeviceBytes(self.h))
+
+    def free(self):
+        if self.h:
+            lib().sptgbCooFree(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def launch_count():
+    return int(lib().sptgbLaunchCount())

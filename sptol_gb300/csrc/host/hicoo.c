@@ -1,0 +1,353 @@
+/*
+ * COO -> HiCOO conversion and HiCOO MTTKRP behind the reference's entry
+ * points (src/sptensor/hicoo/convert.c:237-497, hicoo/mttkrp.c:53-144).
+ *
+ * Conversion on the GPU:
+ *   1. stable device sort in the HiCOO order: kernels (idx >> sk_bits) in
+ *      row-major order, Morton order of the full coordinates inside a kernel
+ *      (convert.c:160-226); the sorted COO is written back into the caller's
+ *      tensor, as the reference sorts it in place;
+ *   2. block / kernel heads are flagged where (idx >> sb_bits) /
+ *      (idx >> sk_bits) change, scanned into block and kernel numbers, and
+ *      compacted into bptr, the first block of every kernel and binds;
+ *      einds = idx & (2^sb - 1) (convert.c:397-456).
+ * The kernel scheduler kschr (one entry per kernel, convert.c:103-146) and
+ * the chunk pointers cptr, whose rule carries a running count across blocks
+ * and kernels (convert.c:386-452), are filled on the host from those
+ * device-built boundaries.
+ */
+#define _GNU_SOURCE
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <cuda_runtime_api.h>
+#include "devtensor.h"
+
+#define SC_BITS 14
+
+static int fail_cuda(cudaError_t e, const char *module, unsigned line) {
+    return sptgb_cuda_fail(e, module, __FILE__, line);
+}
+
+#define C(expr)                                                   \
+    do {                                                          \
+        cudaError_t _c = (expr);                                  \
+        if (_c != cudaSuccess) {                                  \
+            r = fail_cuda(_c, module, __LINE__);                  \
+            goto out;                                             \
+        }                                                         \
+    } while (0)
+#define H(expr)                                                   \
+    do {                                                          \
+        r = (expr);                                               \
+        if (r) goto out;                                          \
+    } while (0)
+
+/* The reference's output for an empty tensor (it reads the zero-filled
+ * first slot of the coordinate vectors): one kernel, one empty block. */
+static int empty_hicoo(sptSparseTensorHiCOO *h, sptNnzIndex *max_nnzb) {
+    int r;
+    if ((r = sptAppendNnzIndexVector(&h->kptr, 0)) || (r = sptAppendNnzIndexVector(&h->kptr, 1))) return r;
+    if ((r = sptAppendNnzIndexVector(&h->cptr, 0)) || (r = sptAppendNnzIndexVector(&h->cptr, 1))) return r;
+    if ((r = sptAppendNnzIndexVector(&h->bptr, 0)) || (r = sptAppendNnzIndexVector(&h->bptr, 0))) return r;
+    for (sptIndex m = 0; m < h->nmodes; ++m) {
+        if ((r = sptAppendBlockIndexVector(&h->binds[m], 0))) return r;
+        if ((r = sptAppendIndexVector(&h->kschr[m][0], 0))) return r;
+        h->nkiters[m] = 1;
+    }
+    *max_nnzb = 0;
+    return 0;
+}
+
+int sptSparseTensorToHiCOO(sptSparseTensorHiCOO *hitsr, sptNnzIndex *max_nnzb, sptSparseTensor *tsr,
+                           const sptElementIndex sb_bits, const sptElementIndex sk_bits, int const tk) {
+    (void)tk;
+    const char *module = "HiSpTns Convert";
+    int r = 0;
+    const sptElementIndex sc_bits = SC_BITS;
+    if (!(sk_bits >= sb_bits) || !(sc_bits >= sb_bits) || sb_bits > 8 || sk_bits > 31) {
+        spt_ComplainError(module, SPTERR_VALUE_ERROR, __FILE__, __LINE__, "need sb_bits <= min(sk_bits, 14, 8)");
+        return SPTERR_VALUE_ERROR;
+    }
+    const int N = (int)tsr->nmodes;
+    const uint64_t n = tsr->nnz;
+    if (N < 1 || N > SPTGB_MAX_MODES || n >= 0xffffffffull) {
+        spt_ComplainError(module, SPTERR_VALUE_ERROR, __FILE__, __LINE__, "unsupported tensor shape");
+        return SPTERR_VALUE_ERROR;
+    }
+    SPTGB_CHECK(sptNewSparseTensorHiCOO(hitsr, (sptIndex)N, tsr->ndims, n, sb_bits, sk_bits, sc_bits), module);
+    for (int m = 0; m < N; ++m) tsr->sortorder[m] = (sptIndex)m;
+    if (n == 0) return empty_hicoo(hitsr, max_nnzb);
+    SPTGB_CHECK(sptgb_ctx(), module);
+    const cudaStream_t s = sptgb_stream();
+
+    uint64_t *h_bstart = NULL, *h_kstart = NULL;
+    uint32_t *h_kblk = NULL;
+    sptgb_lock();
+    uint32_t *din[SPTGB_MAX_MODES] = {0}, *dsrt[SPTGB_MAX_MODES] = {0};
+    for (int m = 0; m < N; ++m) {
+        H(sptgb_dbuf_reserve(&g_ws.inds[m], n * 4));
+        H(sptgb_dbuf_reserve(&g_ws.sinds[m], n * 4));
+        din[m] = (uint32_t *)g_ws.inds[m].ptr;
+        dsrt[m] = (uint32_t *)g_ws.sinds[m].ptr;
+        C(cudaMemcpyAsync(din[m], tsr->inds[m].data, n * 4, cudaMemcpyHostToDevice, s));
+    }
+    H(sptgb_dbuf_reserve(&g_ws.vals, n * 4));
+    H(sptgb_dbuf_reserve(&g_ws.svals, n * 4));
+    C(cudaMemcpyAsync(g_ws.vals.ptr, tsr->values.data, n * 4, cudaMemcpyHostToDevice, s));
+    H(sptgb_validate(din, tsr->ndims, N, n, NULL, NULL, s));
+
+    sptgb_sortpass passes[24];
+    const int np = sptgb_hicoo_passes(tsr->ndims, N, sk_bits, 1, passes);
+    uint32_t *perm = NULL;
+    H(sptgb_sort_perm(din, N, n, passes, np, &perm, s));
+    H(sptgb_gather_tensor(din, (float *)g_ws.vals.ptr, dsrt, (float *)g_ws.svals.ptr, N, perm, n, s));
+
+    /* Scratch: kflags, bflags, kpos, bpos (u32 x n each), scan tmp, totals. */
+    H(sptgb_dbuf_reserve(&g_ws.misc[0], n * 4));
+    H(sptgb_dbuf_reserve(&g_ws.misc[1], n * 4));
+    H(sptgb_dbuf_reserve(&g_ws.misc[2], n * 4));
+    H(sptgb_dbuf_reserve(&g_ws.misc[3], n * 4));
+    H(sptgb_dbuf_reserve(&g_ws.misc[4], sptgb_scan_tmp_bytes(n)));
+    H(sptgb_dbuf_reserve(&g_ws.misc[5], 64));
+    uint32_t *kflags = (uint32_t *)g_ws.misc[0].ptr, *bflags = (uint32_t *)g_ws.misc[1].ptr;
+    uint32_t *kpos = (uint32_t *)g_ws.misc[2].ptr, *bpos = (uint32_t *)g_ws.misc[3].ptr;
+    uint32_t *totals = (uint32_t *)g_ws.misc[5].ptr;
+    C(sptgb_mark_groups((const uint32_t *const *)dsrt, N, sk_bits, n, kflags, s));
+    C(sptgb_mark_groups((const uint32_t *const *)dsrt, N, sb_bits, n, bflags, s));
+    C(sptgb_exclusive_scan_u32(kflags, kpos, n, totals, g_ws.misc[4].ptr, s));
+    C(sptgb_exclusive_scan_u32(bflags, bpos, n, totals + 1, g_ws.misc[4].ptr, s));
+    uint32_t htot[2] = {0, 0};
+    C(cudaMemcpyAsync(htot, totals, sizeof htot, cudaMemcpyDeviceToHost, s));
+    /* Sorted COO back into the caller's tensor. */
+    for (int m = 0; m < N; ++m)
+        C(cudaMemcpyAsync(tsr->inds[m].data, dsrt[m], n * 4, cudaMemcpyDeviceToHost, s));
+    C(cudaMemcpyAsync(tsr->values.data, g_ws.svals.ptr, n * 4, cudaMemcpyDeviceToHost, s));
+    C(cudaStreamSynchronize(s));
+    const uint64_t nk = htot[0], nb = htot[1];
+
+    /* bstart (u64 x nb), kstart (u64 x nk), kblk (u32 x nk), binds (u32 x nb
+     * per mode), einds (u8 x n per mode). */
+    H(sptgb_dbuf_reserve(&g_ws.misc[6], nb * 8 + nk * 8 + nk * 4 + 64));
+    H(sptgb_dbuf_reserve(&g_ws.misc[7], (size_t)N * (nb * 4 + n) + 64));
+    uint64_t *bstart = (uint64_t *)g_ws.misc[6].ptr;
+    uint64_t *kstart = bstart + nb;
+    uint32_t *kblk = (uint32_t *)(kstart + nk);
+    uint32_t *dbinds[SPTGB_MAX_MODES];
+    uint8_t *deinds[SPTGB_MAX_MODES];
+    for (int m = 0; m < N; ++m) {
+        dbinds[m] = (uint32_t *)g_ws.misc[7].ptr + (size_t)m * nb;
+        deinds[m] = (uint8_t *)((uint32_t *)g_ws.misc[7].ptr + (size_t)N * nb) + (size_t)m * n;
+    }
+    C(sptgb_compact_starts(bflags, bpos, n, bstart, s));
+    C(sptgb_compact_starts(kflags, kpos, n, kstart, s));
+    C(sptgb_compact_u32(kflags, kpos, bpos, n, kblk, s));
+    C(sptgb_hicoo_split((const uint32_t *const *)dsrt, N, sb_bits, n, bflags, bpos, deinds, dbinds, s));
+
+    h_bstart = (uint64_t *)malloc(nb * 8);
+    h_kstart = (uint64_t *)malloc(nk * 8);
+    h_kblk = (uint32_t *)malloc(nk * 4);
+    if (!h_bstart || !h_kstart || !h_kblk) {
+        r = SPTERR_OS_ERROR;
+        goto out;
+    }
+    for (int m = 0; m < N; ++m) {
+        H(sptResizeBlockIndexVector(&hitsr->binds[m], nb));
+        H(sptResizeElementIndexVector(&hitsr->einds[m], n));
+        C(cudaMemcpyAsync(hitsr->binds[m].data, dbinds[m], nb * 4, cudaMemcpyDeviceToHost, s));
+        C(cudaMemcpyAsync(hitsr->einds[m].data, deinds[m], n, cudaMemcpyDeviceToHost, s));
+    }
+    C(cudaMemcpyAsync(h_bstart, bstart, nb * 8, cudaMemcpyDeviceToHost, s));
+    C(cudaMemcpyAsync(h_kstart, kstart, nk * 8, cudaMemcpyDeviceToHost, s));
+    C(cudaMemcpyAsync(h_kblk, kblk, nk * 4, cudaMemcpyDeviceToHost, s));
+    H(sptResizeValueVector(&hitsr->values, n));
+    memcpy(hitsr->values.data, tsr->values.data, n * 4);
+    C(cudaStreamSynchronize(s));
+
+    /* bptr: block starts then nnz (convert.c:379, :438, :472). */
+    H(sptResizeNnzIndexVector(&hitsr->bptr, nb + 1));
+    for (uint64_t b = 0; b < nb; ++b) hitsr->bptr.data[b] = (sptNnzIndex)(sptBlockIndex)h_bstart[b];
+    hitsr->bptr.data[nb] = n;
+    /* kptr: first block of every kernel, then #blocks (convert.c:386-388, :470). */
+    H(sptResizeNnzIndexVector(&hitsr->kptr, nk + 1));
+    for (uint64_t k = 0; k < nk; ++k) hitsr->kptr.data[k] = h_kblk[k];
+    hitsr->kptr.data[nk] = nb;
+    /* kschr / nkiters (convert.c:117-143). */
+    for (uint64_t k = 0; k < nk; ++k)
+        for (int m = 0; m < N; ++m) {
+            const sptIndex kc = tsr->inds[m].data[h_kstart[k]] >> sk_bits;
+            H(sptAppendIndexVector(&hitsr->kschr[m][kc], (sptIndex)k));
+        }
+    for (int m = 0; m < N; ++m) {
+        const uint64_t sk = 1ull << sk_bits;
+        const sptIndex kn = (sptIndex)(((uint64_t)tsr->ndims[m] + sk - 1) / sk);
+        sptIndex mx = 0;
+        for (sptIndex i = 0; i < kn; ++i)
+            if (hitsr->kschr[m][i].len > mx) mx = (sptIndex)hitsr->kschr[m][i].len;
+        hitsr->nkiters[m] = mx;
+    }
+    /* cptr (convert.c:386-452): a chunk starts at every kernel, and at a new
+     * block once the running count plus the previous block's size reaches
+     * 2^sc_bits; the running count resets at each kernel start but the first
+     * block of a kernel still tests the previous kernel's last block. */
+    {
+        const uint64_t sc = 1ull << sc_bits;
+        uint64_t chunk = 0;
+        for (uint64_t k = 0; k < nk; ++k) {
+            H(sptAppendNnzIndexVector(&hitsr->cptr, h_kblk[k]));
+            chunk = 0;
+            const uint64_t bend = (k + 1 < nk) ? h_kblk[k + 1] : nb;
+            for (uint64_t b = h_kblk[k]; b < bend; ++b) {
+                if (b == 0) continue;
+                const uint64_t ne = h_bstart[b] - h_bstart[b - 1];
+                if (chunk + ne >= sc) {
+                    H(sptAppendNnzIndexVector(&hitsr->cptr, b));
+                    chunk = 0;
+                } else {
+                    chunk += ne;
+                }
+            }
+        }
+        H(sptAppendNnzIndexVector(&hitsr->cptr, nb));
+    }
+    {
+        sptNnzIndex mx = hitsr->bptr.data[1] - hitsr->bptr.data[0];
+        for (uint64_t b = 0; b < nb; ++b) {
+            const sptNnzIndex c = hitsr->bptr.data[b + 1] - hitsr->bptr.data[b];
+            if (c > mx) mx = c;
+        }
+        *max_nnzb = mx;
+    }
+out:
+    sptgb_unlock();
+    free(h_bstart);
+    free(h_kstart);
+    free(h_kblk);
+    return r;
+}
+
+/* convert.c:237-288 on a tensor already in row-block order: kernel start
+ * positions, then nnz. */
+int sptSetKernelPointers(sptNnzIndexVector *kptr, sptSparseTensor *tsr, const sptElementIndex sk_bits) {
+    const sptIndex N = tsr->nmodes;
+    const uint64_t n = tsr->nnz;
+    int r = sptAppendNnzIndexVector(kptr, 0);
+    if (r) return r;
+    for (uint64_t z = 1; z < n; ++z) {
+        int diff = 0;
+        for (sptIndex m = 0; m < N; ++m)
+            diff |= (tsr->inds[m].data[z] >> sk_bits) != (tsr->inds[m].data[z - 1] >> sk_bits);
+        if (diff && (r = sptAppendNnzIndexVector(kptr, z))) return r;
+    }
+    return sptAppendNnzIndexVector(kptr, n);
+}
+
+/* ------------------------------------------------------- HiCOO MTTKRP -- */
+static int hicoo_mttkrp(sptSparseTensorHiCOO const *h, sptMatrix *mats[], sptIndex const *mats_order, sptIndex mode,
+                        const char *module) {
+    const sptIndex N = h->nmodes;
+    int r = 0;
+    if (N < 2 || N > SPTGB_MAX_MODES || mode >= N) {
+        spt_ComplainError(module, SPTERR_VALUE_ERROR, __FILE__, __LINE__, "unsupported order or mode");
+        return SPTERR_VALUE_ERROR;
+    }
+    for (sptIndex i = 0; i < N; ++i) {
+        if (mats[i]->ncols != mats[N]->ncols) {
+            spt_ComplainError(module, SPTERR_SHAPE_MISMATCH, __FILE__, __LINE__,
+                              "mats[i]->cols != mats[nmodes]->ncols");
+            return SPTERR_SHAPE_MISMATCH;
+        }
+        if (mats[i]->nrows != h->ndims[i]) {
+            spt_ComplainError(module, SPTERR_SHAPE_MISMATCH, __FILE__, __LINE__, "mats[i]->nrows != ndims[i]");
+            return SPTERR_SHAPE_MISMATCH;
+        }
+    }
+    for (sptIndex i = 1; i < N; ++i)
+        if (mats_order[i] >= N) {
+            spt_ComplainError(module, SPTERR_VALUE_ERROR, __FILE__, __LINE__, "mats_order entry out of range");
+            return SPTERR_VALUE_ERROR;
+        }
+    const sptIndex stride = mats[0]->stride;
+    if (stride > 128 || mats[N]->cap < mats[mode]->nrows) {
+        spt_ComplainError(module, SPTERR_VALUE_ERROR, __FILE__, __LINE__, "rank above 128 or output too small");
+        return SPTERR_VALUE_ERROR;
+    }
+    const uint64_t nb = h->bptr.len ? h->bptr.len - 1 : 0;
+    const uint64_t n = h->nnz;
+    const sptIndex tmpI = mats[mode]->nrows;
+    /* Structural checks of the caller's HiCOO arrays, so that no kernel reads
+     * past them: bptr non-decreasing from 0 to nnz, vectors long enough. */
+    int bad = h->values.len < n || (nb && (h->bptr.data[0] != 0 || h->bptr.data[nb] != n)) || h->sb_bits > 8;
+    for (uint64_t b = 0; b < nb && !bad; ++b) bad = h->bptr.data[b + 1] < h->bptr.data[b];
+    for (sptIndex m = 0; m < N && !bad; ++m) bad = h->binds[m].len < nb || h->einds[m].len < n;
+    if (bad) {
+        spt_ComplainError(module, SPTERR_VALUE_ERROR, __FILE__, __LINE__, "inconsistent HiCOO arrays");
+        return SPTERR_VALUE_ERROR;
+    }
+    SPTGB_CHECK(sptgb_ctx(), module);
+    const cudaStream_t s = sptgb_stream();
+    sptgb_lock();
+    sptgb_hicoo_args a;
+    memset(&a, 0, sizeof a);
+    /* bptr, binds, einds, values */
+    H(sptgb_dbuf_reserve(&g_ws.misc[0], (nb + 1) * 8));
+    C(cudaMemcpyAsync(g_ws.misc[0].ptr, h->bptr.data, (nb + 1) * 8, cudaMemcpyHostToDevice, s));
+    H(sptgb_dbuf_reserve(&g_ws.misc[1], (size_t)N * (nb * 4 + n) + 64));
+    for (sptIndex m = 0; m < N; ++m) {
+        uint32_t *db = (uint32_t *)g_ws.misc[1].ptr + (size_t)m * nb;
+        uint8_t *de = (uint8_t *)((uint32_t *)g_ws.misc[1].ptr + (size_t)N * nb) + (size_t)m * n;
+        if (nb) C(cudaMemcpyAsync(db, h->binds[m].data, nb * 4, cudaMemcpyHostToDevice, s));
+        if (n) C(cudaMemcpyAsync(de, h->einds[m].data, n, cudaMemcpyHostToDevice, s));
+        a.binds[m] = db;
+        a.einds[m] = de;
+    }
+    H(sptgb_dbuf_reserve(&g_ws.vals, (n ? n : 1) * 4));
+    if (n) C(cudaMemcpyAsync(g_ws.vals.ptr, h->values.data, n * 4, cudaMemcpyHostToDevice, s));
+    for (sptIndex i = 1; i < N; ++i) {
+        const sptIndex pm = mats_order[i];
+        const size_t bytes = (size_t)mats[pm]->nrows * stride * 4;
+        H(sptgb_dbuf_reserve(&g_ws.fac[pm], bytes ? bytes : 16));
+        if (bytes) C(cudaMemcpyAsync(g_ws.fac[pm].ptr, mats[pm]->values, bytes, cudaMemcpyHostToDevice, s));
+        a.fac[pm] = (const float *)g_ws.fac[pm].ptr;
+    }
+    H(sptgb_dbuf_reserve(&g_ws.out, (size_t)(tmpI ? tmpI : 1) * stride * 4));
+    a.bptr = (const uint64_t *)g_ws.misc[0].ptr;
+    a.vals = (const float *)g_ws.vals.ptr;
+    a.out = (float *)g_ws.out.ptr;
+    a.nb = nb;
+    a.out_rows = tmpI;
+    a.nmodes = N;
+    a.mode = mode;
+    for (sptIndex i = 0; i < N; ++i) a.order[i] = mats_order[i];
+    a.rank = mats[mode]->ncols;
+    a.stride = stride;
+    a.sb_bits = h->sb_bits;
+    for (sptIndex m = 0; m < N; ++m) a.ndims[m] = h->ndims[m];
+    H(sptgb_dbuf_reserve(&g_ws.flag, 2 * sizeof(unsigned int)));
+    a.err = (unsigned int *)g_ws.flag.ptr;
+    C(cudaMemsetAsync(a.err, 0, sizeof(unsigned int), s));
+    C(sptgb_mttkrp_hicoo(&a, s));
+    unsigned int herr = 0;
+    C(cudaMemcpyAsync(&herr, a.err, sizeof herr, cudaMemcpyDeviceToHost, s));
+    if (tmpI) C(cudaMemcpyAsync(mats[N]->values, g_ws.out.ptr, (size_t)tmpI * stride * 4, cudaMemcpyDeviceToHost, s));
+    C(cudaStreamSynchronize(s));
+    if (herr) {
+        spt_ComplainError(module, SPTERR_VALUE_ERROR, __FILE__, __LINE__,
+                          "a coordinate is not smaller than its mode size");
+        r = SPTERR_VALUE_ERROR;
+    }
+out:
+    sptgb_unlock();
+    return r;
+}
+
+int sptMTTKRPHiCOO(sptSparseTensorHiCOO const *const hitsr, sptMatrix *mats[], sptIndex const mats_order[],
+                   sptIndex const mode) {
+    return hicoo_mttkrp(hitsr, mats, mats_order, mode, "GPU HiCOO SpTns MTTKRP");
+}
+
+int sptOmpMTTKRPHiCOO(sptSparseTensorHiCOO const *const hitsr, sptMatrix *mats[], sptIndex const mats_order[],
+                      sptIndex const mode, const int nt) {
+    (void)nt;
+    return hicoo_mttkrp(hitsr, mats, mats_order, mode, "GPU HiCOO SpTns MTTKRP");
+}

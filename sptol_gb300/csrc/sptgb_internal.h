@@ -1,0 +1,182 @@
+/*
+ * Internal interface between the C host layer (csrc/host/*.c) and the CUDA
+ * translation units (csrc/cuda/*.cu).  Plain C types only; every launcher
+ * is extern "C", takes device pointers and a stream, and returns a cudaError_t
+ * value (0 on success) so that the host layer maps it to
+ * SPTERR_CUDA_ERROR + code.
+ */
+#ifndef SPTGB_INTERNAL_H
+#define SPTGB_INTERNAL_H
+
+#include <stdint.h>
+#include <stddef.h>
+#include <cuda_runtime_api.h>
+#include "../../include/ParTI.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPTGB_MAX_MODES 8
+
+/* ----------------------------------------------------------- context -- */
+int          sptgb_ctx(void);            /* lazy init; returns SptError code */
+cudaStream_t sptgb_stream(void);
+void         sptgb_count_launch(unsigned n);
+
+/* Records the error in the thread-local last-error slot and prints it like
+ * the reference's spt_ComplainError (src/error/error.c:33-60). */
+void spt_ComplainError(const char *module, int errcode, const char *file, unsigned line, const char *reason);
+int  sptgb_cuda_fail(cudaError_t e, const char *module, const char *file, unsigned line);
+
+#define SPTGB_CHECK(expr, module) do { int _e = (expr); if (_e) { \
+        spt_ComplainError(module, _e, __FILE__, __LINE__, NULL); return _e; } } while (0)
+#define SPTGB_CUDA(expr, module) do { cudaError_t _c = (expr); if (_c != cudaSuccess) \
+        return sptgb_cuda_fail(_c, module, __FILE__, __LINE__); } while (0)
+
+/* Grow-only device buffer. */
+typedef struct { void *ptr; size_t cap; } sptgb_dbuf;
+int  sptgb_dbuf_reserve(sptgb_dbuf *b, size_t bytes);
+void sptgb_dbuf_release(sptgb_dbuf *b);
+
+/* ----------------------------------------------------------- sorting --
+ * Stable LSD radix sort of (key, val) u32 pairs over key bits [0, bits).
+ * keys/vals are double buffers ([0] holds the input); on return *which
+ * tells which buffer holds the result.  tmp must hold
+ * sptgb_radix_tmp_bytes(n) bytes. */
+size_t      sptgb_radix_tmp_bytes(uint64_t n);
+cudaError_t sptgb_radix_sort_u32(uint32_t *keys[2], uint32_t *vals[2], uint64_t n, int bits,
+                                 void *tmp, int *which, cudaStream_t s);
+
+/* Key slices computed from coordinates gathered through perm:
+ *   kind 0: key = inds[mode][perm[i]] >> shift
+ *   kind 1: 32-bit slice `slice` of the 3-D Morton key (sort.c:748-805)
+ *   kind 2: 32-bit slice `slice` of the 4-D Morton key (sort.c:816-995) */
+typedef struct {
+    const uint32_t *inds[SPTGB_MAX_MODES];
+    int nmodes;
+    int kind;
+    int mode;
+    int shift;
+    int slice;
+} sptgb_keyspec;
+cudaError_t sptgb_make_keys(const sptgb_keyspec *ks, const uint32_t *perm, uint32_t *keys,
+                            uint64_t n, cudaStream_t s);
+cudaError_t sptgb_iota_u32(uint32_t *p, uint64_t n, uint32_t start, cudaStream_t s);
+/* out[i] = in[perm[i]] for 4-byte elements. */
+cudaError_t sptgb_gather_u32(const uint32_t *in, const uint32_t *perm, uint32_t *out, uint64_t n, cudaStream_t s);
+/* out[i] = in[perm[i]] for 1-byte elements. */
+cudaError_t sptgb_gather_u8(const uint8_t *in, const uint32_t *perm, uint8_t *out, uint64_t n, cudaStream_t s);
+
+/* ------------------------------------------------------- COO MTTKRP --
+ * Segmented MTTKRP over a copy sorted by the output mode. */
+typedef struct {
+    const uint32_t *rows;                      /* [nnz] output-mode coordinates, non-decreasing */
+    const uint32_t *idx[SPTGB_MAX_MODES - 1];  /* [nnz] coordinates of the product modes */
+    const void     *fac[SPTGB_MAX_MODES - 1];  /* factor rows of the product modes (f32 or bf16) */
+    const float    *vals;                      /* [nnz] */
+    float          *out;                       /* [out_rows x stride] */
+    uint64_t        nnz;
+    uint32_t        out_rows;
+    uint32_t        nprod;                     /* nmodes - 1 */
+    uint32_t        rank;
+    uint32_t        stride;
+    int             bf16;                      /* factors stored as bf16 */
+} sptgb_mttkrp_args;
+cudaError_t sptgb_mttkrp_coo(const sptgb_mttkrp_args *a, cudaStream_t s);
+
+/* ---------------------------------------------------- HiCOO pieces -- */
+/* flags[i] = 1 when nonzero i starts a new group (coordinates >> bits differ
+ * from nonzero i-1), for i in [0, n); flags[0] = 1. */
+cudaError_t sptgb_mark_groups(const uint32_t *const *inds, int nmodes, int bits, uint64_t n,
+                              uint32_t *flags, cudaStream_t s);
+/* Exclusive prefix sum of u32 flags into u32 positions; *total receives the
+ * sum (device pointer). */
+size_t      sptgb_scan_tmp_bytes(uint64_t n);
+cudaError_t sptgb_exclusive_scan_u32(const uint32_t *in, uint32_t *out, uint64_t n, uint32_t *total,
+                                     void *tmp, cudaStream_t s);
+/* For each i with flags[i]: starts[pos[i]] = i. */
+cudaError_t sptgb_compact_starts(const uint32_t *flags, const uint32_t *pos, uint64_t n, uint64_t *starts,
+                                 cudaStream_t s);
+/* For each i with flags[i]: out[pos[i]] = vals[i]. */
+cudaError_t sptgb_compact_u32(const uint32_t *flags, const uint32_t *pos, const uint32_t *vals, uint64_t n,
+                              uint32_t *out, cudaStream_t s);
+/* *unsorted (device) = 1 when v is not non-decreasing. */
+cudaError_t sptgb_check_sorted(const uint32_t *v, uint64_t n, unsigned int *unsorted, cudaStream_t s);
+/* *bad (device) = 1 when some inds[m][i] >= lims[m] (null inds[m] skipped). */
+cudaError_t sptgb_check_bounds(const uint32_t *const *inds, const uint32_t *lims, int nmodes, uint64_t n,
+                               unsigned int *bad, cudaStream_t s);
+/* HiCOO element split: einds[m][i] = inds[m][i] & ((1<<sb)-1) and, at block
+ * starts, binds[m][b] = inds[m][i] >> sb. */
+cudaError_t sptgb_hicoo_split(const uint32_t *const *inds, int nmodes, int sb_bits, uint64_t n,
+                              const uint32_t *bflags, const uint32_t *bpos,
+                              uint8_t *const *einds, uint32_t *const *binds, cudaStream_t s);
+
+typedef struct {
+    const uint64_t *bptr;                      /* [nb+1] */
+    const uint32_t *binds[SPTGB_MAX_MODES];
+    const uint8_t  *einds[SPTGB_MAX_MODES];
+    const float    *vals;
+    const float    *fac[SPTGB_MAX_MODES];      /* all factor matrices, by mode */
+    float          *out;
+    uint64_t        nb;
+    uint32_t        out_rows;
+    uint32_t        nmodes;
+    uint32_t        mode;
+    uint32_t        order[SPTGB_MAX_MODES];    /* mats_order */
+    uint32_t        rank;
+    uint32_t        stride;
+    uint32_t        sb_bits;
+    uint32_t        ndims[SPTGB_MAX_MODES];    /* elements outside are skipped and flagged */
+    unsigned int   *err;                       /* device flag, set to 1 on an out-of-range element */
+} sptgb_hicoo_args;
+cudaError_t sptgb_mttkrp_hicoo(const sptgb_hicoo_args *a, cudaStream_t s);
+
+/* ---------------------------------------------------- dense CP-ALS --
+ * FP64 pieces; matrices are row-major with `stride` floats per row. */
+typedef struct {
+    int      rank;
+    int      stride;
+    double  *ws;        /* device workspace, sptgb_dense_ws_bytes() */
+} sptgb_dense_ctx;
+size_t      sptgb_dense_ws_bytes(int rank, int max_blocks);
+/* G = A^T A in FP64 (full symmetric) over rows [0, nrows). */
+cudaError_t sptgb_gram(const float *A, uint32_t nrows, int rank, int stride, double *G, double *ws,
+                       cudaStream_t s);
+/* Builds H = Hadamard of grams[m] for m != mode (grams: host array of
+ * device pointers), factorises it (Cholesky, or LU with partial pivoting
+ * when H is not SPD) and writes S = (H^{-1})^T to Hinv.
+ * status (device int): 0 Cholesky, 1 LU fallback, 2 singular. */
+cudaError_t sptgb_solve_prepare(const double *const *grams, int nmodes, int mode, int rank,
+                                double *Hinv, int *status, cudaStream_t s);
+/* X[i,:] solves H x = M[i,:] for i < nrows (FP64 arithmetic, FP32
+ * storage) given S = (H^{-1})^T; leaves per-block partials of X^T X and of
+ * the column maxima in ws for sptgb_normalize.  X must not alias M. */
+cudaError_t sptgb_solve_rows(const float *M, float *X, uint32_t nrows, int rank, int stride,
+                             const double *S, double *ws, cudaStream_t s);
+/* lambda from those partials (2-norm when use_2norm, else the column maximum
+ * clamped to >= 1, matrix.c:390-554), X's columns divided by lambda, and
+ * gram = the Gram matrix of the normalised X. */
+cudaError_t sptgb_normalize(float *X, uint32_t nrows, int rank, int stride, double *gram,
+                            int use_2norm, float *lambda_f32, const double *ws, cudaStream_t s);
+/* <X, K> = sum_r lambda_r sum_i A[i,r] M[i,r] and ||K||^2 from the Grams
+ * (grams: host array of device pointers); writes the fit into *fit_out
+ * given normX2 (device double). */
+cudaError_t sptgb_fit(const float *A, const float *M, uint32_t nrows, int rank, int stride,
+                      const float *lambda, const double *const *grams, int nmodes,
+                      const double *normX2, double *fit_out, double *ws, cudaStream_t s);
+/* sum of squares of values in FP64. */
+cudaError_t sptgb_sumsq(const float *v, uint64_t n, double *out, double *ws, cudaStream_t s);
+/* Column 2-norms of A (FP64 accumulate) into lambda (float) and A /= lambda
+ * (GetFinalLambda multiplies these into the running lambda). */
+cudaError_t sptgb_colnorm_scale(float *A, uint32_t nrows, int rank, int stride, float *lambda_mul,
+                                double *ws, cudaStream_t s);
+
+/* ------------------------------------------------- BF16 conversion -- */
+cudaError_t sptgb_f32_to_bf16(const float *in, uint16_t *out, uint64_t n, cudaStream_t s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

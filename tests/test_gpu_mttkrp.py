@@ -1,0 +1,138 @@
+"""COO MTTKRP on the GPU through the drop-in C API, against the reference's
+own outputs (tests/golden) and the oracle.
+
+Tolerance: relative Frobenius error <= 1e-5 against the reference's
+sequential FP32 sptMTTKRP (the spec criterion); against the FP64 oracle
+where the reference's own FP32 summation error would dominate.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+import sptol_gb300 as S
+from conftest import golden, rel_fro
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+
+
+def _mats(g, N, rank):
+    return [S.Matrix.from_array(g["mat%d" % m][:, :rank]) for m in range(N)]
+
+
+def _with_out(mats, ndims, rank):
+    return mats + [S.Matrix(max(ndims), rank)]
+
+
+@pytest.mark.parametrize("case", ["mttkrp_3d_r16", "mttkrp_3d_r17", "mttkrp_4d_r8"])
+@pytest.mark.parametrize("entry", ["sptMTTKRP", "sptCudaMTTKRP"])
+def test_golden_all_modes(case, entry):
+    g = golden(case)
+    ndims = [int(x) for x in g["ndims"]]
+    rank = int(g["rank"])
+    N = len(ndims)
+    t = S.Tensor.from_arrays(ndims, g["inds"], g["vals"])
+    mats = _with_out(_mats(g, N, rank), ndims, rank)
+    for mode in range(N):
+        out = S.mttkrp(t, mats, mode, entry=entry)
+        assert rel_fro(out, g["out%d" % mode][:, :rank]) <= TOL, (case, mode)
+        # padding columns of the output stay zero, as the reference's memset leaves them
+        assert not mats[N].array()[: ndims[mode], rank:].any()
+
+
+def test_unsorted_input_and_mats_order():
+    g = golden("mttkrp_4d_r8")
+    ndims = [int(x) for x in g["ndims"]]
+    rank = int(g["rank"])
+    rng = np.random.default_rng(5)
+    p = rng.permutation(g["vals"].shape[0])
+    inds, vals = g["inds"][:, p], g["vals"][p]
+    t = S.Tensor.from_arrays(ndims, inds, vals)
+    mats = _with_out(_mats(g, 4, rank), ndims, rank)
+    facs = [g["mat%d" % m] for m in range(4)]
+    for mode in range(4):
+        order = [mode] + [m for m in (3, 2, 1, 0) if m != mode]
+        out = S.mttkrp(t, mats, mode, mats_order=order)
+        ref = O.mttkrp(ndims, inds, vals, facs, rank, mode, order=order)
+        assert rel_fro(out, ref) <= TOL
+
+
+def test_empty_single_and_heavy_row():
+    ndims = [7, 5, 3]
+    rank = 8
+    rng = np.random.default_rng(7)
+    facs = [rng.random((d, 8), dtype=np.float32) for d in ndims]
+    mats = _with_out([S.Matrix.from_array(f) for f in facs], ndims, rank)
+    # empty tensor: every output row is zero
+    t0 = S.Tensor.from_arrays(ndims, np.zeros((3, 0), np.uint32), np.zeros(0, np.float32))
+    mats[3].array()[:] = 1.0
+    out = S.mttkrp(t0, mats, 1)
+    assert out.shape == (5, rank) and not out.any()
+    # one nonzero
+    t1 = S.Tensor.from_arrays(ndims, np.array([[6], [4], [2]], np.uint32), np.array([2.0], np.float32))
+    out = S.mttkrp(t1, mats, 0)
+    exp = np.zeros((7, rank), np.float32)
+    exp[6] = 2.0 * facs[1][4] * facs[2][2]
+    assert np.allclose(out, exp, rtol=1e-6)
+    # every nonzero in one output row, long enough to span many work units
+    big = [3, 4000, 64]
+    n = 150000
+    inds = np.stack([np.full(n, 1), rng.integers(0, big[1], n), rng.integers(0, big[2], n)]).astype(np.uint32)
+    vals = rng.random(n, dtype=np.float32)
+    bf = [rng.random((d, 16), dtype=np.float32) for d in big]
+    bm = _with_out([S.Matrix.from_array(f) for f in bf], big, 16)
+    tb = S.Tensor.from_arrays(big, inds, vals)
+    out = S.mttkrp(tb, bm, 0)
+    ref = O.mttkrp(big, inds, vals, [np.pad(f, ((0, 0), (0, 0))) for f in bf], 16, 0, precision="f64")
+    assert rel_fro(out, ref) <= TOL
+    assert not out[0].any() and not out[2].any()
+
+
+def test_shape_mismatch_is_an_error():
+    ndims = [4, 3, 2]
+    t = S.Tensor.from_arrays(ndims, np.zeros((3, 1), np.uint32), np.ones(1, np.float32))
+    mats = [S.Matrix(4, 8), S.Matrix(3, 8), S.Matrix(5, 8), S.Matrix(4, 8)]
+    with pytest.raises(S.SptError) as e:
+        S.mttkrp(t, mats, 0)
+    assert e.value.code == 2
+
+
+def test_out_of_range_coordinate_is_rejected():
+    ndims = [4, 3, 2]
+    t = S.Tensor.from_arrays(ndims, np.array([[3], [3], [1]], np.uint32), np.ones(1, np.float32))
+    mats = [S.Matrix(4, 8), S.Matrix(3, 8), S.Matrix(2, 8), S.Matrix(4, 8)]
+    with pytest.raises(S.SptError) as e:
+        S.mttkrp(t, mats, 0)
+    assert e.value.code == 3
+
+
+def _c1_tensor():
+    spec = S.GenSpec()
+    spec.seed = 0
+    spec.nmodes = 3
+    for m in range(3):
+        spec.ndims[m] = 1024
+    spec.count = 1_000_000
+    spec.merge_duplicates = 1
+    spec.value_dist = S.VAL_U01
+    return S.Tensor.generate(spec)
+
+
+def test_c1_full_size_against_reference_summary_and_oracle():
+    """The 1024^3 / 1,000,000-draw tensor, rank 16, every mode."""
+    g = golden("c1_summary")
+    t = _c1_tensor()
+    assert t.nnz == int(g["nnz"])
+    inds, vals = t.arrays()
+    ndims = [1024] * 3
+    mats = S.new_factors(ndims, 16, seed=1)
+    facs = [m.array()[:1024].copy() for m in mats[:3]]
+    rows = g["sample_rows"]
+    for mode in range(3):
+        out = S.mttkrp(t, mats, mode, entry="sptCudaMTTKRP").astype(np.float64)
+        ref = O.mttkrp(ndims, inds, vals, facs, 16, mode)
+        f64 = O.mttkrp(ndims, inds, vals, facs, 16, mode, precision="f64")
+        assert rel_fro(out, ref) <= TOL
+        assert rel_fro(out, f64) <= TOL
+        assert abs(np.linalg.norm(out) - float(g["norm%d" % mode])) <= 1e-5 * float(g["norm%d" % mode])
+        assert rel_fro(out[rows], g["rows%d" % mode]) <= TOL
