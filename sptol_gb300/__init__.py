@@ -204,7 +204,8 @@ class Tensor:
         for m in range(N):
             _check(L.sptResizeIndexVector(C.byref(t.s.inds[m]), n), "sptResizeIndexVector")
             if n:
-                C.memmove(t.s.inds[m].data, np.ascontiguousarray(inds[m], dtype=np.uint32).ctypes.data, 4 * n)
+                row = np.ascontiguousarray(inds[m], dtype=np.uint32)  # keep alive across memmove
+                C.memmove(t.s.inds[m].data, row.ctypes.data, 4 * n)
         _check(L.sptResizeValueVector(C.byref(t.s.values), n), "sptResizeValueVector")
         if n:
             C.memmove(t.s.values.data, vals.ctypes.data, 4 * n)

@@ -1,0 +1,84 @@
+"""The C-ABI boundary without a GPU: the library loads, exports every function
+include/*.h declares, and its struct layouts equal the reference's."""
+import ctypes as C
+import os
+import re
+import subprocess
+import tempfile
+
+import pytest
+
+import sptol_gb300 as S
+from conftest import ROOT
+
+HEADERS = [os.path.join(ROOT, "include", h) for h in ("ParTI.h", "sptgb.h")]
+
+
+def declared_functions():
+    names = set()
+    for h in HEADERS:
+        src = open(h).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"^\s*[A-Za-z_][\w\s\*]*?\b([A-Za-z_]\w*)\s*\(", src, flags=re.M):
+            name = m.group(1)
+            if name in ("if", "for", "while", "return", "sizeof", "defined"):
+                continue
+            names.add(name)
+    return sorted(names)
+
+
+def test_library_loads_and_exports_every_declared_symbol():
+    L = S.lib()
+    names = declared_functions()
+    assert len(names) > 60
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+
+
+LAYOUT_PROBE = r"""
+#include <stdio.h>
+#include <stddef.h>
+#include <ParTI.h>
+#define P(T) printf(#T " %zu\n", sizeof(T));
+#define O(T, f) printf(#T "." #f " %zu\n", offsetof(T, f));
+int main(void) {
+  P(sptIndexVector) P(sptValueVector) P(sptNnzIndexVector) P(sptElementIndexVector)
+  P(sptMatrix) P(sptRankMatrix) P(sptSparseTensor) P(sptSparseTensorHiCOO) P(sptKruskalTensor)
+  O(sptSparseTensor, nnz) O(sptSparseTensor, inds) O(sptSparseTensor, values)
+  O(sptMatrix, stride) O(sptMatrix, values)
+  O(sptSparseTensorHiCOO, sb_bits) O(sptSparseTensorHiCOO, sc_bits) O(sptSparseTensorHiCOO, kptr)
+  O(sptSparseTensorHiCOO, kschr) O(sptSparseTensorHiCOO, nkiters) O(sptSparseTensorHiCOO, cptr)
+  O(sptSparseTensorHiCOO, knnzs) O(sptSparseTensorHiCOO, bptr) O(sptSparseTensorHiCOO, binds)
+  O(sptSparseTensorHiCOO, einds) O(sptSparseTensorHiCOO, values)
+  O(sptKruskalTensor, lambda) O(sptKruskalTensor, fit) O(sptKruskalTensor, factors)
+  return 0;
+}
+"""
+
+
+def layout(include_dir, extra=()):
+    with tempfile.TemporaryDirectory() as d:
+        src = os.path.join(d, "p.c")
+        exe = os.path.join(d, "p")
+        open(src, "w").write(LAYOUT_PROBE)
+        subprocess.run(["gcc", "-std=gnu99", "-I", include_dir] + list(extra) + [src, "-o", exe], check=True,
+                       capture_output=True)
+        out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout
+    return dict(l.rsplit(" ", 1) for l in out.strip().splitlines())
+
+
+def test_ctypes_mirror_matches_header():
+    ours = layout(os.path.join(ROOT, "include"))
+    assert int(ours["sptSparseTensor"]) == C.sizeof(S.SparseTensorS)
+    assert int(ours["sptMatrix"]) == C.sizeof(S.MatrixS)
+    assert int(ours["sptSparseTensorHiCOO"]) == C.sizeof(S.HiCOOS)
+    assert int(ours["sptKruskalTensor"]) == C.sizeof(S.KruskalS)
+    assert int(ours["sptSparseTensorHiCOO.bptr"]) == S.HiCOOS.bptr.offset
+
+
+@pytest.mark.skipif(not os.path.isdir("/root/reference/include"), reason="reference headers not present")
+def test_struct_layouts_equal_reference():
+    ours = layout(os.path.join(ROOT, "include"))
+    ref = layout("/root/reference/include", ["-DPARTI_INDEX_TYPEWIDTH=32", "-DPARTI_VALUE_TYPEWIDTH=32",
+                                             "-DPARTI_ELEMENT_INDEX_TYPEWIDTH=8", "-DPARTI_USE_OPENMP", "-fopenmp"])
+    assert ours == ref

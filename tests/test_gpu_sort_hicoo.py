@@ -1,0 +1,135 @@
+"""Device sorts and COO -> HiCOO conversion: bit-exact against the reference's
+own outputs (tests/golden) and against the oracle on larger inputs; HiCOO
+MTTKRP within the MTTKRP tolerance."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle as O
+import sptol_gb300 as S
+from conftest import golden, rel_fro
+
+pytestmark = pytest.mark.gpu
+
+
+def _tensor(g, key_i="inds", key_v="vals"):
+    ndims = [int(x) for x in g["ndims"]]
+    return ndims, S.Tensor.from_arrays(ndims, g[key_i], g[key_v])
+
+
+@pytest.mark.parametrize("case", ["sort_3d", "sort_4d"])
+def test_sort_golden(case):
+    g = golden(case)
+    ndims, t = _tensor(g)
+    S.lib().sptSparseTensorSortIndex(t.ptr(), 1, 1)
+    i, v = t.arrays()
+    assert np.array_equal(i, g["lex_inds"]) and np.array_equal(v, g["lex_vals"])
+    assert t.sortorder == list(range(len(ndims)))
+    ndims, t = _tensor(g)
+    order = np.ascontiguousarray(g["order"], np.uint32)
+    S.lib().sptSparseTensorSortIndexCustomOrder(t.ptr(), order.ctypes.data_as(C.POINTER(C.c_uint32)), 1, 1)
+    i, v = t.arrays()
+    assert np.array_equal(i, g["custom_inds"]) and np.array_equal(v, g["custom_vals"])
+    assert t.sortorder == [int(x) for x in order]
+
+
+def test_sort_large_against_oracle():
+    rng = np.random.default_rng(9)
+    ndims = [3000, 70000, 257, 5]
+    n = 400000
+    inds = np.unique(np.stack([rng.integers(0, d, n + n // 4) for d in ndims]).astype(np.uint32), axis=1)
+    inds = inds[:, rng.permutation(inds.shape[1])[:n]]
+    vals = rng.random(inds.shape[1], dtype=np.float32)
+    for order in ([0, 1, 2, 3], [2, 3, 0, 1]):
+        t = S.Tensor.from_arrays(ndims, inds, vals)
+        o = np.ascontiguousarray(order, np.uint32)
+        S.lib().sptSparseTensorSortIndexCustomOrder(t.ptr(), o.ctypes.data_as(C.POINTER(C.c_uint32)), 1, 1)
+        p = O.sort_lex(inds, order)
+        i, v = t.arrays()
+        assert np.array_equal(i, inds[:, p]) and np.array_equal(v, vals[p])
+
+
+def _check_hicoo(h, g, n):
+    a = h.arrays()
+    N = len(a["binds"])
+    assert np.array_equal(a["kptr"], g["kptr"])
+    assert np.array_equal(a["cptr"], g["cptr"])
+    assert np.array_equal(a["bptr"], g["bptr"])
+    assert np.array_equal(np.stack(a["binds"]), g["binds"])
+    assert np.array_equal(np.stack(a["einds"]), g["einds"])
+    assert np.array_equal(np.array(a["nkiters"], np.uint32), g["nkiters"])
+    klen = np.array([len(r) for m in range(N) for r in a["kschr"][m]], np.uint32)
+    assert np.array_equal(klen, g["kschr_len"])
+    kflat = np.concatenate([r for m in range(N) for r in a["kschr"][m]]).astype(np.uint32)
+    assert np.array_equal(kflat, g["kschr"])
+    assert h.max_nnzb == int(g["max_nnzb"])
+
+
+@pytest.mark.parametrize("case", ["hicoo_3d_small", "hicoo_3d_skew", "hicoo_4d"])
+def test_hicoo_golden(case):
+    g = golden(case)
+    ndims, t = _tensor(g)
+    h = S.HiCOO(t, int(g["sb"]), int(g["sk"]))
+    i, v = t.arrays()
+    assert np.array_equal(i, g["sorted_inds"]) and np.array_equal(v, g["sorted_vals"])
+    _check_hicoo(h, g, t.nnz)
+    a = h.arrays()
+    assert np.array_equal(a["values"], g["sorted_vals"])
+    if "out0" in g.files:
+        rank = int(g["rank"])
+        N = len(ndims)
+        mats = [S.Matrix.from_array(g["mat%d" % m][:, :rank]) for m in range(N)] + [S.Matrix(max(ndims), rank)]
+        for mode in range(N):
+            out = S.mttkrp_hicoo(h, mats, mode)
+            assert rel_fro(out, g["out%d" % mode][:, :rank]) <= 1e-5
+
+
+def test_hicoo_skewed_against_oracle():
+    """A power-law tensor large enough for many kernels and chunks."""
+    spec = S.GenSpec()
+    spec.seed = 5
+    spec.nmodes = 3
+    for m, d in enumerate([2_000_000, 1_000_000, 20_000]):
+        spec.ndims[m] = d
+    spec.coord_dist[0] = spec.coord_dist[1] = S.DIST_ZIPF
+    spec.zipf_s[0] = spec.zipf_s[1] = 1.2
+    spec.count = 600_000
+    spec.value_dist = S.VAL_LOGNORMAL
+    t = S.Tensor.generate(spec)
+    ndims = t.ndims
+    inds, vals = t.arrays()
+    p = O.sort_hicoo(inds, 17)
+    oh = O.hicoo_build(ndims, inds[:, p], 7, 17)
+    h = S.HiCOO(t, 7, 17)
+    i2, v2 = t.arrays()
+    assert np.array_equal(i2, inds[:, p]) and np.array_equal(v2, vals[p])
+    _check_hicoo(h, oh, t.nnz)
+    rank = 16
+    mats = S.new_factors(ndims, rank, seed=4)
+    facs = [m.array()[: ndims[k]].copy() for k, m in enumerate(mats[:3])]
+    for mode in range(3):
+        out = S.mttkrp_hicoo(h, mats, mode)
+        ref = O.mttkrp(ndims, i2, v2, facs, rank, mode, precision="f64")
+        assert rel_fro(out, ref) <= 1e-5
+
+
+def test_morton_sort_matches_oracle_within_kernels():
+    rng = np.random.default_rng(2)
+    ndims = [5000, 3000, 700]
+    n = 50000
+    inds = np.unique(np.stack([rng.integers(0, d, 2 * n) for d in ndims]).astype(np.uint32), axis=1)
+    inds = inds[:, rng.permutation(inds.shape[1])[:n]]
+    vals = rng.random(inds.shape[1], dtype=np.float32)
+    t = S.Tensor.from_arrays(ndims, inds, vals)
+    assert S.lib().sptSparseTensorMixedOrder(t.ptr(), 4, 9, 1) == 0
+    p = O.sort_hicoo(inds, 9)
+    i, v = t.arrays()
+    assert np.array_equal(i, inds[:, p])
+
+
+def test_empty_tensor_conversion():
+    t = S.Tensor.from_arrays([10, 10, 10], np.zeros((3, 0), np.uint32), np.zeros(0, np.float32))
+    h = S.HiCOO(t, 2, 3)
+    a = h.arrays()
+    assert list(a["kptr"]) == [0, 1] and list(a["bptr"]) == [0, 0] and list(a["cptr"]) == [0, 1]

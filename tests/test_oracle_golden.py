@@ -1,0 +1,108 @@
+"""Pins the oracle (the C restatement in oracle/orc.c) to the reference's own
+outputs stored in tests/golden: bit-exact sorts, HiCOO arrays and MTTKRP
+(same summation order), CP-ALS fits within 1e-6."""
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import golden, rel_fro
+
+
+@pytest.mark.parametrize("case", ["sort_3d", "sort_4d"])
+def test_sorts(case):
+    g = golden(case)
+    p = O.sort_lex(g["inds"])
+    assert np.array_equal(g["inds"][:, p], g["lex_inds"]) and np.array_equal(g["vals"][p], g["lex_vals"])
+    order = [int(x) for x in g["order"]]
+    p = O.sort_lex(g["inds"], order)
+    assert np.array_equal(g["inds"][:, p], g["custom_inds"])
+
+
+@pytest.mark.parametrize("case", ["hicoo_3d_small", "hicoo_3d_skew", "hicoo_4d"])
+def test_hicoo(case):
+    g = golden(case)
+    ndims = [int(x) for x in g["ndims"]]
+    p = O.sort_hicoo(g["inds"], int(g["sk"]))
+    si = g["inds"][:, p]
+    assert np.array_equal(si, g["sorted_inds"])
+    h = O.hicoo_build(ndims, si, int(g["sb"]), int(g["sk"]))
+    for k in ("kptr", "cptr", "bptr", "binds", "einds", "nkiters", "kschr_len", "kschr"):
+        assert np.array_equal(h[k], g[k]), k
+    assert h["max_nnzb"] == int(g["max_nnzb"])
+    if "out0" in g.files:
+        rank = int(g["rank"])
+        mats = [g["mat%d" % m] for m in range(len(ndims))]
+        for mode in range(len(ndims)):
+            out = O.mttkrp_hicoo(ndims, h, g["sorted_vals"], int(g["sb"]), mats, rank, mode)
+            assert np.array_equal(out, g["out%d" % mode][:, :rank])
+
+
+@pytest.mark.parametrize("case", ["mttkrp_3d_r16", "mttkrp_3d_r17", "mttkrp_4d_r8"])
+def test_mttkrp_bitexact(case):
+    g = golden(case)
+    ndims = [int(x) for x in g["ndims"]]
+    rank = int(g["rank"])
+    mats = [g["mat%d" % m] for m in range(len(ndims))]
+    for mode in range(len(ndims)):
+        out = O.mttkrp(ndims, g["inds"], g["vals"], mats, rank, mode)
+        assert np.array_equal(out, g["out%d" % mode][:, :rank])
+        f64 = O.mttkrp(ndims, g["inds"], g["vals"], mats, rank, mode, precision="f64")
+        assert rel_fro(out, f64) <= 1e-6
+        omp = O.mttkrp(ndims, g["inds"], g["vals"], mats, rank, mode, precision="omp", tk=4)
+        assert rel_fro(omp, f64) <= 1e-6
+
+
+@pytest.mark.parametrize("case", ["cpd_3d", "cpd_4d"])
+def test_cpd_fits(case):
+    g = golden(case)
+    ndims = [int(x) for x in g["ndims"]]
+    rank, niters = int(g["rank"]), int(g["niters"])
+    init = [g["init%d" % m] for m in range(len(ndims))]
+    facs, lam, fits, it = O.cpd_als(ndims, g["inds"], g["vals"], rank, niters, 0.0, init)
+    assert it == niters
+    assert np.abs(fits - g["fits"]).max() <= 1e-6
+    assert rel_fro(lam, g["lam"]) <= 1e-4
+    assert abs(O.fit_exact(ndims, g["inds"], g["vals"], [g["final%d" % m] for m in range(len(ndims))], g["lam"])
+               - g["fits"][-1]) <= 1e-6
+
+
+def test_c1_summary_from_generator():
+    """The library generator reproduces the 1024^3 tensor the summary was taken
+    on, and the oracle reproduces the reference's per-mode outputs on it."""
+    import sptol_gb300 as S
+    g = golden("c1_summary")
+    spec = S.GenSpec()
+    spec.seed = 0
+    spec.nmodes = 3
+    for m in range(3):
+        spec.ndims[m] = 1024
+    spec.count = 1_000_000
+    spec.merge_duplicates = 1
+    spec.value_dist = S.VAL_U01
+    t = S.Tensor.generate(spec)
+    inds, vals = t.arrays()
+    assert t.nnz == int(g["nnz"])
+    ck = (inds[0].astype(np.uint64) * 1048576 * 1024 + inds[1].astype(np.uint64) * 1024 + inds[2]).sum()
+    assert np.uint64(ck) == g["key_checksum"]
+    assert vals.astype(np.float64).sum() == pytest.approx(float(g["val_sum"]), rel=1e-12)
+    mats = [m.array()[:1024].copy() for m in S.new_factors([1024] * 3, 16, seed=1)[:3]]
+    for mode in range(3):
+        out = O.mttkrp([1024] * 3, inds, vals, mats, 16, mode).astype(np.float64)
+        assert abs(np.linalg.norm(out) - float(g["norm%d" % mode])) <= 1e-6 * float(g["norm%d" % mode])
+        assert np.array_equal(out[g["sample_rows"]], g["rows%d" % mode])
+
+
+@pytest.mark.skipif(not O.ref_available(), reason="reference sources not present")
+def test_reference_library_agrees_with_oracle_on_fresh_inputs():
+    rng = np.random.default_rng(99)
+    ndims = [70, 60, 50]
+    inds = np.unique(np.stack([rng.integers(0, d, 9000) for d in ndims]).astype(np.uint32), axis=1)
+    inds = inds[:, rng.permutation(inds.shape[1])]
+    vals = rng.random(inds.shape[1], dtype=np.float32)
+    si, sv = O.ref_sort(ndims, inds, vals)
+    p = O.sort_lex(inds)
+    assert np.array_equal(si, inds[:, p])
+    mats = [rng.random((d, 8), dtype=np.float32) for d in ndims]
+    for mode in range(3):
+        r, _ = O.ref_mttkrp(ndims, inds, vals, mats, 8, mode)
+        assert np.array_equal(r, O.mttkrp(ndims, inds, vals, mats, 8, mode))
