@@ -13,7 +13,7 @@ Workload (one "step" = MTTKRP of every mode, 0, 1, 2, on one GPU):
   e2e     the same metric through the drop-in C entry point sptCudaMTTKRP with
           host buffers: every call copies the tensor and factors to the GPU,
           sorts by the output mode when needed and copies the result back.
-  roofline  the segmented MTTKRP launch (k_zero_shared + k_mttkrp_seg), per
+  roofline  the segmented MTTKRP launch (output memset + k_mttkrp_rec), per
           launch duration from CUDA events on the launching stream.
   cpu_baseline  the oracle port of sptOmpMTTKRP_Reduce (all host threads) on
           a 10M-nonzero sample tensor of the same shape and distributions.
@@ -268,7 +268,9 @@ def run_ours(args, world, rank, local):
     mats = S.new_factors(ndims, RANK, seed=1)
     dfac = [torch.from_numpy(mats[m].array()[: ndims[m]].copy()).cuda() for m in range(3)]
     dout = torch.zeros((max(ndims), stride), dtype=torch.float32, device="cuda")
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: the library kernels and the timing events share it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     sh = stream.cuda_stream
     prep_t0 = time.time()
     coo = S.DeviceCoo(t, stream=sh)
@@ -358,7 +360,7 @@ def run_ours(args, world, rank, local):
                        "parallelism": "replicas" if world > 1 else "single"},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": peak_kind,
-                         "kernel": "k_zero_shared + k_mttkrp_seg (one MTTKRP launch)",
+                         "kernel": "k_mttkrp_rec (order-3 record kernel) after the output memset, one launch per mode",
                          "ms_per_launch_by_mode": [round(x, 4) for x in per_mode]},
             "e2e": {"value": round(e2e, 2), "unit": "GB/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "entry": "sptCudaMTTKRP (host buffers)", "ms_per_step": e_s * 1e3},

@@ -6,7 +6,8 @@
  * caller keep a tensor, its per-mode segmented copies and the factor
  * matrices resident in HBM and call the same kernels on device pointers and a
  * caller-chosen CUDA stream (passed as void* so that this header does not
- * need the CUDA headers).  Nothing here has a counterpart in the reference.
+ * need the CUDA headers; NULL is the CUDA default stream, as in the CUDA
+ * runtime API).  Nothing here has a counterpart in the reference.
  */
 #ifndef SPTGB_H
 #define SPTGB_H
@@ -48,6 +49,9 @@ int  sptgbCooMTTKRP(sptgbCoo *t, sptIndex mode, const sptIndex *mats_order,
 int  sptgbCooMTTKRPBf16(sptgbCoo *t, sptIndex mode, const sptIndex *mats_order,
                         const uint16_t *const *d_mats_bf16, sptIndex rank, sptIndex stride,
                         float *d_out, void *stream);
+/* Device arrays of the copy sorted by `mode` (prepared on demand): inds[m]
+ * for m < nmodes and the values, nnz entries each, owned by t. */
+int  sptgbCooModeArrays(sptgbCoo *t, sptIndex mode, const uint32_t **inds, const float **vals, void *stream);
 sptNnzIndex sptgbCooNnz(const sptgbCoo *t);
 size_t      sptgbCooDeviceBytes(const sptgbCoo *t);
 /* Time of the last sptgbCooMTTKRP kernel sequence on its stream (ms),

@@ -142,6 +142,8 @@ def _declare(L):
         "sptgbCooMTTKRPBf16": (C.c_int, [C.c_void_p, C.c_uint32, u32p, C.POINTER(C.c_void_p), C.c_uint32,
                                          C.c_uint32, C.c_void_p, C.c_void_p]),
         "sptgbCooNnz": (C.c_uint64, [C.c_void_p]),
+        "sptgbCooModeArrays": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
+                                         C.c_void_p]),
         "sptgbCooDeviceBytes": (C.c_size_t, [C.c_void_p]),
         "sptgbCooSetTiming": (None, [C.c_void_p, C.c_int]),
         "sptgbCooLastKernelMs": (C.c_float, [C.c_void_p]),
@@ -429,6 +431,13 @@ class DeviceCoo:
         arr = (C.c_void_p * len(dev_ptrs))(*dev_ptrs)
         f = lib().sptgbCooMTTKRPBf16 if bf16 else lib().sptgbCooMTTKRP
         _check(f(self.h, mode, op, arr, rank, stride, out_ptr, stream), "sptgbCooMTTKRP")
+
+    def mode_arrays(self, mode, stream=None):
+        """Device pointers of the copy sorted by `mode`: ([inds per mode], vals)."""
+        inds = (C.c_void_p * self.nmodes)()
+        vals = C.c_void_p()
+        _check(lib().sptgbCooModeArrays(self.h, mode, inds, C.byref(vals), stream), "sptgbCooModeArrays")
+        return [int(p) for p in inds], int(vals.value)
 
     def set_timing(self, on):
         lib().sptgbCooSetTiming(self.h, 1 if on else 0)

@@ -8,6 +8,15 @@
 // output rows [0, I) are fully written (rows without nonzeros are zero, as the
 // reference's memset leaves them).
 //
+// Order 3 (the hot path) runs k_mttkrp_rec: the mode-sorted copy is stored as
+// 16-byte records {row, idx_a, idx_b, value}, so the W lanes of a worker get a
+// nonzero with one broadcast 128-bit load; record batches are software-
+// pipelined (the next batch is in flight while the current batch's factor rows
+// are gathered) and the Hadamard product uses packed FP32x2 arithmetic.  The
+// output is zeroed by one memset; rows inside a unit are written with plain
+// stores, rows shared by neighbouring units with vector atomics.  Other orders
+// run k_mttkrp_seg below.
+//
 // Work decomposition.  A "worker" is a group of W lanes that owns one nonzero
 // at a time; lane l of the group holds columns [4l, 4l+4) of the rank
 // (float4, 128-bit gathers of factor rows).  The nonzero stream is cut into
@@ -153,6 +162,114 @@ k_mttkrp_seg(sptgb_mttkrp_args a, uint32_t unit_len, uint64_t nunits) {
     }
 }
 
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) {
+    uint64_t ra = *reinterpret_cast<uint64_t *>(&a), rb = *reinterpret_cast<uint64_t *>(&b), rd;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(rd) : "l"(ra), "l"(rb));
+    return *reinterpret_cast<float2 *>(&rd);
+}
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+    uint64_t ra = *reinterpret_cast<uint64_t *>(&a), rb = *reinterpret_cast<uint64_t *>(&b);
+    uint64_t rc = *reinterpret_cast<uint64_t *>(&c), rd;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(rd) : "l"(ra), "l"(rb), "l"(rc));
+    return *reinterpret_cast<float2 *>(&rd);
+}
+
+template <int W, bool BF16>
+__device__ __forceinline__ float4 gather_row(const char *base, uint32_t row, uint32_t row_bytes) {
+    if (!BF16) return __ldg(reinterpret_cast<const float4 *>(base + (size_t)row * row_bytes));
+    const uint2 u = __ldg(reinterpret_cast<const uint2 *>(base + (size_t)row * row_bytes));
+    return make_float4(__uint_as_float(u.x << 16), __uint_as_float(u.x & 0xffff0000u), __uint_as_float(u.y << 16),
+                       __uint_as_float(u.y & 0xffff0000u));
+}
+
+// Order-3 record kernel (see the header comment).  Lanes whose columns lie
+// past the stride stay idle; columns past the rank are never stored non-zero.
+template <int W, bool BF16>
+__global__ void __launch_bounds__(BLOCK, 3)
+k_mttkrp_rec(const uint4 *__restrict__ rec, const void *__restrict__ Fa, const void *__restrict__ Fb,
+             float *__restrict__ out, uint64_t nnz, uint32_t stride, uint32_t rank, uint32_t ul, uint64_t nunits) {
+    constexpr int BATCH_R = 4;
+    const int lane = threadIdx.x & 31;
+    const int sl = lane % W;
+    const bool col_ok = (uint32_t)(sl * 4) < stride;
+    const uint32_t elem = BF16 ? 2u : 4u;
+    const uint32_t row_bytes = stride * elem;
+    const char *Al = static_cast<const char *>(Fa) + (size_t)sl * 4 * elem;
+    const char *Bl = static_cast<const char *>(Fb) + (size_t)sl * 4 * elem;
+    const int c0 = sl * 4;
+    const float4 keep = make_float4(c0 + 0 < (int)rank ? 1.f : 0.f, c0 + 1 < (int)rank ? 1.f : 0.f,
+                                    c0 + 2 < (int)rank ? 1.f : 0.f, c0 + 3 < (int)rank ? 1.f : 0.f);
+    const uint64_t worker = ((uint64_t)blockIdx.x * BLOCK + threadIdx.x) / W;
+    const uint64_t nworkers = ((uint64_t)gridDim.x * BLOCK) / W;
+
+    for (uint64_t u = worker; u < nunits; u += nworkers) {
+        const uint64_t start = u * ul;
+        const uint32_t len = (uint32_t)min((uint64_t)ul, nnz - start);
+        const uint4 *r0 = rec + start;
+        const uint32_t prev = start > 0 ? rec[start - 1].x : NONE;
+        const uint32_t next = start + len < nnz ? rec[start + len].x : NONE;
+        uint32_t cur = r0[0].x;
+        float4 acc = f4_zero();
+        auto flush = [&](bool shared) {
+            if (!col_ok) return;
+            // padding columns (past the rank) are written as zero
+            const float4 v = make_float4(keep.x != 0.f ? acc.x : 0.f, keep.y != 0.f ? acc.y : 0.f,
+                                         keep.z != 0.f ? acc.z : 0.f, keep.w != 0.f ? acc.w : 0.f);
+            store_row4(out, cur, stride, sl, v, shared);
+        };
+        auto consume = [&](const uint4 &q, const float4 &fa, const float4 &fb) {
+            if (q.x != cur) {
+                flush(cur == prev);
+                acc = f4_zero();
+                cur = q.x;
+            }
+            const float v = __uint_as_float(q.w);
+            const float2 p0 = mul2(make_float2(v, v), make_float2(fa.x, fa.y));
+            const float2 p1 = mul2(make_float2(v, v), make_float2(fa.z, fa.w));
+            const float2 s0 = fma2(p0, make_float2(fb.x, fb.y), make_float2(acc.x, acc.y));
+            const float2 s1 = fma2(p1, make_float2(fb.z, fb.w), make_float2(acc.z, acc.w));
+            acc = make_float4(s0.x, s0.y, s1.x, s1.y);
+        };
+        uint32_t k = 0;
+        uint4 qn[BATCH_R];
+        if (len >= BATCH_R) {
+#pragma unroll
+            for (int j = 0; j < BATCH_R; ++j) qn[j] = __ldg(r0 + j);
+        }
+        for (; k + BATCH_R <= len; k += BATCH_R) {
+            uint4 q[BATCH_R];
+            float4 fa[BATCH_R], fb[BATCH_R];
+#pragma unroll
+            for (int j = 0; j < BATCH_R; ++j) q[j] = qn[j];
+#pragma unroll
+            for (int j = 0; j < BATCH_R; ++j) {
+                fa[j] = col_ok ? gather_row<W, BF16>(Al, q[j].y, row_bytes) : f4_zero();
+                fb[j] = col_ok ? gather_row<W, BF16>(Bl, q[j].z, row_bytes) : f4_zero();
+            }
+            if (k + 2 * BATCH_R <= len) {
+#pragma unroll
+                for (int j = 0; j < BATCH_R; ++j) qn[j] = __ldg(r0 + k + BATCH_R + j);
+            }
+#pragma unroll
+            for (int j = 0; j < BATCH_R; ++j) consume(q[j], fa[j], fb[j]);
+        }
+        for (; k < len; ++k) {
+            const uint4 q = __ldg(r0 + k);
+            const float4 fa = col_ok ? gather_row<W, BF16>(Al, q.y, row_bytes) : f4_zero();
+            const float4 fb = col_ok ? gather_row<W, BF16>(Bl, q.z, row_bytes) : f4_zero();
+            consume(q, fa, fb);
+        }
+        flush(cur == prev || cur == next);
+    }
+}
+
+__global__ void k_pack_records(const uint32_t *__restrict__ rows, const uint32_t *__restrict__ ia,
+                               const uint32_t *__restrict__ ib, const float *__restrict__ vals, uint4 *__restrict__ rec,
+                               uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        rec[i] = make_uint4(rows[i], ia[i], ib[i], __float_as_uint(vals[i]));
+}
+
 // Zero every row that two neighbouring units share, before the main kernel
 // accumulates into it with atomics.
 __global__ void k_zero_shared(const uint32_t *__restrict__ rows, uint64_t nnz, uint32_t unit_len, uint64_t nunits,
@@ -202,7 +319,32 @@ cudaError_t launch(const sptgb_mttkrp_args &a, cudaStream_t s) {
 }
 
 template <int W, bool BF16>
+cudaError_t launch_rec(const sptgb_mttkrp_args &a, cudaStream_t s) {
+    static int max_blocks = 0;
+    if (max_blocks == 0) {
+        int dev = 0, nsm = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mttkrp_rec<W, BF16>, BLOCK, 0);
+        max_blocks = (per_sm < 1 ? 1 : per_sm) * nsm;
+    }
+    // 256-nonzero units: enough of them to balance a power-law row distribution
+    const uint32_t ul = 256;
+    const uint64_t nunits = (a.nnz + ul - 1) / ul;
+    const uint64_t wpb = BLOCK / W;
+    uint64_t blocks = (nunits + wpb - 1) / wpb;
+    if (blocks > (uint64_t)max_blocks) blocks = max_blocks;
+    cudaError_t e = cudaMemsetAsync(a.out, 0, (size_t)a.out_rows * a.stride * sizeof(float), s);
+    if (e != cudaSuccess) return e;
+    k_mttkrp_rec<W, BF16><<<(unsigned)blocks, BLOCK, 0, s>>>(static_cast<const uint4 *>(a.rec), a.fac[0], a.fac[1],
+                                                            a.out, a.nnz, a.stride, a.rank, ul, nunits);
+    sptgb_count_launch(1);
+    return cudaGetLastError();
+}
+
+template <int W, bool BF16>
 cudaError_t dispatch_np(const sptgb_mttkrp_args &a, cudaStream_t s) {
+    if (a.rec && a.nprod == 2) return launch_rec<W, BF16>(a, s);
     switch (a.nprod) {
         case 1: return launch<W, 1, BF16>(a, s);
         case 2: return launch<W, 2, BF16>(a, s);
@@ -222,6 +364,16 @@ cudaError_t dispatch_w(const sptgb_mttkrp_args &a, cudaStream_t s) {
 }
 
 }  // namespace
+
+extern "C" cudaError_t sptgb_pack_records(const uint32_t *rows, const uint32_t *ia, const uint32_t *ib,
+                                          const float *vals, void *rec, uint64_t n, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    uint64_t g = (n + 255) / 256;
+    if (g > 152ull * 16) g = 152ull * 16;
+    k_pack_records<<<(unsigned)g, 256, 0, s>>>(rows, ia, ib, vals, static_cast<uint4 *>(rec), n);
+    sptgb_count_launch(1);
+    return cudaGetLastError();
+}
 
 extern "C" cudaError_t sptgb_mttkrp_coo(const sptgb_mttkrp_args *a, cudaStream_t s) {
     if (a->stride % 8 != 0 || a->stride > 128 || a->nprod < 1 || a->nprod > SPTGB_MAX_MODES - 1)

@@ -311,7 +311,7 @@ int sptSparseTensorMixedOrder(sptSparseTensor *tsr, const sptElementIndex sb_bit
 int sptgbCooCreate(sptgbCoo **out, const sptSparseTensor *X, void *stream) {
     *out = NULL;
     SPTGB_CHECK(sptgb_ctx(), "GPU COO create");
-    const cudaStream_t s = stream ? (cudaStream_t)stream : sptgb_stream();
+    const cudaStream_t s = (cudaStream_t)stream;
     if (X->nmodes < 2 || X->nmodes > SPTGB_MAX_MODES || X->nnz >= 0xffffffffull) {
         spt_ComplainError("GPU COO create", SPTERR_VALUE_ERROR, __FILE__, __LINE__, "unsupported tensor shape");
         return SPTERR_VALUE_ERROR;
@@ -353,7 +353,7 @@ int sptgbCooPrepareMode(sptgbCoo *t, sptIndex mode, void *stream) {
     if (mode >= t->nmodes) return SPTERR_VALUE_ERROR;
     if (t->ready[mode]) return 0;
     SPTGB_CHECK(sptgb_ctx(), "GPU COO prepare");
-    const cudaStream_t s = stream ? (cudaStream_t)stream : sptgb_stream();
+    const cudaStream_t s = (cudaStream_t)stream;
     const uint64_t n = t->nnz;
     const int N = (int)t->nmodes;
     for (int m = 0; m < N; ++m)
@@ -372,6 +372,16 @@ int sptgbCooPrepareMode(sptgbCoo *t, sptIndex mode, void *stream) {
     uint32_t *perm = NULL;
     int r = sptgb_sort_perm(t->inds, N, n, passes, np, &perm, s);
     if (!r) r = sptgb_gather_tensor(t->inds, t->vals, t->minds[mode], t->mvals[mode], N, perm, n, s);
+    if (!r && N == 3) {
+        /* records {row, idx_a, idx_b, value}, a < b the two other modes */
+        const int a = mode == 0 ? 1 : 0, b = mode == 2 ? 1 : 2;
+        cudaError_t e = cudaMalloc(&t->mrec[mode], (n ? n : 1) * 16);
+        if (e == cudaSuccess)
+            e = sptgb_pack_records(t->minds[mode][mode], t->minds[mode][a], t->minds[mode][b], t->mvals[mode],
+                                   t->mrec[mode], n, s);
+        if (e != cudaSuccess) r = sptgb_cuda_fail(e, "GPU COO prepare", __FILE__, __LINE__);
+        t->bytes += (size_t)n * 16;
+    }
     if (!r) {
         cudaError_t e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) r = sptgb_cuda_fail(e, "GPU COO prepare", __FILE__, __LINE__);
@@ -385,15 +395,22 @@ static int coo_mttkrp(sptgbCoo *t, sptIndex mode, const sptIndex *mats_order, co
                       sptIndex rank, sptIndex stride, float *d_out, void *stream, int bf16) {
     if (mode >= t->nmodes) return SPTERR_VALUE_ERROR;
     SPTGB_CHECK(sptgbCooPrepareMode(t, mode, stream), "GPU COO MTTKRP");
-    const cudaStream_t s = stream ? (cudaStream_t)stream : sptgb_stream();
+    const cudaStream_t s = (cudaStream_t)stream;
     sptgb_mttkrp_args a;
     memset(&a, 0, sizeof a);
     a.rows = t->minds[mode][mode];
     for (sptIndex i = 1; i < t->nmodes; ++i) {
         const sptIndex pm = mats_order[i];
-        if (pm >= t->nmodes) return SPTERR_VALUE_ERROR;
+        if (pm >= t->nmodes || pm == mode) return SPTERR_VALUE_ERROR;
         a.idx[i - 1] = t->minds[mode][pm];
         a.fac[i - 1] = d_mats[pm];
+    }
+    if (t->nmodes == 3 && t->mrec[mode]) {
+        /* the records hold the two other modes in ascending order */
+        const sptIndex ma = mode == 0 ? 1 : 0, mb = mode == 2 ? 1 : 2;
+        a.rec = t->mrec[mode];
+        a.fac[0] = d_mats[ma];
+        a.fac[1] = d_mats[mb];
     }
     a.vals = t->mvals[mode];
     a.out = d_out;
@@ -429,6 +446,14 @@ int sptgbCooMTTKRPBf16(sptgbCoo *t, sptIndex mode, const sptIndex *mats_order, c
     return coo_mttkrp(t, mode, mats_order, (const void *const *)d_mats_bf16, rank, stride, d_out, stream, 1);
 }
 
+int sptgbCooModeArrays(sptgbCoo *t, sptIndex mode, const uint32_t **inds, const float **vals, void *stream) {
+    if (mode >= t->nmodes) return SPTERR_VALUE_ERROR;
+    SPTGB_CHECK(sptgbCooPrepareMode(t, mode, stream), "GPU COO arrays");
+    for (sptIndex m = 0; m < t->nmodes; ++m) inds[m] = t->minds[mode][m];
+    *vals = t->mvals[mode];
+    return 0;
+}
+
 sptNnzIndex sptgbCooNnz(const sptgbCoo *t) { return t->nnz; }
 size_t sptgbCooDeviceBytes(const sptgbCoo *t) { return t->bytes; }
 void sptgbCooSetTiming(sptgbCoo *t, int enable) { t->timing = enable; }
@@ -441,6 +466,7 @@ void sptgbCooFree(sptgbCoo *t) {
         for (int k = 0; k < SPTGB_MAX_MODES; ++k)
             if (t->minds[m][k]) cudaFree(t->minds[m][k]);
         if (t->mvals[m]) cudaFree(t->mvals[m]);
+        if (t->mrec[m]) cudaFree(t->mrec[m]);
     }
     if (t->vals) cudaFree(t->vals);
     if (t->ev0) cudaEventDestroy(t->ev0);

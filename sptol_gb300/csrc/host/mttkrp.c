@@ -20,7 +20,34 @@
 #include <stdlib.h>
 #include <string.h>
 #include <cuda_runtime_api.h>
+#include <time.h>
 #include "devtensor.h"
+
+/* SPTGB_TRACE=1 prints the wall time of each phase of a host-buffer call to
+ * stderr (the reference prints its H2D / kernel / D2H times the same way,
+ * src/sptensor/mttkrp_cuda_onekernel.cu:151-155, :381-404). */
+static int trace_on(void) {
+    static int on = -1;
+    if (on < 0) {
+        const char *e = getenv("SPTGB_TRACE");
+        on = (e && e[0] && e[0] != '0') ? 1 : 0;
+    }
+    return on;
+}
+static double wall(void) {
+    struct timespec t;
+    clock_gettime(CLOCK_MONOTONIC, &t);
+    return t.tv_sec + 1e-9 * t.tv_nsec;
+}
+#define TRACE(name)                                                              \
+    do {                                                                         \
+        if (trace_on()) {                                                        \
+            cudaStreamSynchronize(s);                                            \
+            const double _t = wall();                                            \
+            fprintf(stderr, "[sptgb trace] %-10s %8.3f ms\n", name, (_t - t_prev) * 1e3); \
+            t_prev = _t;                                                         \
+        }                                                                        \
+    } while (0)
 
 static int check_mats(sptIndex nmodes, const sptIndex *ndims, sptMatrix *mats[], sptIndex mode, const char *module) {
     if (nmodes < 2 || nmodes > SPTGB_MAX_MODES || mode >= nmodes) {
@@ -62,6 +89,7 @@ static int mttkrp_host_locked(sptSparseTensor const *X, sptMatrix *mats[], sptIn
     const sptIndex R = mats[mode]->ncols;
     const sptIndex tmpI = mats[mode]->nrows;
     sptMatrix *M = mats[N];
+    double t_prev = wall();
 
     int need[SPTGB_MAX_MODES] = {0};
     need[mode] = 1;
@@ -77,6 +105,7 @@ static int mttkrp_host_locked(sptSparseTensor const *X, sptMatrix *mats[], sptIn
         SPTGB_CUDA(cudaMemsetAsync(g_ws.out.ptr, 0, (size_t)tmpI * stride * sizeof(float), s), module);
     } else {
         SPTGB_CHECK(sptgb_upload_tensor(X, g_ws.inds, &g_ws.vals, need, s), module);
+        TRACE("h2d tensor");
         uint32_t *din[SPTGB_MAX_MODES] = {0};
         for (sptIndex m = 0; m < N; ++m)
             if (need[m]) din[m] = (uint32_t *)g_ws.inds[m].ptr;
@@ -88,8 +117,10 @@ static int mttkrp_host_locked(sptSparseTensor const *X, sptMatrix *mats[], sptIn
                 SPTGB_CUDA(cudaMemcpyAsync(g_ws.fac[pm].ptr, mats[pm]->values, bytes, cudaMemcpyHostToDevice, s),
                            module);
         }
+        TRACE("h2d mats");
         int unsorted = 1;
         SPTGB_CHECK(sptgb_validate(din, X->ndims, (int)N, n, din[mode], &unsorted, s), module);
+        TRACE("validate");
         uint32_t *rows = din[mode];
         uint32_t *cols[SPTGB_MAX_MODES] = {0};
         float *vals = (float *)g_ws.vals.ptr;
@@ -111,6 +142,7 @@ static int mttkrp_host_locked(sptSparseTensor const *X, sptMatrix *mats[], sptIn
             for (sptIndex m = 0; m < N; ++m) cols[m] = dout[m];
             rows = dout[mode];
             vals = (float *)g_ws.svals.ptr;
+            TRACE("sort");
         }
         sptgb_mttkrp_args a;
         memset(&a, 0, sizeof a);
@@ -120,6 +152,12 @@ static int mttkrp_host_locked(sptSparseTensor const *X, sptMatrix *mats[], sptIn
             a.fac[i - 1] = g_ws.fac[mats_order[i]].ptr;
         }
         a.vals = vals;
+        if (N == 3) {
+            SPTGB_CHECK(sptgb_dbuf_reserve(&g_ws.misc[0], n * 16), module);
+            SPTGB_CUDA(sptgb_pack_records(rows, cols[mats_order[1]], cols[mats_order[2]], vals, g_ws.misc[0].ptr, n, s),
+                       module);
+            a.rec = g_ws.misc[0].ptr;
+        }
         a.out = (float *)g_ws.out.ptr;
         a.nnz = n;
         a.out_rows = tmpI;
@@ -127,12 +165,14 @@ static int mttkrp_host_locked(sptSparseTensor const *X, sptMatrix *mats[], sptIn
         a.rank = R;
         a.stride = stride;
         SPTGB_CUDA(sptgb_mttkrp_coo(&a, s), module);
+        TRACE("kernel");
     }
     if (tmpI)
         SPTGB_CUDA(cudaMemcpyAsync(M->values, g_ws.out.ptr, (size_t)tmpI * stride * sizeof(float),
                                    cudaMemcpyDeviceToHost, s),
                    module);
     SPTGB_CUDA(cudaStreamSynchronize(s), module);
+    TRACE("d2h out");
     return 0;
 }
 

@@ -82,8 +82,13 @@ typedef struct {
     uint32_t        rank;
     uint32_t        stride;
     int             bf16;                      /* factors stored as bf16 */
+    const void     *rec;                       /* order 3: [nnz] 16-byte records {row, idx[0], idx[1], value}
+                                                  (sptgb_pack_records); used instead of rows/idx/vals */
 } sptgb_mttkrp_args;
 cudaError_t sptgb_mttkrp_coo(const sptgb_mttkrp_args *a, cudaStream_t s);
+/* rec[i] = {rows[i], ia[i], ib[i], bits of vals[i]} for the order-3 kernel. */
+cudaError_t sptgb_pack_records(const uint32_t *rows, const uint32_t *ia, const uint32_t *ib, const float *vals,
+                               void *rec, uint64_t n, cudaStream_t s);
 
 /* ---------------------------------------------------- HiCOO pieces -- */
 /* flags[i] = 1 when nonzero i starts a new group (coordinates >> bits differ
