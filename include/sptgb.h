@@ -92,6 +92,37 @@ int sptgbFillMatrix(sptMatrix *mtx, uint64_t seed, uint64_t stream_id, float lo,
 int sptgbCpdAls(sptSparseTensor const *spten, sptIndex rank, sptIndex niters, double tol,
                 sptMatrix **mats, sptValue *lambda, double *fits, sptIndex *iters_done);
 
+/* ------------------------------------------------- batched / served CP-ALS --
+ * A server holds CP-ALS jobs of different sizes, orders (3 or 4) and ranks
+ * (<= 64) as device-resident slots: mode-sorted tensor records, factors,
+ * FP64 Grams.  One step runs one ALS iteration of every admitted job as a
+ * single CUDA-graph launch (MTTKRP, FP64 solve, normalisation and fit for all
+ * slots), then completes the jobs that reached their iteration count
+ * (GetFinalLambda, factors, lambda and per-iteration fits copied into the
+ * job's buffers).  Jobs submitted while others run are admitted at the next
+ * step as slots and HBM budget free up (continuous batching).  Each job
+ * computes what sptgbCpdAls computes for it (tol = 0).  The MTTKRP unit length
+ * per rank group is chosen by timing the candidates on the first step. */
+typedef struct sptgbServer sptgbServer;
+int  sptgbServerCreate(sptgbServer **out, size_t hbm_budget_bytes, uint32_t max_slots);
+/* Queues a job.  X, init[m] (ndims[m] x rank), out[m] (same shape), lambda[rank]
+ * and fits[niters] must stay valid until sptgbServerDone reports the job. */
+int  sptgbServerSubmit(sptgbServer *s, const sptSparseTensor *X, sptIndex rank, sptIndex niters,
+                       sptMatrix *const *init, sptMatrix *const *out, sptValue *lambda, double *fits,
+                       uint64_t *ticket);
+/* Admits what fits, runs one iteration of every admitted job, completes
+ * finished jobs.  *active / *queued receive the counts after the step. */
+int  sptgbServerStep(sptgbServer *s, uint32_t *active, uint32_t *queued);
+/* 1 once the job's results are in its buffers, 0 before; *submit_s and
+ * *done_s (CLOCK_MONOTONIC seconds) may be NULL. */
+int  sptgbServerDone(sptgbServer *s, uint64_t ticket, double *submit_s, double *done_s);
+/* Steps until every submitted job is done. */
+int  sptgbServerDrain(sptgbServer *s);
+size_t sptgbServerBytesInUse(const sptgbServer *s);
+/* Unit length (nonzeros) the autotuner chose for rank group g (W = 2<<g). */
+uint32_t sptgbServerUnitLength(const sptgbServer *s, int group);
+void sptgbServerFree(sptgbServer *s);
+
 /* ------------------------------------------------ without device allocation --
  * No counterpart in the reference.  ||X||^2 of the tensor's values, as
  * SparseTensorFrobeniusNormSquared computes it, for callers that must not

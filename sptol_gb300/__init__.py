@@ -16,7 +16,7 @@ import numpy as np
 __all__ = [
     "lib", "Tensor", "Matrix", "HiCOO", "GenSpec", "mttkrp", "mttkrp_hicoo", "cpd_als",
     "new_factors", "SptError", "DIST_UNIFORM", "DIST_ZIPF", "VAL_U01", "VAL_UPM1", "VAL_LOGNORMAL",
-    "VAL_PLANTED", "DeviceCoo",
+    "VAL_PLANTED", "DeviceCoo", "Server",
 ]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -148,6 +148,15 @@ def _declare(L):
         "sptgbCooSetTiming": (None, [C.c_void_p, C.c_int]),
         "sptgbCooLastKernelMs": (C.c_float, [C.c_void_p]),
         "sptgbCooFree": (None, [C.c_void_p]),
+        "sptgbServerCreate": (C.c_int, [C.POINTER(C.c_void_p), C.c_size_t, C.c_uint32]),
+        "sptgbServerSubmit": (C.c_int, [C.c_void_p, T, C.c_uint32, C.c_uint32, MM, MM, f32p,
+                                        C.POINTER(C.c_double), u64p]),
+        "sptgbServerStep": (C.c_int, [C.c_void_p, u32p, u32p]),
+        "sptgbServerDone": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+        "sptgbServerDrain": (C.c_int, [C.c_void_p]),
+        "sptgbServerBytesInUse": (C.c_size_t, [C.c_void_p]),
+        "sptgbServerUnitLength": (C.c_uint32, [C.c_void_p, C.c_int]),
+        "sptgbServerFree": (None, [C.c_void_p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -323,8 +332,9 @@ def _mat_array(mats):
     return arr
 
 
-def mttkrp(tensor, mats, mode, mats_order=None, entry="sptMTTKRP"):
-    """Runs the drop-in entry point `entry`; returns mats[N] rows [0, ndims[mode])."""
+def mttkrp(tensor, mats, mode, mats_order=None, entry="sptMTTKRP", copy=True):
+    """Runs the drop-in entry point `entry`; returns a copy of mats[N] rows
+    [0, ndims[mode]) (copy=False: a view of mats[N] itself)."""
     L = lib()
     N = tensor.nmodes
     if mats_order is None:
@@ -341,7 +351,8 @@ def mttkrp(tensor, mats, mode, mats_order=None, entry="sptMTTKRP"):
     else:
         raise ValueError(entry)
     _check(r, entry)
-    return mats[N].array()[: tensor.ndims[mode], : int(mats[N].s.ncols)].copy()
+    out = mats[N].array()[: tensor.ndims[mode], : int(mats[N].s.ncols)]
+    return out.copy() if copy else out
 
 
 class HiCOO:
@@ -462,3 +473,75 @@ class DeviceCoo:
 
 def launch_count():
     return int(lib().sptgbLaunchCount())
+
+
+class Server:
+    """sptgbServer handle: batched / served CP-ALS under an HBM budget.
+
+    submit() queues a job and returns its ticket; step() admits what fits and
+    runs one ALS iteration of every admitted job; result() returns a finished
+    job's (factors, lambda, fits).  The tensor, the initial factors and the
+    result buffers of a job are kept alive here until the job is done."""
+
+    QUEUED, DONE, FAILED = 0, 1, -1
+
+    def __init__(self, hbm_budget, max_slots):
+        self.h = C.c_void_p()
+        _check(lib().sptgbServerCreate(C.byref(self.h), int(hbm_budget), int(max_slots)), "sptgbServerCreate")
+        self.jobs = {}
+
+    def submit(self, tensor, rank, niters, init):
+        """init: list of N arrays (ndims[m] x rank) or Matrix objects."""
+        N = tensor.nmodes
+        ini = [a if isinstance(a, Matrix) else Matrix.from_array(a) for a in init]
+        out = [Matrix(int(tensor.ndims[m]), rank) for m in range(N)]
+        lam = np.zeros(rank, np.float32)
+        fits = np.zeros(max(niters, 1), np.float64)
+        ia, oa = _mat_array(ini), _mat_array(out)
+        t = C.c_uint64()
+        _check(lib().sptgbServerSubmit(self.h, tensor.ptr(), rank, niters, ia, oa, lam.ctypes.data_as(f32p),
+                                       fits.ctypes.data_as(C.POINTER(C.c_double)), C.byref(t)),
+               "sptgbServerSubmit")
+        self.jobs[t.value] = (tensor, ini, out, lam, fits, ia, oa, niters)
+        return t.value
+
+    def step(self):
+        a, q = C.c_uint32(), C.c_uint32()
+        _check(lib().sptgbServerStep(self.h, C.byref(a), C.byref(q)), "sptgbServerStep")
+        return int(a.value), int(q.value)
+
+    def drain(self):
+        _check(lib().sptgbServerDrain(self.h), "sptgbServerDrain")
+
+    def state(self, ticket):
+        """(state, submit time, completion time) in seconds of CLOCK_MONOTONIC."""
+        a, b = C.c_double(), C.c_double()
+        st = lib().sptgbServerDone(self.h, ticket, C.byref(a), C.byref(b))
+        return int(st), a.value, b.value
+
+    def result(self, ticket, release=True):
+        st = self.state(ticket)[0]
+        if st != self.DONE:
+            raise RuntimeError("job %d is not done (state %d)%s" % (ticket, st, _last_reason()))
+        tensor, ini, out, lam, fits, ia, oa, niters = self.jobs[ticket]
+        res = ([m.view().copy() for m in out], lam.copy(), fits[:niters].copy())
+        if release:
+            del self.jobs[ticket]
+        return res
+
+    def bytes_in_use(self):
+        return int(lib().sptgbServerBytesInUse(self.h))
+
+    def unit_length(self, group):
+        return int(lib().sptgbServerUnitLength(self.h, group))
+
+    def free(self):
+        if self.h:
+            lib().sptgbServerFree(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass

@@ -34,6 +34,7 @@
 #include <cuda_bf16.h>
 #include <stdint.h>
 #include "../sptgb_internal.h"
+#include "mttkrp_unit.cuh"
 
 namespace {
 
@@ -162,104 +163,23 @@ k_mttkrp_seg(sptgb_mttkrp_args a, uint32_t unit_len, uint64_t nunits) {
     }
 }
 
-__device__ __forceinline__ float2 mul2(float2 a, float2 b) {
-    uint64_t ra = *reinterpret_cast<uint64_t *>(&a), rb = *reinterpret_cast<uint64_t *>(&b), rd;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(rd) : "l"(ra), "l"(rb));
-    return *reinterpret_cast<float2 *>(&rd);
-}
-__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
-    uint64_t ra = *reinterpret_cast<uint64_t *>(&a), rb = *reinterpret_cast<uint64_t *>(&b);
-    uint64_t rc = *reinterpret_cast<uint64_t *>(&c), rd;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(rd) : "l"(ra), "l"(rb), "l"(rc));
-    return *reinterpret_cast<float2 *>(&rd);
-}
-
-template <int W, bool BF16>
-__device__ __forceinline__ float4 gather_row(const char *base, uint32_t row, uint32_t row_bytes) {
-    if (!BF16) return __ldg(reinterpret_cast<const float4 *>(base + (size_t)row * row_bytes));
-    const uint2 u = __ldg(reinterpret_cast<const uint2 *>(base + (size_t)row * row_bytes));
-    return make_float4(__uint_as_float(u.x << 16), __uint_as_float(u.x & 0xffff0000u), __uint_as_float(u.y << 16),
-                       __uint_as_float(u.y & 0xffff0000u));
-}
-
-// Order-3 record kernel (see the header comment).  Lanes whose columns lie
-// past the stride stay idle; columns past the rank are never stored non-zero.
-template <int W, bool BF16>
+// Order-3 record kernel (see the header comment): one work unit per worker,
+// the unit body is shared with the batched kernel (mttkrp_unit.cuh).
+// FULL: the stride is exactly 4*W floats, so every lane owns real columns.
+template <int W, bool BF16, bool FULL>
 __global__ void __launch_bounds__(BLOCK, 3)
 k_mttkrp_rec(const uint4 *__restrict__ rec, const void *__restrict__ Fa, const void *__restrict__ Fb,
              float *__restrict__ out, uint64_t nnz, uint32_t stride, uint32_t rank, uint32_t ul, uint64_t nunits) {
-    constexpr int BATCH_R = 4;
-    const int lane = threadIdx.x & 31;
-    const int sl = lane % W;
-    const bool col_ok = (uint32_t)(sl * 4) < stride;
+    const int sl = (threadIdx.x & 31) % W;
     const uint32_t elem = BF16 ? 2u : 4u;
-    const uint32_t row_bytes = stride * elem;
-    const char *Al = static_cast<const char *>(Fa) + (size_t)sl * 4 * elem;
-    const char *Bl = static_cast<const char *>(Fb) + (size_t)sl * 4 * elem;
-    const int c0 = sl * 4;
-    const float4 keep = make_float4(c0 + 0 < (int)rank ? 1.f : 0.f, c0 + 1 < (int)rank ? 1.f : 0.f,
-                                    c0 + 2 < (int)rank ? 1.f : 0.f, c0 + 3 < (int)rank ? 1.f : 0.f);
+    const char *F[2] = {static_cast<const char *>(Fa) + (size_t)sl * 4 * elem,
+                        static_cast<const char *>(Fb) + (size_t)sl * 4 * elem};
     const uint64_t worker = ((uint64_t)blockIdx.x * BLOCK + threadIdx.x) / W;
     const uint64_t nworkers = ((uint64_t)gridDim.x * BLOCK) / W;
-
     for (uint64_t u = worker; u < nunits; u += nworkers) {
         const uint64_t start = u * ul;
         const uint32_t len = (uint32_t)min((uint64_t)ul, nnz - start);
-        const uint4 *r0 = rec + start;
-        const uint32_t prev = start > 0 ? rec[start - 1].x : NONE;
-        const uint32_t next = start + len < nnz ? rec[start + len].x : NONE;
-        uint32_t cur = r0[0].x;
-        float4 acc = f4_zero();
-        auto flush = [&](bool shared) {
-            if (!col_ok) return;
-            // padding columns (past the rank) are written as zero
-            const float4 v = make_float4(keep.x != 0.f ? acc.x : 0.f, keep.y != 0.f ? acc.y : 0.f,
-                                         keep.z != 0.f ? acc.z : 0.f, keep.w != 0.f ? acc.w : 0.f);
-            store_row4(out, cur, stride, sl, v, shared);
-        };
-        auto consume = [&](const uint4 &q, const float4 &fa, const float4 &fb) {
-            if (q.x != cur) {
-                flush(cur == prev);
-                acc = f4_zero();
-                cur = q.x;
-            }
-            const float v = __uint_as_float(q.w);
-            const float2 p0 = mul2(make_float2(v, v), make_float2(fa.x, fa.y));
-            const float2 p1 = mul2(make_float2(v, v), make_float2(fa.z, fa.w));
-            const float2 s0 = fma2(p0, make_float2(fb.x, fb.y), make_float2(acc.x, acc.y));
-            const float2 s1 = fma2(p1, make_float2(fb.z, fb.w), make_float2(acc.z, acc.w));
-            acc = make_float4(s0.x, s0.y, s1.x, s1.y);
-        };
-        uint32_t k = 0;
-        uint4 qn[BATCH_R];
-        if (len >= BATCH_R) {
-#pragma unroll
-            for (int j = 0; j < BATCH_R; ++j) qn[j] = __ldg(r0 + j);
-        }
-        for (; k + BATCH_R <= len; k += BATCH_R) {
-            uint4 q[BATCH_R];
-            float4 fa[BATCH_R], fb[BATCH_R];
-#pragma unroll
-            for (int j = 0; j < BATCH_R; ++j) q[j] = qn[j];
-#pragma unroll
-            for (int j = 0; j < BATCH_R; ++j) {
-                fa[j] = col_ok ? gather_row<W, BF16>(Al, q[j].y, row_bytes) : f4_zero();
-                fb[j] = col_ok ? gather_row<W, BF16>(Bl, q[j].z, row_bytes) : f4_zero();
-            }
-            if (k + 2 * BATCH_R <= len) {
-#pragma unroll
-                for (int j = 0; j < BATCH_R; ++j) qn[j] = __ldg(r0 + k + BATCH_R + j);
-            }
-#pragma unroll
-            for (int j = 0; j < BATCH_R; ++j) consume(q[j], fa[j], fb[j]);
-        }
-        for (; k < len; ++k) {
-            const uint4 q = __ldg(r0 + k);
-            const float4 fa = col_ok ? gather_row<W, BF16>(Al, q.y, row_bytes) : f4_zero();
-            const float4 fb = col_ok ? gather_row<W, BF16>(Bl, q.z, row_bytes) : f4_zero();
-            consume(q, fa, fb);
-        }
-        flush(cur == prev || cur == next);
+        sptgb_mttkrp::unit<BF16, FULL, 2>(rec, nullptr, F, stride * elem, out, nnz, start, len, stride, rank, sl);
     }
 }
 
@@ -318,14 +238,14 @@ cudaError_t launch(const sptgb_mttkrp_args &a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-template <int W, bool BF16>
-cudaError_t launch_rec(const sptgb_mttkrp_args &a, cudaStream_t s) {
+template <int W, bool BF16, bool FULL>
+cudaError_t launch_rec_k(const sptgb_mttkrp_args &a, cudaStream_t s) {
     static int max_blocks = 0;
     if (max_blocks == 0) {
         int dev = 0, nsm = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mttkrp_rec<W, BF16>, BLOCK, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mttkrp_rec<W, BF16, FULL>, BLOCK, 0);
         max_blocks = (per_sm < 1 ? 1 : per_sm) * nsm;
     }
     // 256-nonzero units: enough of them to balance a power-law row distribution
@@ -336,10 +256,16 @@ cudaError_t launch_rec(const sptgb_mttkrp_args &a, cudaStream_t s) {
     if (blocks > (uint64_t)max_blocks) blocks = max_blocks;
     cudaError_t e = cudaMemsetAsync(a.out, 0, (size_t)a.out_rows * a.stride * sizeof(float), s);
     if (e != cudaSuccess) return e;
-    k_mttkrp_rec<W, BF16><<<(unsigned)blocks, BLOCK, 0, s>>>(static_cast<const uint4 *>(a.rec), a.fac[0], a.fac[1],
-                                                            a.out, a.nnz, a.stride, a.rank, ul, nunits);
+    k_mttkrp_rec<W, BF16, FULL><<<(unsigned)blocks, BLOCK, 0, s>>>(static_cast<const uint4 *>(a.rec), a.fac[0],
+                                                                  a.fac[1], a.out, a.nnz, a.stride, a.rank, ul,
+                                                                  nunits);
     sptgb_count_launch(1);
     return cudaGetLastError();
+}
+
+template <int W, bool BF16>
+cudaError_t launch_rec(const sptgb_mttkrp_args &a, cudaStream_t s) {
+    return a.stride == 4u * W ? launch_rec_k<W, BF16, true>(a, s) : launch_rec_k<W, BF16, false>(a, s);
 }
 
 template <int W, bool BF16>

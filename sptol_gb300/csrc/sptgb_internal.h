@@ -177,6 +177,59 @@ cudaError_t sptgb_sumsq(const float *v, uint64_t n, double *out, double *ws, cud
 cudaError_t sptgb_colnorm_scale(float *A, uint32_t nrows, int rank, int stride, float *lambda_mul,
                                 double *ws, cudaStream_t s);
 
+/* ------------------------------------------------- batched CP-ALS --
+ * Device descriptor of one tensor ("slot") of a batch.  Records for mode m
+ * are 16-byte {row, a, b, value} (order 3) or {row, a, b, c} with the value in
+ * val4[m] (order 4), a < b < c the other modes; sorted by (m, a, b, c). */
+typedef struct {
+    uint32_t nmodes, rank, stride, iter;
+    uint32_t ndims[4];
+    uint64_t nnz;
+    const void *rec[4];
+    const float *val4[4];
+    float *fac[4];
+    float *M;
+    double *gram[4];
+    double *S;
+    float *lambda;
+    double *ws;
+    double *fits;
+    double *normX2;
+    int *status;
+} sptgb_slot;
+
+/* A work list: count active entries (device u32), their slot ids and the
+ * exclusive prefix of work items per entry (pre[count] = total items). */
+typedef struct {
+    const uint32_t *count;
+    const uint32_t *ids;
+    const uint64_t *pre;
+} sptgb_wlist;
+
+/* One ALS iteration of every listed slot, as a fixed kernel sequence (graph
+ * capturable: all sizes are read from device memory).  mt[m][g]: MTTKRP unit
+ * lists of mode m for lane group g (W = 2, 4, 8, 16); dn[m]: slots with more
+ * than m modes, items = row blocks; one[m]: the same slots, one item each;
+ * zr[m]: row chunks to zero; fit: slots, items = fit blocks. */
+typedef struct {
+    sptgb_wlist mt[4][4];
+    uint32_t ul[4];
+    sptgb_wlist zr[4], one[4], dn[4], fit, fit_one;
+} sptgb_step_lists;
+cudaError_t sptgb_batch_step(const sptgb_slot *slots, const sptgb_step_lists *L, cudaStream_t s);
+/* The MTTKRP launch of mode m, lane group g alone (for timing). */
+cudaError_t sptgb_batch_mttkrp(const sptgb_slot *slots, const sptgb_wlist *w, int mode, int group, uint32_t ul,
+                               cudaStream_t s);
+/* Grid sizes the step uses, so that hosts size their prefix lists. */
+uint32_t sptgb_batch_rows_per_block(void);
+uint32_t sptgb_batch_fit_rows_per_block(void);
+uint32_t sptgb_batch_zero_rows(void);
+uint32_t sptgb_batch_max_blocks(void);
+/* Records of one mode for a batch slot: order 3 as sptgb_pack_records, order
+ * 4 with idx[2] in the fourth word and the values copied to val4. */
+cudaError_t sptgb_pack_records4(const uint32_t *rows, const uint32_t *ia, const uint32_t *ib, const uint32_t *ic,
+                                void *rec, uint64_t n, cudaStream_t s);
+
 /* ------------------------------------------------- BF16 conversion -- */
 cudaError_t sptgb_f32_to_bf16(const float *in, uint16_t *out, uint64_t n, cudaStream_t s);
 
