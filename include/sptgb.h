@@ -96,8 +96,9 @@ int sptgbCpdAls(sptSparseTensor const *spten, sptIndex rank, sptIndex niters, do
  * A server holds CP-ALS jobs of different sizes, orders (3 or 4) and ranks
  * (<= 64) as device-resident slots: mode-sorted tensor records, factors,
  * FP64 Grams.  One step runs one ALS iteration of every admitted job as a
- * single CUDA-graph launch (MTTKRP, FP64 solve, normalisation and fit for all
- * slots), then completes the jobs that reached their iteration count
+ * single CUDA-graph launch (MTTKRP, solve, normalisation and fit for all
+ * slots; the R x R factorisations in FP64, the row-wise contractions in
+ * double-float), then completes the jobs that reached their iteration count
  * (GetFinalLambda, factors, lambda and per-iteration fits copied into the
  * job's buffers).  Jobs submitted while others run are admitted at the next
  * step as slots and HBM budget free up (continuous batching).  Each job
@@ -113,9 +114,13 @@ int  sptgbServerSubmit(sptgbServer *s, const sptSparseTensor *X, sptIndex rank, 
 /* Admits what fits, runs one iteration of every admitted job, completes
  * finished jobs.  *active / *queued receive the counts after the step. */
 int  sptgbServerStep(sptgbServer *s, uint32_t *active, uint32_t *queued);
-/* 1 once the job's results are in its buffers, 0 before; *submit_s and
+/* 1 once the job's results are in its buffers, 0 before, -1 if it failed
+ * (larger than the budget, or a coordinate out of range); *submit_s and
  * *done_s (CLOCK_MONOTONIC seconds) may be NULL. */
 int  sptgbServerDone(sptgbServer *s, uint64_t ticket, double *submit_s, double *done_s);
+/* Tickets of the jobs that finished (done or failed) since the previous call,
+ * in completion order; at most `max` are returned, the rest on later calls. */
+uint32_t sptgbServerCompleted(sptgbServer *s, uint64_t *tickets, uint32_t max);
 /* Steps until every submitted job is done. */
 int  sptgbServerDrain(sptgbServer *s);
 size_t sptgbServerBytesInUse(const sptgbServer *s);

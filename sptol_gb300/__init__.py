@@ -154,6 +154,7 @@ def _declare(L):
         "sptgbServerStep": (C.c_int, [C.c_void_p, u32p, u32p]),
         "sptgbServerDone": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
         "sptgbServerDrain": (C.c_int, [C.c_void_p]),
+        "sptgbServerCompleted": (C.c_uint32, [C.c_void_p, u64p, C.c_uint32]),
         "sptgbServerBytesInUse": (C.c_size_t, [C.c_void_p]),
         "sptgbServerUnitLength": (C.c_uint32, [C.c_void_p, C.c_int]),
         "sptgbServerFree": (None, [C.c_void_p]),
@@ -278,11 +279,12 @@ class Tensor:
 class Matrix:
     """An sptMatrix allocated by sptNewMatrix (row-major, stride = ncols rounded up to 8)."""
 
-    def __init__(self, nrows, ncols):
+    def __init__(self, nrows, ncols, zero=True):
         self.s = MatrixS()
         _check(lib().sptNewMatrix(C.byref(self.s), nrows, ncols), "sptNewMatrix")
         self._owned = True
-        self.array()[:] = 0
+        if zero:
+            self.array()[:] = 0
 
     @classmethod
     def from_array(cls, a, stride_like=None):
@@ -490,11 +492,13 @@ class Server:
         _check(lib().sptgbServerCreate(C.byref(self.h), int(hbm_budget), int(max_slots)), "sptgbServerCreate")
         self.jobs = {}
 
-    def submit(self, tensor, rank, niters, init):
-        """init: list of N arrays (ndims[m] x rank) or Matrix objects."""
+    def submit(self, tensor, rank, niters, init, out=None):
+        """init: list of N arrays (ndims[m] x rank) or Matrix objects; out:
+        optional Matrix objects of the same shapes for the results."""
         N = tensor.nmodes
         ini = [a if isinstance(a, Matrix) else Matrix.from_array(a) for a in init]
-        out = [Matrix(int(tensor.ndims[m]), rank) for m in range(N)]
+        if out is None:
+            out = [Matrix(int(tensor.ndims[m]), rank, zero=False) for m in range(N)]
         lam = np.zeros(rank, np.float32)
         fits = np.zeros(max(niters, 1), np.float64)
         ia, oa = _mat_array(ini), _mat_array(out)
@@ -519,12 +523,23 @@ class Server:
         st = lib().sptgbServerDone(self.h, ticket, C.byref(a), C.byref(b))
         return int(st), a.value, b.value
 
-    def result(self, ticket, release=True):
+    def completed(self, max_n=4096):
+        """Tickets finished (done or failed) since the previous call."""
+        buf = (C.c_uint64 * max_n)()
+        n = lib().sptgbServerCompleted(self.h, buf, max_n)
+        return [int(buf[i]) for i in range(n)]
+
+    def result(self, ticket, release=True, copy=True):
+        """(factors, lambda, fits) of a finished job; copy=False returns views
+        of the job's own buffers."""
         st = self.state(ticket)[0]
         if st != self.DONE:
             raise RuntimeError("job %d is not done (state %d)%s" % (ticket, st, _last_reason()))
         tensor, ini, out, lam, fits, ia, oa, niters = self.jobs[ticket]
-        res = ([m.view().copy() for m in out], lam.copy(), fits[:niters].copy())
+        if copy:
+            res = ([m.view().copy() for m in out], lam.copy(), fits[:niters].copy())
+        else:
+            res = ([m.view() for m in out], lam, fits[:niters])
         if release:
             del self.jobs[ticket]
         return res

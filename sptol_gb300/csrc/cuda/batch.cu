@@ -112,7 +112,7 @@ __global__ void __launch_bounds__(DT) k_b_prepare(const sptgb_slot *__restrict__
     }
 }
 
-__global__ void __launch_bounds__(DT) k_b_solve(const sptgb_slot *__restrict__ slots, sptgb_wlist w, int mode) {
+__global__ void __launch_bounds__(DT, 2) k_b_solve(const sptgb_slot *__restrict__ slots, sptgb_wlist w, int mode) {
     const uint32_t cnt = *w.count;
     if (cnt == 0) return;
     const uint64_t total = w.pre[cnt];
@@ -128,12 +128,14 @@ __global__ void __launch_bounds__(DT) k_b_solve(const sptgb_slot *__restrict__ s
     }
 }
 
-__global__ void k_b_lambda(const sptgb_slot *__restrict__ slots, sptgb_wlist w, int mode) {
+// w: one item per slot; parts: the solve's list (same slots, same order), its
+// item count per slot is the number of partials to reduce.
+__global__ void k_b_lambda(const sptgb_slot *__restrict__ slots, sptgb_wlist w, sptgb_wlist parts, int mode) {
     const uint32_t cnt = *w.count;
     for (uint32_t e = blockIdx.x; e < cnt; e += gridDim.x) {
         const sptgb_slot &s = slots[w.ids[e]];
         const size_t P = (size_t)s.rank * (s.rank + 1) / 2;
-        lambda_body(s.ws, s.ws + NBLK * P, nblocks_for_rows(s.ndims[mode]), (int)s.rank, s.iter == 0 ? 1 : 0,
+        lambda_body(s.ws, s.ws + NBLK * P, (int)(parts.pre[e + 1] - parts.pre[e]), (int)s.rank, s.status[4] == 0 ? 1 : 0,
                     s.gram[mode], s.lambda, nullptr);
         __syncthreads();
     }
@@ -165,16 +167,16 @@ __global__ void __launch_bounds__(DT) k_b_fit_partial(const sptgb_slot *__restri
     }
 }
 
-__global__ void k_b_fit_final(sptgb_slot *__restrict__ slots, sptgb_wlist w, sptgb_wlist parts) {
+__global__ void k_b_fit_final(const sptgb_slot *__restrict__ slots, sptgb_wlist w, sptgb_wlist parts) {
     const uint32_t cnt = *w.count;
     for (uint32_t e = blockIdx.x; e < cnt; e += gridDim.x) {
-        sptgb_slot &s = slots[w.ids[e]];
+        const sptgb_slot &s = slots[w.ids[e]];
         GramPtrs gp;
         for (int m = 0; m < SPTGB_MAX_MODES; ++m) gp.g[m] = m < 4 && m < (int)s.nmodes ? s.gram[m] : nullptr;
         const int nbf = (int)(parts.pre[e + 1] - parts.pre[e]);
-        fit_final_body(s.ws, nbf, (int)s.rank, s.lambda, gp, (int)s.nmodes, s.normX2, s.fits + s.iter);
+        fit_final_body(s.ws, nbf, (int)s.rank, s.lambda, gp, (int)s.nmodes, s.normX2, s.fits + s.status[4]);
         __syncthreads();
-        if (threadIdx.x == 0) s.iter += 1;
+        if (threadIdx.x == 0) s.status[4] += 1;
         __syncthreads();
     }
 }
@@ -184,6 +186,156 @@ __global__ void k_pack_records4(const uint32_t *__restrict__ rows, const uint32_
                                 uint4 *__restrict__ rec, uint64_t n) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
         rec[i] = make_uint4(rows[i], ia[i], ib[i], ic[i]);
+}
+
+// ------------------------------------------------------------ admission --
+// Last job j with offs[j] <= i.
+__device__ __forceinline__ uint32_t job_of(const uint64_t *offs, uint32_t njobs, uint64_t i) {
+    uint32_t lo = 0, hi = njobs;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (offs[mid] <= i) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void k_adm_check(sptgb_adm_group g) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < g.total;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t j = job_of(g.offs, g.njobs, i);
+        const sptgb_adm_job &jb = g.jobs[j];
+        bool bad = false;
+        for (uint32_t m = 0; m < jb.nmodes && m < 4; ++m) bad |= g.ind[m][i] >= jb.ndims[m];
+        if (bad) g.err[j] = 1u;
+    }
+}
+
+__global__ void k_adm_keys(sptgb_adm_group g, int mode, int rowbits, int kind, const uint32_t *__restrict__ perm,
+                           uint32_t *__restrict__ keys) {
+    for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < g.total;
+         p += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t q = perm ? perm[p] : p;
+        const uint32_t j = job_of(g.offs, g.njobs, q);
+        const uint32_t row = g.jobs[j].nmodes > (uint32_t)mode ? g.ind[mode][q] : 0u;
+        keys[p] = kind == 0 ? ((j << rowbits) | row) : kind == 1 ? row : j;
+    }
+}
+
+__global__ void k_adm_pack(sptgb_adm_group g, const sptgb_slot *__restrict__ slots, int mode,
+                           const uint32_t *__restrict__ perm) {
+    for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < g.total;
+         p += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t j = job_of(g.offs, g.njobs, p);   // sorted by job: same job as perm[p]
+        const sptgb_adm_job &jb = g.jobs[j];
+        if (jb.nmodes <= (uint32_t)mode) continue;
+        const sptgb_slot &s = slots[jb.slot];
+        const uint64_t q = perm[p];
+        const uint64_t k = p - g.offs[j];
+        const uint32_t o0 = 0 + (0 >= mode), o1 = 1 + (1 >= mode), o2 = 2 + (2 >= mode);
+        uint4 r;
+        r.x = g.ind[mode][q];
+        r.y = g.ind[o0][q];
+        r.z = g.ind[o1][q];
+        const float v = g.val[q];
+        if (jb.nmodes == 3) {
+            r.w = __float_as_uint(v);
+        } else {
+            r.w = g.ind[o2][q];
+            const_cast<float *>(s.val4[mode])[k] = v;
+        }
+        static_cast<uint4 *>(const_cast<void *>(s.rec[mode]))[k] = r;
+    }
+}
+
+__global__ void __launch_bounds__(DT) k_adm_sumsq_partial(const sptgb_slot *__restrict__ slots, sptgb_adm_group g,
+                                                          sptgb_wlist w) {
+    const uint32_t cnt = *w.count;
+    if (cnt == 0) return;
+    const uint64_t total = w.pre[cnt];
+    for (uint64_t it = blockIdx.x; it < total; it += gridDim.x) {
+        const uint32_t e = find_entry(w.pre, cnt, it);
+        const sptgb_adm_job &jb = g.jobs[w.ids[e]];
+        const sptgb_slot &s = slots[jb.slot];
+        sumsq_partial_body(g.val + jb.off, jb.n, s.ws, (unsigned)(it - w.pre[e]), (unsigned)(w.pre[e + 1] - w.pre[e]));
+        __syncthreads();
+    }
+}
+
+__global__ void k_adm_sum_final(const sptgb_slot *__restrict__ slots, sptgb_adm_group g, sptgb_wlist w,
+                                sptgb_wlist parts) {
+    const uint32_t cnt = *w.count;
+    for (uint32_t e = blockIdx.x; e < cnt; e += gridDim.x) {
+        const sptgb_slot &s = slots[g.jobs[w.ids[e]].slot];
+        sum_final_body(s.ws, (int)(parts.pre[e + 1] - parts.pre[e]), s.normX2);
+        for (uint32_t r = threadIdx.x; r < s.rank; r += blockDim.x) s.lambda[r] = 1.0f;
+        if (threadIdx.x < 5) s.status[threadIdx.x] = 0;
+    }
+}
+
+__global__ void __launch_bounds__(DT) k_b_gram_partial(const sptgb_slot *__restrict__ slots, sptgb_wlist w, int mode) {
+    const uint32_t cnt = *w.count;
+    if (cnt == 0) return;
+    const uint64_t total = w.pre[cnt];
+    for (uint64_t it = blockIdx.x; it < total; it += gridDim.x) {
+        const uint32_t e = find_entry(w.pre, cnt, it);
+        const sptgb_slot &s = slots[w.ids[e]];
+        gram_partial_body(s.fac[mode], s.ndims[mode], (int)s.rank, (int)s.stride, s.ws, (unsigned)(it - w.pre[e]),
+                          (unsigned)(w.pre[e + 1] - w.pre[e]));
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(DT) k_b_gram_reduce(const sptgb_slot *__restrict__ slots, sptgb_wlist w,
+                                                      sptgb_wlist parts, int mode) {
+    const uint32_t cnt = *w.count;
+    for (uint32_t e = blockIdx.x; e < cnt; e += gridDim.x) {
+        const sptgb_slot &s = slots[w.ids[e]];
+        gram_reduce_body(s.ws, (int)(parts.pre[e + 1] - parts.pre[e]), (int)s.rank, s.gram[mode]);
+        __syncthreads();
+    }
+}
+
+// ----------------------------------------------------------- retirement --
+__global__ void __launch_bounds__(DT) k_b_colsq_partial(const sptgb_slot *__restrict__ slots, sptgb_wlist w, int mode) {
+    const uint32_t cnt = *w.count;
+    if (cnt == 0) return;
+    const uint64_t total = w.pre[cnt];
+    for (uint64_t it = blockIdx.x; it < total; it += gridDim.x) {
+        const uint32_t e = find_entry(w.pre, cnt, it);
+        const sptgb_slot &s = slots[w.ids[e]];
+        colsq_partial_body(s.fac[mode], s.ndims[mode], (int)s.rank, (int)s.stride, s.ws, (unsigned)(it - w.pre[e]),
+                           (unsigned)(w.pre[e + 1] - w.pre[e]));
+        __syncthreads();
+    }
+}
+
+__global__ void k_b_colnorm_final(const sptgb_slot *__restrict__ slots, sptgb_wlist w, sptgb_wlist parts, int mode) {
+    const uint32_t cnt = *w.count;
+    for (uint32_t e = blockIdx.x; e < cnt; e += gridDim.x) {
+        const sptgb_slot &s = slots[w.ids[e]];
+        colnorm_final_body(s.ws, (int)(parts.pre[e + 1] - parts.pre[e]), (int)s.rank, s.lambda,
+                           reinterpret_cast<float *>(s.ws + (size_t)NBLK * s.rank));
+    }
+}
+
+__global__ void k_b_scale_norms(const sptgb_slot *__restrict__ slots, sptgb_wlist w, int mode) {
+    const uint32_t cnt = *w.count;
+    if (cnt == 0) return;
+    const uint64_t total = w.pre[cnt];
+    for (uint64_t it = blockIdx.x; it < total; it += gridDim.x) {
+        const uint32_t e = find_entry(w.pre, cnt, it);
+        const sptgb_slot &s = slots[w.ids[e]];
+        scale_cols_body(s.fac[mode], s.ndims[mode], (int)s.rank, (int)s.stride,
+                        reinterpret_cast<const float *>(s.ws + (size_t)NBLK * s.rank), (unsigned)(it - w.pre[e]),
+                        (unsigned)(w.pre[e + 1] - w.pre[e]));
+    }
+}
+
+unsigned grid_for(uint64_t n, unsigned cap) {
+    uint64_t b = (n + 255) / 256;
+    if (b > cap) b = cap;
+    return b ? (unsigned)b : 1u;
 }
 
 int g_nsm = 0;
@@ -236,7 +388,6 @@ extern "C" cudaError_t sptgb_batch_mttkrp(const sptgb_slot *slots, const sptgb_w
 
 extern "C" cudaError_t sptgb_batch_step(const sptgb_slot *slots, const sptgb_step_lists *L, cudaStream_t s) {
     const int n = nsm();
-    sptgb_slot *mslots = const_cast<sptgb_slot *>(slots);
     for (int m = 0; m < 4; ++m) {
         k_b_zero<<<n * 8, BT, 0, s>>>(slots, L->zr[m], m);
         sptgb_count_launch(1);
@@ -245,13 +396,13 @@ extern "C" cudaError_t sptgb_batch_step(const sptgb_slot *slots, const sptgb_ste
             if (e != cudaSuccess) return e;
         }
         k_b_prepare<<<n * 2, DT, PREP_SMEM, s>>>(slots, L->one[m], m);
-        k_b_solve<<<n * 3, DT, SOLVE_SMEM, s>>>(slots, L->dn[m], m);
-        k_b_lambda<<<n * 2, DT, 0, s>>>(slots, L->one[m], m);
+        k_b_solve<<<n * 2, DT, SOLVE_SMEM, s>>>(slots, L->dn[m], m);
+        k_b_lambda<<<n * 2, DT, 0, s>>>(slots, L->one[m], L->dn[m], m);
         k_b_scale<<<n * 8, 256, 0, s>>>(slots, L->dn[m], m);
         sptgb_count_launch(4);
     }
     k_b_fit_partial<<<n * 4, DT, 0, s>>>(slots, L->fit);
-    k_b_fit_final<<<n * 2, DT, 0, s>>>(mslots, L->fit_one, L->fit);
+    k_b_fit_final<<<n * 2, DT, 0, s>>>(slots, L->fit_one, L->fit);
     sptgb_count_launch(2);
     return cudaGetLastError();
 }
@@ -263,5 +414,68 @@ extern "C" cudaError_t sptgb_pack_records4(const uint32_t *rows, const uint32_t 
     if (g > 152ull * 16) g = 152ull * 16;
     k_pack_records4<<<(unsigned)g, 256, 0, s>>>(rows, ia, ib, ic, static_cast<uint4 *>(rec), n);
     sptgb_count_launch(1);
+    return cudaGetLastError();
+}
+
+extern "C" uint32_t sptgb_sumsq_blocks(uint64_t n) {
+    uint64_t b = (n + DT - 1) / DT;
+    if (b > (uint64_t)NBLK) b = NBLK;
+    return b ? (uint32_t)b : 1u;
+}
+extern "C" uint32_t sptgb_colnorm_blocks(uint32_t nrows) {
+    uint32_t b = (nrows + 7) / 8;
+    if (b > (uint32_t)NBLK) b = NBLK;
+    return b ? b : 1u;
+}
+extern "C" uint32_t sptgb_gram_blocks(uint32_t nrows) { return (uint32_t)nblocks_for_rows(nrows); }
+
+extern "C" cudaError_t sptgb_adm_check(const sptgb_adm_group *g, cudaStream_t s) {
+    if (g->total == 0) return cudaSuccess;
+    k_adm_check<<<grid_for(g->total, 152 * 16), 256, 0, s>>>(*g);
+    sptgb_count_launch(1);
+    return cudaGetLastError();
+}
+
+extern "C" cudaError_t sptgb_adm_keys(const sptgb_adm_group *g, int mode, int rowbits, int kind,
+                                      const uint32_t *perm, uint32_t *keys, cudaStream_t s) {
+    if (g->total == 0) return cudaSuccess;
+    k_adm_keys<<<grid_for(g->total, 152 * 16), 256, 0, s>>>(*g, mode, rowbits, kind, perm, keys);
+    sptgb_count_launch(1);
+    return cudaGetLastError();
+}
+
+extern "C" cudaError_t sptgb_adm_pack(const sptgb_adm_group *g, const sptgb_slot *slots, int mode,
+                                      const uint32_t *perm, cudaStream_t s) {
+    if (g->total == 0) return cudaSuccess;
+    k_adm_pack<<<grid_for(g->total, 152 * 16), 256, 0, s>>>(*g, slots, mode, perm);
+    sptgb_count_launch(1);
+    return cudaGetLastError();
+}
+
+extern "C" cudaError_t sptgb_adm_normsq(const sptgb_slot *slots, const sptgb_adm_group *g, const sptgb_wlist *sq,
+                                        const sptgb_wlist *one, cudaStream_t s) {
+    const int n = nsm();
+    k_adm_sumsq_partial<<<n * 4, DT, 0, s>>>(slots, *g, *sq);
+    k_adm_sum_final<<<n * 2, 64, 0, s>>>(slots, *g, *one, *sq);
+    sptgb_count_launch(2);
+    return cudaGetLastError();
+}
+
+extern "C" cudaError_t sptgb_batch_gram(const sptgb_slot *slots, const sptgb_wlist *dn, const sptgb_wlist *one,
+                                        int mode, cudaStream_t s) {
+    const int n = nsm();
+    k_b_gram_partial<<<n * 3, DT, 0, s>>>(slots, *dn, mode);
+    k_b_gram_reduce<<<n * 2, DT, 0, s>>>(slots, *one, *dn, mode);
+    sptgb_count_launch(2);
+    return cudaGetLastError();
+}
+
+extern "C" cudaError_t sptgb_batch_final_lambda(const sptgb_slot *slots, const sptgb_wlist *dn,
+                                                const sptgb_wlist *one, int mode, cudaStream_t s) {
+    const int n = nsm();
+    k_b_colsq_partial<<<n * 4, DT, 0, s>>>(slots, *dn, mode);
+    k_b_colnorm_final<<<n * 2, 64, 0, s>>>(slots, *one, *dn, mode);
+    k_b_scale_norms<<<n * 8, 256, 0, s>>>(slots, *dn, mode);
+    sptgb_count_launch(3);
     return cudaGetLastError();
 }

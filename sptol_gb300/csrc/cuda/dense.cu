@@ -27,7 +27,7 @@ __global__ void __launch_bounds__(DT) k_gram_partial(const float *__restrict__ A
 __global__ void k_gram_reduce(const double *__restrict__ part, int nblk, int rank, double *__restrict__ G) { gram_reduce_body(part, nblk, rank, G); }
 __global__ void __launch_bounds__(DT) k_solve_prepare(GramPtrs grams, int nmodes, int mode, int rank, double *__restrict__ S,
                 int *__restrict__ status) { solve_prepare_body(grams, nmodes, mode, rank, S, status); }
-__global__ void __launch_bounds__(DT) k_solve_rows(const float *__restrict__ M, float *__restrict__ X, uint32_t nrows, int rank, int stride,
+__global__ void __launch_bounds__(DT, 2) k_solve_rows(const float *__restrict__ M, float *__restrict__ X, uint32_t nrows, int rank, int stride,
              const double *__restrict__ S, double *__restrict__ gpart, double *__restrict__ mpart) { solve_rows_body(M, X, nrows, rank, stride, S, gpart, mpart, blockIdx.x, gridDim.x); }
 __global__ void k_lambda(const double *__restrict__ gpart, const double *__restrict__ mpart, int nblk, int rank,
                          int use_2norm, double *__restrict__ G, float *__restrict__ lambda_f32,

@@ -1,4 +1,4 @@
-// Block-level bodies of the FP64 CP-ALS kernels, shared by the single-tensor
+// Block-level bodies of the FP64 / double-float CP-ALS kernels, shared by the single-tensor
 // kernels (dense.cu) and the batched ones (batch.cu) so that both compute the
 // same arithmetic.  Functions that walk row tiles take (bid, nbk): this block's
 // index and the number of blocks sharing the rows.  See dense.cu for the
@@ -90,6 +90,31 @@ __device__ __forceinline__ void gram_reduce_body(const double *__restrict__ part
 // positive definite, as the reference falls back from spotrf_ to sgesv_).
 struct GramPtrs { const double *g[SPTGB_MAX_MODES]; };
 
+// Rewrites the FP64 inverse S[0, RR) in place as two FP32 arrays, hi then
+// lo (hi = fl32(S), lo = fl32(S - hi)), the operand form of the double-float
+// row solve.  The buffer holds RR doubles = 2 RR floats.
+__device__ __forceinline__ void split_inverse(double *S, int RR) {
+    constexpr int PER = (RMAX * RMAX + DT - 1) / DT;
+    double v[PER];
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int e = threadIdx.x + i * DT;
+        v[i] = e < RR ? S[e] : 0.0;
+    }
+    __syncthreads();
+    float *Sf = reinterpret_cast<float *>(S);
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int e = threadIdx.x + i * DT;
+        if (e < RR) {
+            const float h = (float)v[i];
+            Sf[e] = h;
+            Sf[RR + e] = (float)(v[i] - (double)h);
+        }
+    }
+}
+
 __device__ __forceinline__ void solve_prepare_body(GramPtrs grams, int nmodes, int mode, int rank, double *__restrict__ S,
                 int *__restrict__ status) {
     extern __shared__ double sm[];
@@ -153,6 +178,7 @@ __device__ __forceinline__ void solve_prepare_body(GramPtrs grams, int nmodes, i
             S[e] = s;
         }
         if (tid == 0) *status = 0;
+        split_inverse(S, RR);
         return;
     }
 
@@ -218,71 +244,238 @@ __device__ __forceinline__ void solve_prepare_body(GramPtrs grams, int nmodes, i
         for (int i = 0; i < rank; ++i) S[j * rank + i] = x[i];
     }
     if (tid == 0) *status = singular ? 2 : 1;
+    split_inverse(S, RR);
 }
 
-// X[i, :] = M[i, :] * S (S = (H^{-1})^T, so row i of X solves H x = m_i),
-// computed in FP64, stored FP32; per-block partials of X^T X and of the
-// column maxima of the stored values.
+// X[i, :] = M[i, :] * S (S = (H^{-1})^T, so row i of X solves H x = m_i).
+// Double-float arithmetic (a value is hi + lo, two FP32 numbers, about 48
+// significant bits): the row-wise contractions of the solve run on the FP32
+// pipes, which on this GPU issue 64 times the FP64 rate.  Products of FP32
+// inputs are exact as (p, fma(a, b, -p)); sums use Knuth's TwoSum, so the only
+// rounding is in the low word.  Explicit _rn intrinsics keep the compiler from
+// contracting or reassociating the error terms.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = __fadd_rn(a, b);
+    const float bp = __fsub_rn(s, a);
+    const float ap = __fsub_rn(s, bp);
+    e = __fadd_rn(__fsub_rn(a, ap), __fsub_rn(b, bp));
+}
+
+// (hi, lo) += m * (shi + slo)
+__device__ __forceinline__ void df_fma(float &hi, float &lo, float m, float shi, float slo) {
+    const float p = __fmul_rn(m, shi);
+    const float pe = __fmaf_rn(m, shi, -p);
+    float t, e;
+    two_sum(hi, p, t, e);
+    hi = t;
+    lo = __fadd_rn(lo, __fadd_rn(e, __fmaf_rn(m, slo, pe)));
+}
+
+// (hi, lo) += a * b, exactly up to the low word's rounding
+__device__ __forceinline__ void df_prod_acc(float &hi, float &lo, float a, float b) {
+    const float p = __fmul_rn(a, b);
+    const float pe = __fmaf_rn(a, b, -p);
+    float t, e;
+    two_sum(hi, p, t, e);
+    hi = t;
+    lo = __fadd_rn(lo, __fadd_rn(e, pe));
+}
+
+__device__ __forceinline__ void df_renorm(float &hi, float &lo) {
+    const float t = __fadd_rn(hi, lo);
+    lo = __fsub_rn(lo, __fsub_rn(t, hi));
+    hi = t;
+}
+
+// Packed double-float: two independent double-float values in the x and y
+// lanes of float2 registers, advanced by the FP32x2 instructions (one
+// instruction per pair).  Same operation order as the scalar forms above.
+namespace df2 {
+__device__ __forceinline__ uint64_t u(float2 a) { return *reinterpret_cast<uint64_t *>(&a); }
+__device__ __forceinline__ float2 f(uint64_t a) { return *reinterpret_cast<float2 *>(&a); }
+__device__ __forceinline__ float2 add(float2 a, float2 b) {
+    uint64_t r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(u(a)), "l"(u(b)));
+    return f(r);
+}
+__device__ __forceinline__ float2 sub(float2 a, float2 b) {
+    uint64_t r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(u(a)), "l"(u(b)));
+    return f(r);
+}
+__device__ __forceinline__ float2 mul(float2 a, float2 b) {
+    uint64_t r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(u(a)), "l"(u(b)));
+    return f(r);
+}
+__device__ __forceinline__ float2 fma(float2 a, float2 b, float2 c) {
+    uint64_t r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(u(a)), "l"(u(b)), "l"(u(c)));
+    return f(r);
+}
+// (hi, lo) += m * (sh + sl); sn = -sh
+__device__ __forceinline__ void fma_acc(float2 &hi, float2 &lo, float2 m, float2 sh, float2 sn, float2 sl) {
+    const float2 p = mul(m, sh);
+    const float2 npe = fma(m, sn, p);   // p - m*sh exactly: minus the product's rounding error
+    const float2 t = add(hi, p);
+    const float2 bp = sub(t, hi);
+    const float2 ap = sub(t, bp);
+    const float2 e = add(sub(hi, ap), sub(p, bp));
+    lo = add(lo, fma(m, sl, sub(e, npe)));
+    hi = t;
+}
+// (hi, lo) += a * b; nb = -b
+__device__ __forceinline__ void prod_acc(float2 &hi, float2 &lo, float2 a, float2 b, float2 nb) {
+    const float2 p = mul(a, b);
+    const float2 npe = fma(a, nb, p);
+    const float2 t = add(hi, p);
+    const float2 bp = sub(t, hi);
+    const float2 ap = sub(t, bp);
+    const float2 e = add(sub(hi, ap), sub(p, bp));
+    lo = add(lo, sub(e, npe));
+    hi = t;
+}
+__device__ __forceinline__ void renorm(float2 &hi, float2 &lo) {
+    const float2 t = add(hi, lo);
+    lo = sub(lo, sub(t, hi));
+    hi = t;
+}
+// the two lanes' double-float values added: (hi, lo) scalar
+__device__ __forceinline__ void fold(float2 hi, float2 lo, float &h, float &l) {
+    float e;
+    two_sum(hi.x, hi.y, h, e);
+    l = __fadd_rn(__fadd_rn(lo.x, lo.y), e);
+}
+}  // namespace df2
+
+constexpr int LDK = RMAX + 2;   // row length of the k-major tiles (even: 8-byte pairs)
+constexpr int LDR = TR + 2;     // row length of the transposed X tile
+
+// One tile of X = M * S for a thread that owns column c0 of rows
+// r0 + j * rstep, j < NOUT; the k sum runs over pairs (k, k+1) in the two
+// lanes, which are added at the end.
+template <int NOUT>
+__device__ __forceinline__ void solve_tile_cols(const float *__restrict__ Mt, const float *__restrict__ StH,
+                                                const float *__restrict__ StN, const float *__restrict__ StL,
+                                                float *__restrict__ XT, float *__restrict__ XN, float *__restrict__ X,
+                                                uint64_t t0, uint32_t nrows, int rank2, int stride, int c0, int r0,
+                                                int rstep) {
+    float2 hi[NOUT], lo[NOUT];
+#pragma unroll
+    for (int j = 0; j < NOUT; ++j) hi[j] = lo[j] = make_float2(0.f, 0.f);
+    const float *sh_p = StH + c0 * LDK, *sn_p = StN + c0 * LDK, *sl_p = StL + c0 * LDK;
+#pragma unroll 2
+    for (int k = 0; k < rank2; k += 2) {
+        const float2 sh = *reinterpret_cast<const float2 *>(sh_p + k);
+        const float2 sn = *reinterpret_cast<const float2 *>(sn_p + k);
+        const float2 sl = *reinterpret_cast<const float2 *>(sl_p + k);
+#pragma unroll
+        for (int j = 0; j < NOUT; ++j)
+            df2::fma_acc(hi[j], lo[j], *reinterpret_cast<const float2 *>(Mt + (r0 + j * rstep) * LDK + k), sh, sn, sl);
+    }
+#pragma unroll
+    for (int j = 0; j < NOUT; ++j) {
+        float h, l;
+        df2::fold(hi[j], lo[j], h, l);
+        const int r = r0 + j * rstep;
+        const uint64_t row = t0 + r;
+        const float xf = row < nrows ? __fadd_rn(h, l) : 0.f;
+        XT[c0 * LDR + r] = xf;
+        XN[c0 * LDR + r] = -xf;
+        if (row < nrows) X[row * stride + c0] = xf;
+    }
+}
+
+// X = M * S over a grid-stride set of row tiles (S = H^{-1} from
+// solve_prepare_body, as hi and lo FP32 arrays), plus this block's partial of
+// X^T X (over the FP32 values written) and the column maxima.  Each output
+// element and each Gram entry is accumulated in double-float (packed FP32x2)
+// and rounded once: outputs to FP32, Gram partials to FP64.
 __device__ __forceinline__ void solve_rows_body(const float *__restrict__ M, float *__restrict__ X, uint32_t nrows, int rank, int stride,
              const double *__restrict__ S, double *__restrict__ gpart, double *__restrict__ mpart, unsigned bid, unsigned nbk) {
-    extern __shared__ double sm[];
-    double *Ss = sm;                        // [rank][rank]
-    double *Mt = Ss + RMAX * RMAX;          // [TR][RMAX+1]
-    double *Xt = Mt + TR * (RMAX + 1);      // [TR][RMAX+1]
+    extern __shared__ float smf[];
+    float *StH = smf;                       // [RMAX][LDK]: S^T hi, k-major per column
+    float *StN = StH + RMAX * LDK;          // -hi
+    float *StL = StN + RMAX * LDK;          // lo
+    float *Mt = StL + RMAX * LDK;           // [TR][LDK]
+    float *XT = Mt + TR * LDK;              // [RMAX][LDR]: tile of X, transposed
+    float *XN = XT + RMAX * LDR;            // -XT
     __shared__ unsigned char pp_s[PMAX], qq_s[PMAX];
-    const int ld = RMAX + 1;
     const int P = rank * (rank + 1) / 2;
-    for (int e = threadIdx.x; e < rank * rank; e += DT) Ss[e] = S[e];
+    const int RR = rank * rank;
+    const int rank2 = (rank + 1) & ~1;
+    const float *Sf = reinterpret_cast<const float *>(S);
+    for (int e = threadIdx.x; e < rank * rank2; e += DT) {
+        const int c = e / rank2, k = e % rank2;   // S[k][c]
+        const float h = k < rank ? Sf[k * rank + c] : 0.f;
+        StH[c * LDK + k] = h;
+        StN[c * LDK + k] = -h;
+        StL[c * LDK + k] = k < rank ? Sf[RR + k * rank + c] : 0.f;
+    }
     for (int i = threadIdx.x; i < P; i += DT) {
         int p, q;
         pair_of(i, rank, &p, &q);
         pp_s[i] = (unsigned char)p;
         qq_s[i] = (unsigned char)q;
     }
-    double acc[PPT];
+    float2 ghi[PPT], glo[PPT];
 #pragma unroll
-    for (int k = 0; k < PPT; ++k) acc[k] = 0.0;
-    double cmax = 0.0;   // column maximum, starting at 0 as matrix.c:484-486
+    for (int k = 0; k < PPT; ++k) ghi[k] = glo[k] = make_float2(0.f, 0.f);
+    float cmax = 0.f;   // column maximum, starting at 0 as matrix.c:484-486
+    // with rank | DT a thread keeps one column c0 and rows r0 + j * (DT / rank)
+    const bool fixed_col = (DT % rank) == 0;
+    const int c0 = threadIdx.x % rank, r0 = threadIdx.x / rank, rstep = DT / rank;
+    const int nout = (TR * rank + DT - 1) / DT;   // 1, 2, 4 or 8 when fixed_col
     for (uint64_t t0 = (uint64_t)bid * TR; t0 < nrows; t0 += (uint64_t)nbk * TR) {
         __syncthreads();
-        for (int e = threadIdx.x; e < TR * rank; e += DT) {
-            const int r = e / rank, c = e % rank;
+        for (int e = threadIdx.x; e < TR * rank2; e += DT) {
+            const int r = e / rank2, c = e % rank2;
             const uint64_t row = t0 + r;
-            Mt[r * ld + c] = row < nrows ? (double)M[row * stride + c] : 0.0;
+            Mt[r * LDK + c] = (row < nrows && c < rank) ? M[row * stride + c] : 0.f;
         }
         __syncthreads();
-        for (int e = threadIdx.x; e < TR * rank; e += DT) {
-            const int r = e / rank, c = e % rank;
-            const uint64_t row = t0 + r;
-            double s = 0.0;
-            for (int k = 0; k < rank; ++k) s = fma(Mt[r * ld + k], Ss[k * rank + c], s);
-            const float xf = (float)s;
-            Xt[r * ld + c] = row < nrows ? (double)xf : 0.0;
-            if (row < nrows) X[row * stride + c] = xf;
+        if (fixed_col) {
+            if (r0 < TR) {
+                switch (nout) {
+                    case 8: solve_tile_cols<8>(Mt, StH, StN, StL, XT, XN, X, t0, nrows, rank2, stride, c0, r0, rstep); break;
+                    case 4: solve_tile_cols<4>(Mt, StH, StN, StL, XT, XN, X, t0, nrows, rank2, stride, c0, r0, rstep); break;
+                    case 2: solve_tile_cols<2>(Mt, StH, StN, StL, XT, XN, X, t0, nrows, rank2, stride, c0, r0, rstep); break;
+                    default: solve_tile_cols<1>(Mt, StH, StN, StL, XT, XN, X, t0, nrows, rank2, stride, c0, r0, rstep); break;
+                }
+            }
+        } else {
+            for (int e = threadIdx.x; e < TR * rank; e += DT)
+                solve_tile_cols<1>(Mt, StH, StN, StL, XT, XN, X, t0, nrows, rank2, stride, e % rank, e / rank, 0);
         }
         __syncthreads();
+        // Gram partial: this thread's pairs over row pairs (r, r+1)
 #pragma unroll
         for (int k = 0; k < PPT; ++k) {
             const int i = threadIdx.x + k * DT;
             if (i < P) {
-                const int p = pp_s[i], q = qq_s[i];
-                double s = 0.0;
-#pragma unroll 8
-                for (int r = 0; r < TR; ++r) s = fma(Xt[r * ld + p], Xt[r * ld + q], s);
-                acc[k] += s;
+                const float *xp = XT + pp_s[i] * LDR, *xq = XT + qq_s[i] * LDR, *nq = XN + qq_s[i] * LDR;
+#pragma unroll 4
+                for (int r = 0; r < TR; r += 2)
+                    df2::prod_acc(ghi[k], glo[k], *reinterpret_cast<const float2 *>(xp + r),
+                                  *reinterpret_cast<const float2 *>(xq + r), *reinterpret_cast<const float2 *>(nq + r));
+                df2::renorm(ghi[k], glo[k]);
             }
         }
         if (threadIdx.x < rank) {
             for (int r = 0; r < TR; ++r)
-                if (t0 + r < nrows && Xt[r * ld + threadIdx.x] > cmax) cmax = Xt[r * ld + threadIdx.x];
+                if (t0 + r < nrows && XT[threadIdx.x * LDR + r] > cmax) cmax = XT[threadIdx.x * LDR + r];
         }
     }
 #pragma unroll
     for (int k = 0; k < PPT; ++k) {
         const int i = threadIdx.x + k * DT;
-        if (i < P) gpart[(uint64_t)bid * P + i] = acc[k];
+        if (i < P) {
+            float h, l;
+            df2::fold(ghi[k], glo[k], h, l);
+            gpart[(uint64_t)bid * P + i] = (double)h + (double)l;
+        }
     }
-    if (threadIdx.x < rank) mpart[(uint64_t)bid * rank + threadIdx.x] = cmax;
+    if (threadIdx.x < rank) mpart[(uint64_t)bid * rank + threadIdx.x] = (double)cmax;
 }
 
 // Reduces the solve statistics, forms lambda and the normalised Gram.
@@ -471,7 +664,7 @@ __host__ __device__ inline int nblocks_for_rows(uint64_t nrows) {
     return (int)b;
 }
 
-constexpr size_t SOLVE_SMEM = (size_t)(RMAX * RMAX + 2 * TR * (RMAX + 1)) * sizeof(double);
+constexpr size_t SOLVE_SMEM = (size_t)(3 * RMAX * LDK + TR * LDK + 2 * RMAX * LDR) * sizeof(float);
 constexpr size_t PREP_SMEM = (size_t)(2 * RMAX * (RMAX + 1)) * sizeof(double);
 
 

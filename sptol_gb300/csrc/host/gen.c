@@ -17,8 +17,9 @@
  *     draws (each round draws exactly the number still missing, so no round
  *     overshoots) until exactly `count` unique coordinates exist; values are
  *     then drawn per unique coordinate in sorted position order.
- * Coordinates are packed into one 64-bit key (mode 0 most significant), so
- * the bit widths of all modes must sum to at most 64.
+ * Coordinates are packed into one key (mode 0 most significant): 64 bits
+ * when the bit widths of all modes sum to at most 64, else 128 bits, sorted
+ * by the low 64 bits and then stably by the high bits.
  */
 #define _GNU_SOURCE
 #include <math.h>
@@ -186,6 +187,109 @@ static uint64_t unique_sorted(uint64_t *a, uint64_t n) {
     return w;
 }
 
+typedef unsigned __int128 u128;
+
+static void draw_keys128(const gen_ctx *g, uint64_t first, uint64_t count, u128 *keys) {
+    const sptgbGenSpec *sp = g->spec;
+#pragma omp parallel for schedule(static)
+    for (uint64_t i = 0; i < count; ++i) {
+        u128 key = 0;
+        for (sptIndex m = 0; m < sp->nmodes; ++m) {
+            const uint64_t r = rng_at(g->base[m], first + i);
+            uint32_t c;
+            if (sp->coord_dist[m] == SPTGB_DIST_ZIPF) c = zipf_sample(&g->z[m], u01d(r));
+            else c = uniform_index(r, sp->ndims[m]);
+            key |= (u128)c << g->shift[m];
+        }
+        keys[i] = key;
+    }
+}
+
+/* Stable sort of 128-bit keys (and u32 payloads): the 64-bit sort on the low
+ * halves, then on the high halves, carrying a permutation. */
+static int radix_sort_u128(u128 *keys, uint32_t *pay, uint64_t n, int bits) {
+    if (n < 2 || bits <= 0) return 0;
+    uint64_t *half = (uint64_t *)malloc(n * sizeof(uint64_t));
+    uint32_t *perm = (uint32_t *)malloc(n * sizeof(uint32_t));
+    u128 *tk = (u128 *)malloc(n * sizeof(u128));
+    uint32_t *tp = pay ? (uint32_t *)malloc(n * sizeof(uint32_t)) : NULL;
+    int r = (!half || !perm || !tk || (pay && !tp)) ? SPTERR_OS_ERROR : 0;
+    if (!r) {
+#pragma omp parallel for schedule(static)
+        for (uint64_t i = 0; i < n; ++i) {
+            half[i] = (uint64_t)keys[i];
+            perm[i] = (uint32_t)i;
+        }
+        r = radix_sort_u64(half, perm, n, bits < 64 ? bits : 64);
+    }
+    if (!r && bits > 64) {
+#pragma omp parallel for schedule(static)
+        for (uint64_t i = 0; i < n; ++i) half[i] = (uint64_t)(keys[perm[i]] >> 64);
+        r = radix_sort_u64(half, perm, n, bits - 64);
+    }
+    if (!r) {
+#pragma omp parallel for schedule(static)
+        for (uint64_t i = 0; i < n; ++i) {
+            tk[i] = keys[perm[i]];
+            if (pay) tp[i] = pay[perm[i]];
+        }
+        memcpy(keys, tk, n * sizeof(u128));
+        if (pay) memcpy(pay, tp, n * sizeof(uint32_t));
+    }
+    free(half);
+    free(perm);
+    free(tk);
+    free(tp);
+    return r;
+}
+
+/* Unique coordinates (merge_duplicates = 0) with keys wider than 64 bits:
+ * the same draw-sort-dedupe-top-up rounds as the 64-bit path. */
+static int unique_keys128(const gen_ctx *g, uint64_t target, int tb, u128 **out) {
+    u128 *keys = (u128 *)malloc((target ? target : 1) * sizeof(u128));
+    u128 *fresh = (u128 *)malloc((target ? target : 1) * sizeof(u128));
+    u128 *merged = (u128 *)malloc((target ? target : 1) * sizeof(u128));
+    if (!keys || !fresh || !merged) {
+        free(keys);
+        free(fresh);
+        free(merged);
+        return SPTERR_OS_ERROR;
+    }
+    uint64_t have = 0, drawn = 0;
+    int r = 0;
+    while (have < target) {
+        const uint64_t need = target - have;
+        draw_keys128(g, drawn, need, fresh);
+        drawn += need;
+        r = radix_sort_u128(fresh, NULL, need, tb);
+        if (r) break;
+        uint64_t nf = need ? 1 : 0;
+        for (uint64_t i = 1; i < need; ++i)
+            if (fresh[i] != fresh[nf - 1]) fresh[nf++] = fresh[i];
+        uint64_t i = 0, j = 0, w = 0;
+        while (i < have || j < nf) {
+            if (j >= nf || (i < have && keys[i] < fresh[j])) merged[w++] = keys[i++];
+            else if (i >= have || fresh[j] < keys[i]) merged[w++] = fresh[j++];
+            else {
+                merged[w++] = keys[i++];
+                ++j;
+            }
+        }
+        u128 *t = keys;
+        keys = merged;
+        merged = t;
+        have = w;
+    }
+    free(fresh);
+    free(merged);
+    if (r) {
+        free(keys);
+        return r;
+    }
+    *out = keys;
+    return 0;
+}
+
 int sptgbGenerate(sptSparseTensor *X, const sptgbGenSpec *sp) {
     const char *module = "SpTns generate";
     if (sp->nmodes < 1 || sp->nmodes > SPTGB_MAX_MODES) return SPTERR_VALUE_ERROR;
@@ -206,8 +310,9 @@ int sptgbGenerate(sptSparseTensor *X, const sptgbGenSpec *sp) {
         tb += b;
     }
     g.total_bits = tb;
-    if (tb > 64) {
-        spt_ComplainError(module, SPTERR_VALUE_ERROR, __FILE__, __LINE__, "mode bit widths exceed 64");
+    if (tb > 128 || (tb > 64 && sp->merge_duplicates)) {
+        spt_ComplainError(module, SPTERR_VALUE_ERROR, __FILE__, __LINE__,
+                          tb > 128 ? "mode bit widths exceed 128" : "merged duplicates need at most 64 key bits");
         return SPTERR_VALUE_ERROR;
     }
     uint64_t space = 1;
@@ -222,10 +327,18 @@ int sptgbGenerate(sptSparseTensor *X, const sptgbGenSpec *sp) {
         return SPTERR_VALUE_ERROR;
     }
     uint64_t *keys = NULL;
+    u128 *wkeys = NULL;
     float *vals = NULL;
     uint64_t nnz = 0;
     int r = 0;
-    if (sp->merge_duplicates) {
+    if (tb > 64) {
+        r = unique_keys128(&g, sp->count, tb, &wkeys);
+        nnz = sp->count;
+        if (!r) {
+            vals = (float *)malloc((nnz ? nnz : 1) * sizeof(float));
+            if (!vals) r = SPTERR_OS_ERROR;
+        }
+    } else if (sp->merge_duplicates) {
         const uint64_t n = sp->count;
         keys = (uint64_t *)malloc((n ? n : 1) * sizeof(uint64_t));
         uint32_t *order = (uint32_t *)malloc((n ? n : 1) * sizeof(uint32_t));
@@ -287,6 +400,7 @@ int sptgbGenerate(sptSparseTensor *X, const sptgbGenSpec *sp) {
     for (sptIndex m = 0; m < sp->nmodes; ++m) zipf_free(&g.z[m]);
     if (r) {
         free(keys);
+        free(wkeys);
         free(vals);
         return r;
     }
@@ -300,7 +414,8 @@ int sptgbGenerate(sptSparseTensor *X, const sptgbGenSpec *sp) {
 #pragma omp parallel for schedule(static)
     for (uint64_t i = 0; i < nnz; ++i)
         for (sptIndex m = 0; m < sp->nmodes; ++m)
-            X->inds[m].data[i] = (uint32_t)((keys[i] >> g.shift[m]) & ((1ULL << g.bits[m]) - 1));
+            X->inds[m].data[i] = wkeys ? (uint32_t)((wkeys[i] >> g.shift[m]) & ((1ULL << g.bits[m]) - 1))
+                                       : (uint32_t)((keys[i] >> g.shift[m]) & ((1ULL << g.bits[m]) - 1));
 
     if (sp->merge_duplicates) {
         memcpy(X->values.data, vals, nnz * sizeof(float));
@@ -341,6 +456,7 @@ int sptgbGenerate(sptSparseTensor *X, const sptgbGenSpec *sp) {
         }
     }
     free(keys);
+    free(wkeys);
     free(vals);
     return 0;
 }

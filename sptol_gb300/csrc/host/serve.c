@@ -3,19 +3,31 @@
  *
  * A server owns one device arena of the HBM budget and a table of slots.  A
  * submitted job waits in a FIFO queue until a slot and enough arena space are
- * free; admission then uploads the tensor, builds its mode-sorted 16-byte
- * records on the device (the stable radix sort of the single-tensor path),
- * uploads the initial factors and computes their FP64 Grams and ||X||^2.
- * Every step runs one ALS iteration of all admitted jobs with one launch of a
- * CUDA graph (csrc/cuda/batch.cu: the kernels read device-side work lists, so
- * the graph is captured once and only the lists change with membership) and
- * then completes jobs that reached their iteration count: GetFinalLambda on
- * the device, factors, lambda and per-iteration fits copied into the job's
- * buffers, slot and arena space returned.
+ * free.  Each step then
+ *   1. admits, as one group, the queued jobs that fit: their nonzeros are
+ *      staged back to back, bounds-checked, and sorted for every mode by one
+ *      stable radix sort of (job, row) keys over the whole group; one kernel
+ *      writes each job's 16-byte records into its slot; ||X||^2 and the Grams
+ *      of the initial factors are computed for all new jobs by work-list
+ *      kernels (csrc/cuda/batch.cu), with the same block decomposition as the
+ *      single-tensor path;
+ *   2. runs one ALS iteration of every admitted job with one launch of a CUDA
+ *      graph: the kernels read device-side work lists, so the graph is
+ *      captured once and only the lists change with membership;
+ *   3. retires jobs that reached their iteration count: GetFinalLambda for all
+ *      of them by work-list kernels, then factors, lambda and per-iteration
+ *      fits copied into each job's buffers, slot and arena space returned.
+ * Slot descriptors are written once at admission (the iteration counter lives
+ * in the slot's status words), so membership changes never touch a running
+ * job's state.
  *
  * The first capture times the MTTKRP of each rank group with unit lengths of
  * 64..512 nonzeros on the admitted jobs and keeps the fastest (the autotuner);
  * the chosen lengths are fixed in the captured graph.
+ *
+ * Staging buffers of an admission group (coordinates, values, sort keys and
+ * permutations, about 40 bytes per nonzero) are outside the budget; a group
+ * holds at most SERVE_GROUP_NNZ nonzeros unless a single job is larger.
  */
 #define _GNU_SOURCE
 #include <math.h>
@@ -26,8 +38,16 @@
 #include <cuda_runtime_api.h>
 #include "devtensor.h"
 
-enum { NL_MT = 0, NL_ZR = 16, NL_ONE = 20, NL_DN = 24, NL_FIT = 28, NL_FITONE = 29, NLISTS = 30 };
+/* step lists (fixed positions, captured in the graph) */
+enum { NL_MT = 0, NL_ZR = 16, NL_ONE = 20, NL_DN = 24, NL_FIT = 28, NL_FITONE = 29, NL_STEP = 30 };
+/* admission lists: ids are group job indices for SQ/SQONE, slot ids for the rest */
+enum { NL_SQ = NL_STEP, NL_SQONE = NL_STEP + 1, NL_GDN = NL_STEP + 2, NL_GONE = NL_STEP + 6, NL_ADM_END = NL_STEP + 10 };
+/* retirement lists (slot ids) */
+enum { NL_RDN = NL_ADM_END, NL_RONE = NL_ADM_END + 4, NLISTS = NL_ADM_END + 8 };
 enum { JOB_QUEUED = 0, JOB_ACTIVE = 1, JOB_DONE = 2, JOB_FAILED = -1 };
+
+#define SERVE_GROUP_NNZ (32ull << 20)
+#define SERVE_GROUP_JOBS 4096u
 
 typedef struct {
     uint64_t ticket;
@@ -68,6 +88,19 @@ struct sptgbServer {
     int have_graph;
     int changed;
     uint32_t nactive;
+    /* admission group */
+    uint32_t *grp;               /* job indices */
+    sptgb_adm_job *h_gjobs;
+    uint64_t *h_goffs;
+    unsigned int *h_gerr;
+    sptgb_dbuf st_ind[4], st_val, keys[2], perm[2], rtmp, d_gjobs, d_goffs, d_gerr;
+    uint32_t *ret;               /* retiring slots */
+    uint64_t *fin;               /* completion queue: tickets in completion order */
+    uint64_t nfin, fincap, finread;
+    /* SPTGB_TRACE=1: wall time per phase, printed by sptgbServerFree */
+    int trace;
+    double t_select, t_admit_host, t_admit_h2d, t_admit_dev, t_step, t_retire;
+    uint64_t n_groups, n_steps, n_retire_calls;
 };
 
 static double now_s(void) {
@@ -102,14 +135,13 @@ static void arena_free(sptgbServer *s, uint64_t off, uint64_t len) {
     uint32_t i = 0;
     while (i < s->nfree && s->freel[i].off < off) ++i;
     if (s->nfree == s->freecap) {
-        s->freecap = s->freecap ? 2 * s->freecap : 64;
+        s->freecap *= 2;
         s->freel = (span_t *)realloc(s->freel, s->freecap * sizeof(span_t));
     }
     memmove(&s->freel[i + 1], &s->freel[i], (s->nfree - i) * sizeof(span_t));
     s->freel[i].off = off;
     s->freel[i].len = len;
     ++s->nfree;
-    /* merge with the neighbours */
     if (i + 1 < s->nfree && s->freel[i].off + s->freel[i].len == s->freel[i + 1].off) {
         s->freel[i].len += s->freel[i + 1].len;
         memmove(&s->freel[i + 1], &s->freel[i + 2], (s->nfree - i - 2) * sizeof(span_t));
@@ -124,11 +156,13 @@ static void arena_free(sptgbServer *s, uint64_t off, uint64_t len) {
 
 /* ------------------------------------------------------ slot layout -- */
 typedef struct {
-    size_t rec[4], val4[4], fac[4], M, gram[4], S, lambda, ws, fits, normX2, status, total;
+    size_t rec[4], val4[4], fac[4], M, gram[4], S, lambda, ws, fits, status, normX2, total;
 } layout_t;
 
+static uint32_t stride_of(uint32_t rank) { return ((rank - 1) / 8 + 1) * 8; }
+
 static void layout(const sptSparseTensor *X, uint32_t rank, uint32_t niters, layout_t *L) {
-    const uint32_t N = X->nmodes, stride = ((rank - 1) / 8 + 1) * 8;
+    const uint32_t N = X->nmodes, stride = stride_of(rank);
     const uint64_t n = X->nnz ? X->nnz : 1;
     size_t o = 0;
     uint32_t maxd = 1;
@@ -160,9 +194,9 @@ static void layout(const sptSparseTensor *X, uint32_t rank, uint32_t niters, lay
     o += up256(sptgb_dense_ws_bytes((int)rank, 0));
     L->fits = o;
     o += up256((size_t)(niters ? niters : 1) * 8);
-    L->normX2 = o;
-    o += 256;
     L->status = o;
+    o += 256;
+    L->normX2 = o;
     o += 256;
     L->total = o;
 }
@@ -173,55 +207,31 @@ static int group_of(uint32_t stride) {
 }
 
 /* ------------------------------------------------------------ lists -- */
-static void lists_reset(sptgbServer *s) {
-    memset(s->h_counts, 0, NLISTS * sizeof(uint32_t));
-    for (int l = 0; l < NLISTS; ++l) s->h_pre[(size_t)l * (s->cap + 1)] = 0;
+static void list_clear(sptgbServer *s, int l) {
+    s->h_counts[l] = 0;
+    s->h_pre[(size_t)l * (s->cap + 1)] = 0;
 }
 
-static void lists_add(sptgbServer *s, int l, uint32_t slot, uint64_t items) {
+static void list_add(sptgbServer *s, int l, uint32_t id, uint64_t items) {
     if (items == 0) return;
     const uint32_t c = s->h_counts[l];
     uint64_t *pre = s->h_pre + (size_t)l * (s->cap + 1);
-    s->h_ids[(size_t)l * s->cap + c] = slot;
+    s->h_ids[(size_t)l * s->cap + c] = id;
     pre[c + 1] = pre[c] + items;
     s->h_counts[l] = c + 1;
 }
 
-static uint64_t dense_blocks(uint64_t rows, uint32_t per) {
-    const uint64_t nb = sptgb_batch_max_blocks();
-    uint64_t b = (rows + per - 1) / per;
-    if (b > nb) b = nb;
-    return b ? b : 1;
-}
-
-static void lists_build(sptgbServer *s) {
-    lists_reset(s);
-    const uint32_t tr = sptgb_batch_rows_per_block(), fr = sptgb_batch_fit_rows_per_block();
-    const uint32_t zr = sptgb_batch_zero_rows();
-    for (uint32_t i = 0; i < s->cap; ++i) {
-        if (s->slot_job[i] < 0) continue;
-        const sptgb_slot *d = &s->hs[i];
-        const int g = group_of(d->stride);
-        for (uint32_t m = 0; m < d->nmodes; ++m) {
-            lists_add(s, NL_MT + 4 * (int)m + g, i, (d->nnz + s->ul[g] - 1) / s->ul[g]);
-            lists_add(s, NL_ZR + (int)m, i, ((uint64_t)d->ndims[m] + zr - 1) / zr);
-            lists_add(s, NL_ONE + (int)m, i, 1);
-            lists_add(s, NL_DN + (int)m, i, dense_blocks(d->ndims[m], tr));
-        }
-        lists_add(s, NL_FIT, i, dense_blocks(d->ndims[d->nmodes - 1], fr));
-        lists_add(s, NL_FITONE, i, 1);
-    }
-}
-
-static int lists_upload(sptgbServer *s) {
-    SPTGB_CUDA(cudaMemcpyAsync(s->d_counts, s->h_counts, NLISTS * sizeof(uint32_t), cudaMemcpyHostToDevice, s->cs),
-               "GPU server lists");
-    SPTGB_CUDA(cudaMemcpyAsync(s->d_ids, s->h_ids, (size_t)NLISTS * s->cap * sizeof(uint32_t), cudaMemcpyHostToDevice,
-                               s->cs),
-               "GPU server lists");
-    SPTGB_CUDA(cudaMemcpyAsync(s->d_pre, s->h_pre, (size_t)NLISTS * (s->cap + 1) * sizeof(uint64_t),
-                               cudaMemcpyHostToDevice, s->cs),
-               "GPU server lists");
+/* Uploads lists [l0, l1). */
+static int lists_upload(sptgbServer *s, int l0, int l1) {
+    const char *module = "GPU server lists";
+    SPTGB_CUDA(cudaMemcpyAsync(s->d_counts + l0, s->h_counts + l0, (size_t)(l1 - l0) * 4, cudaMemcpyHostToDevice, s->cs),
+               module);
+    SPTGB_CUDA(cudaMemcpyAsync(s->d_ids + (size_t)l0 * s->cap, s->h_ids + (size_t)l0 * s->cap,
+                               (size_t)(l1 - l0) * s->cap * 4, cudaMemcpyHostToDevice, s->cs),
+               module);
+    SPTGB_CUDA(cudaMemcpyAsync(s->d_pre + (size_t)l0 * (s->cap + 1), s->h_pre + (size_t)l0 * (s->cap + 1),
+                               (size_t)(l1 - l0) * (s->cap + 1) * 8, cudaMemcpyHostToDevice, s->cs),
+               module);
     return 0;
 }
 
@@ -230,21 +240,52 @@ static sptgb_wlist wl(sptgbServer *s, int l) {
     return w;
 }
 
+static uint64_t clamp_blocks(uint64_t rows, uint32_t per) {
+    const uint64_t nb = sptgb_batch_max_blocks();
+    uint64_t b = (rows + per - 1) / per;
+    if (b > nb) b = nb;
+    return b ? b : 1;
+}
+
+/* Row blocks of a slot's solve for mode m: eight TR-row tiles each (enough
+ * to amortise the per-block setup, small enough to balance many slots over
+ * the persistent grid), at most the partial space NBLK.  The split depends
+ * only on the slot's own shape, so a job's arithmetic does not change with
+ * the mix it runs in. */
+static uint64_t solve_items(uint64_t rows, uint32_t tr) { return clamp_blocks(rows, 8 * tr); }
+
+static void step_lists_build(sptgbServer *s) {
+    for (int l = 0; l < NL_STEP; ++l) list_clear(s, l);
+    const uint32_t tr = sptgb_batch_rows_per_block(), fr = sptgb_batch_fit_rows_per_block();
+    const uint32_t zr = sptgb_batch_zero_rows();
+    for (uint32_t i = 0; i < s->cap; ++i) {
+        if (s->slot_job[i] < 0 || s->jobs[s->slot_job[i]].state != JOB_ACTIVE) continue;
+        const sptgb_slot *d = &s->hs[i];
+        const int g = group_of(d->stride);
+        for (uint32_t m = 0; m < d->nmodes; ++m) {
+            list_add(s, NL_MT + 4 * (int)m + g, i, (d->nnz + s->ul[g] - 1) / s->ul[g]);
+            list_add(s, NL_ZR + (int)m, i, ((uint64_t)d->ndims[m] + zr - 1) / zr);
+            list_add(s, NL_ONE + (int)m, i, 1);
+            list_add(s, NL_DN + (int)m, i, solve_items(d->ndims[m], tr));
+        }
+        list_add(s, NL_FIT, i, clamp_blocks(d->ndims[d->nmodes - 1], fr));
+        list_add(s, NL_FITONE, i, 1);
+    }
+}
+
 /* ------------------------------------------------------ admission -- */
-static int admit(sptgbServer *s, job_t *j, uint32_t slot) {
-    const char *module = "GPU server admit";
+static void fill_descriptor(sptgbServer *s, uint32_t slot, const job_t *j) {
     const sptSparseTensor *X = j->X;
-    const uint32_t N = X->nmodes, R = j->rank, stride = ((R - 1) / 8 + 1) * 8;
-    const uint64_t n = X->nnz;
+    const uint32_t N = X->nmodes;
     layout_t Lo;
-    layout(X, R, j->niters, &Lo);
+    layout(X, j->rank, j->niters, &Lo);
     char *base = s->arena + s->slot_off[slot];
     sptgb_slot *d = &s->hs[slot];
     memset(d, 0, sizeof *d);
     d->nmodes = N;
-    d->rank = R;
-    d->stride = stride;
-    d->nnz = n;
+    d->rank = j->rank;
+    d->stride = stride_of(j->rank);
+    d->nnz = X->nnz;
     for (uint32_t m = 0; m < N; ++m) {
         d->ndims[m] = X->ndims[m];
         d->rec[m] = base + Lo.rec[m];
@@ -259,64 +300,38 @@ static int admit(sptgbServer *s, job_t *j, uint32_t slot) {
     d->fits = (double *)(base + Lo.fits);
     d->normX2 = (double *)(base + Lo.normX2);
     d->status = (int *)(base + Lo.status);
-    const cudaStream_t cs = s->cs;
-    int r = 0;
-    if (n) {
-        sptgb_lock();
-        uint32_t *din[SPTGB_MAX_MODES] = {0}, *dsrt[SPTGB_MAX_MODES] = {0};
-        r = sptgb_upload_tensor(X, g_ws.inds, &g_ws.vals, NULL, cs);
-        for (uint32_t m = 0; m < N && !r; ++m) {
-            din[m] = (uint32_t *)g_ws.inds[m].ptr;
-            r = sptgb_dbuf_reserve(&g_ws.sinds[m], n * 4);
-            dsrt[m] = (uint32_t *)g_ws.sinds[m].ptr;
-        }
-        if (!r) r = sptgb_dbuf_reserve(&g_ws.svals, n * 4);
-        if (!r) r = sptgb_validate(din, X->ndims, (int)N, n, NULL, NULL, cs);
-        if (!r && sptgb_sumsq((const float *)g_ws.vals.ptr, n, d->normX2, d->ws, cs) != cudaSuccess)
-            r = sptgb_cuda_fail(cudaGetLastError(), module, __FILE__, __LINE__);
-        for (uint32_t m = 0; m < N && !r; ++m) {
-            sptIndex order[4];
-            uint32_t k = 0, o[3];
-            order[k++] = m;
-            for (uint32_t q = 0; q < N; ++q)
-                if (q != m) order[k++] = q;
-            for (uint32_t q = 0; q < N - 1; ++q) o[q] = order[q + 1];
-            sptgb_sortpass passes[SPTGB_MAX_MODES];
-            const int np = sptgb_lex_passes(X->ndims, order, (int)N, passes);
-            uint32_t *perm = NULL;
-            r = sptgb_sort_perm(din, (int)N, n, passes, np, &perm, cs);
-            if (!r) r = sptgb_gather_tensor(din, (float *)g_ws.vals.ptr, dsrt, (float *)g_ws.svals.ptr, (int)N, perm, n, cs);
-            if (r) break;
-            cudaError_t e;
-            if (N == 3) {
-                e = sptgb_pack_records(dsrt[m], dsrt[o[0]], dsrt[o[1]], (const float *)g_ws.svals.ptr,
-                                       (void *)d->rec[m], n, cs);
-            } else {
-                e = sptgb_pack_records4(dsrt[m], dsrt[o[0]], dsrt[o[1]], dsrt[o[2]], (void *)d->rec[m], n, cs);
-                if (e == cudaSuccess)
-                    e = cudaMemcpyAsync((void *)d->val4[m], g_ws.svals.ptr, n * 4, cudaMemcpyDeviceToDevice, cs);
-            }
-            if (e != cudaSuccess) r = sptgb_cuda_fail(e, module, __FILE__, __LINE__);
-        }
-        /* the workspace is reused by the next admission: finish with it first */
-        if (!r && cudaStreamSynchronize(cs) != cudaSuccess) r = sptgb_cuda_fail(cudaGetLastError(), module, __FILE__, __LINE__);
-        sptgb_unlock();
+}
+
+static int sort_group_mode(sptgbServer *s, const sptgb_adm_group *g, int mode, int jbits, int rowbits,
+                           uint32_t **perm_out) {
+    const char *module = "GPU server admit";
+    const uint64_t n = g->total;
+    uint32_t *keys[2] = {(uint32_t *)s->keys[0].ptr, (uint32_t *)s->keys[1].ptr};
+    uint32_t *perm[2] = {(uint32_t *)s->perm[0].ptr, (uint32_t *)s->perm[1].ptr};
+    int cur = 0;
+    SPTGB_CUDA(sptgb_iota_u32(perm[0], n, 0, s->cs), module);
+    /* (job, row) in one key when it fits in 32 bits, else row then job */
+    int kinds[2], bits[2], np = 0;
+    if (jbits + rowbits <= 32) {
+        kinds[np] = 0;
+        bits[np++] = jbits + rowbits;
     } else {
-        if (cudaMemsetAsync(d->normX2, 0, 8, cs) != cudaSuccess)
-            r = sptgb_cuda_fail(cudaGetLastError(), module, __FILE__, __LINE__);
+        kinds[np] = 1;
+        bits[np++] = rowbits;
+        kinds[np] = 2;
+        bits[np++] = jbits;
     }
-    for (uint32_t m = 0; m < N && !r; ++m) {
-        const size_t bytes = (size_t)X->ndims[m] * stride * 4;
-        if (bytes && cudaMemcpyAsync(d->fac[m], j->init[m]->values, bytes, cudaMemcpyHostToDevice, cs) != cudaSuccess)
-            r = sptgb_cuda_fail(cudaGetLastError(), module, __FILE__, __LINE__);
-        if (!r && sptgb_gram(d->fac[m], X->ndims[m], (int)R, (int)stride, d->gram[m], d->ws, cs) != cudaSuccess)
-            r = sptgb_cuda_fail(cudaGetLastError(), module, __FILE__, __LINE__);
+    for (int p = 0; p < np; ++p) {
+        if (bits[p] == 0) continue;
+        SPTGB_CUDA(sptgb_adm_keys(g, mode, rowbits, kinds[p], p ? perm[cur] : NULL, keys[0], s->cs), module);
+        uint32_t *kk[2] = {keys[0], keys[1]};
+        uint32_t *vv[2] = {perm[cur], perm[cur ^ 1]};
+        int which = 0;
+        SPTGB_CUDA(sptgb_radix_sort_u32(kk, vv, n, bits[p], s->rtmp.ptr, &which, s->cs), module);
+        if (which) cur ^= 1;
     }
-    if (!r && cudaMemsetAsync(d->status, 0, 16, cs) != cudaSuccess)
-        r = sptgb_cuda_fail(cudaGetLastError(), module, __FILE__, __LINE__);
-    if (!r && cudaMemcpyAsync(&s->ds[slot], d, sizeof *d, cudaMemcpyHostToDevice, cs) != cudaSuccess)
-        r = sptgb_cuda_fail(cudaGetLastError(), module, __FILE__, __LINE__);
-    return r;
+    *perm_out = perm[cur];
+    return 0;
 }
 
 static void release(sptgbServer *s, uint32_t slot) {
@@ -326,40 +341,223 @@ static void release(sptgbServer *s, uint32_t slot) {
     --s->nactive;
 }
 
-/* GetFinalLambda, results into the job's buffers (matrix.c:557-573). */
-static int retire(sptgbServer *s, uint32_t slot) {
-    const char *module = "GPU server retire";
-    job_t *j = &s->jobs[s->slot_job[slot]];
-    const sptgb_slot *d = &s->hs[slot];
-    int r = 0;
-    for (uint32_t m = 0; m < d->nmodes && !r; ++m)
-        if (sptgb_colnorm_scale(d->fac[m], d->ndims[m], (int)d->rank, (int)d->stride, d->lambda, d->ws, s->cs) !=
-            cudaSuccess)
-            r = sptgb_cuda_fail(cudaGetLastError(), module, __FILE__, __LINE__);
-    for (uint32_t m = 0; m < d->nmodes && !r; ++m) {
-        const size_t bytes = (size_t)d->ndims[m] * d->stride * 4;
-        if (bytes && cudaMemcpyAsync(j->out[m]->values, d->fac[m], bytes, cudaMemcpyDeviceToHost, s->cs) != cudaSuccess)
-            r = sptgb_cuda_fail(cudaGetLastError(), module, __FILE__, __LINE__);
+static void push_completed(sptgbServer *s, uint64_t ticket) {
+    if (s->nfin == s->fincap) {
+        s->fincap = s->fincap ? 2 * s->fincap : 256;
+        s->fin = (uint64_t *)realloc(s->fin, s->fincap * sizeof(uint64_t));
     }
-    if (!r && cudaMemcpyAsync(j->lambda, d->lambda, d->rank * 4, cudaMemcpyDeviceToHost, s->cs) != cudaSuccess)
-        r = sptgb_cuda_fail(cudaGetLastError(), module, __FILE__, __LINE__);
-    if (!r && j->niters &&
-        cudaMemcpyAsync(j->fits, d->fits, (size_t)j->niters * 8, cudaMemcpyDeviceToHost, s->cs) != cudaSuccess)
-        r = sptgb_cuda_fail(cudaGetLastError(), module, __FILE__, __LINE__);
-    if (!r && cudaStreamSynchronize(s->cs) != cudaSuccess)
-        r = sptgb_cuda_fail(cudaGetLastError(), module, __FILE__, __LINE__);
+    s->fin[s->nfin++] = ticket;
+}
+
+static void fail_job(sptgbServer *s, job_t *j) {
+    push_completed(s, j->ticket);
+    j->state = JOB_FAILED;
     j->t_done = now_s();
-    j->state = r ? JOB_FAILED : JOB_DONE;
-    release(s, slot);
-    return r;
+    if (j->slot >= 0) release(s, (uint32_t)j->slot);
+    j->slot = -1;
+}
+
+/* Admits the group s->grp[0..G) (slots and arena space already reserved). */
+static int admit_group(sptgbServer *s, uint32_t G) {
+    const char *module = "GPU server admit";
+    const cudaStream_t cs = s->cs;
+    uint64_t total = 0;
+    uint32_t lo = s->cap, hi = 0;
+    int maxN = 0, rowbits[4] = {0, 0, 0, 0};
+    for (uint32_t q = 0; q < G; ++q) {
+        job_t *j = &s->jobs[s->grp[q]];
+        const sptSparseTensor *X = j->X;
+        fill_descriptor(s, (uint32_t)j->slot, j);
+        if ((uint32_t)j->slot < lo) lo = (uint32_t)j->slot;
+        if ((uint32_t)j->slot > hi) hi = (uint32_t)j->slot;
+        sptgb_adm_job *a = &s->h_gjobs[q];
+        memset(a, 0, sizeof *a);
+        a->off = total;
+        a->n = X->nnz;
+        a->slot = (uint32_t)j->slot;
+        a->nmodes = X->nmodes;
+        for (uint32_t m = 0; m < X->nmodes; ++m) {
+            a->ndims[m] = X->ndims[m];
+            const int b = sptgb_bitwidth(X->ndims[m] ? X->ndims[m] - 1 : 0);
+            if (b > rowbits[m]) rowbits[m] = b;
+        }
+        if ((int)X->nmodes > maxN) maxN = (int)X->nmodes;
+        s->h_goffs[q] = total;
+        total += X->nnz;
+    }
+    s->h_goffs[G] = total;
+    const int jbits = sptgb_bitwidth(G - 1);
+    double t0 = s->trace ? now_s() : 0.0;
+
+    /* descriptors of the new slots (a contiguous range; other slots in it are rewritten unchanged) */
+    SPTGB_CUDA(cudaMemcpyAsync(&s->ds[lo], &s->hs[lo], (size_t)(hi - lo + 1) * sizeof(sptgb_slot),
+                               cudaMemcpyHostToDevice, cs),
+               module);
+
+    /* staging */
+    const uint64_t nn = total ? total : 1;
+    for (int m = 0; m < maxN; ++m) SPTGB_CHECK(sptgb_dbuf_reserve(&s->st_ind[m], nn * 4), module);
+    SPTGB_CHECK(sptgb_dbuf_reserve(&s->st_val, nn * 4), module);
+    for (int b = 0; b < 2; ++b) {
+        SPTGB_CHECK(sptgb_dbuf_reserve(&s->keys[b], nn * 4), module);
+        SPTGB_CHECK(sptgb_dbuf_reserve(&s->perm[b], nn * 4), module);
+    }
+    SPTGB_CHECK(sptgb_dbuf_reserve(&s->rtmp, sptgb_radix_tmp_bytes(nn)), module);
+    SPTGB_CHECK(sptgb_dbuf_reserve(&s->d_gjobs, (size_t)G * sizeof(sptgb_adm_job)), module);
+    SPTGB_CHECK(sptgb_dbuf_reserve(&s->d_goffs, (size_t)(G + 1) * 8), module);
+    SPTGB_CHECK(sptgb_dbuf_reserve(&s->d_gerr, (size_t)G * 4), module);
+    for (uint32_t q = 0; q < G; ++q) {
+        const job_t *j = &s->jobs[s->grp[q]];
+        const sptSparseTensor *X = j->X;
+        const uint64_t off = s->h_goffs[q], n = X->nnz;
+        if (!n) continue;
+        for (uint32_t m = 0; m < X->nmodes; ++m)
+            SPTGB_CUDA(cudaMemcpyAsync((uint32_t *)s->st_ind[m].ptr + off, X->inds[m].data, n * 4,
+                                       cudaMemcpyHostToDevice, cs),
+                       module);
+        SPTGB_CUDA(cudaMemcpyAsync((float *)s->st_val.ptr + off, X->values.data, n * 4, cudaMemcpyHostToDevice, cs),
+                   module);
+    }
+    if (s->trace) {
+        const double t1 = now_s();
+        s->t_admit_host += t1 - t0;
+        t0 = t1;
+    }
+    SPTGB_CUDA(cudaMemcpyAsync(s->d_gjobs.ptr, s->h_gjobs, (size_t)G * sizeof(sptgb_adm_job), cudaMemcpyHostToDevice,
+                               cs),
+               module);
+    SPTGB_CUDA(cudaMemcpyAsync(s->d_goffs.ptr, s->h_goffs, (size_t)(G + 1) * 8, cudaMemcpyHostToDevice, cs), module);
+    SPTGB_CUDA(cudaMemsetAsync(s->d_gerr.ptr, 0, (size_t)G * 4, cs), module);
+
+    sptgb_adm_group g;
+    memset(&g, 0, sizeof g);
+    for (int m = 0; m < maxN; ++m) g.ind[m] = (const uint32_t *)s->st_ind[m].ptr;
+    g.val = (const float *)s->st_val.ptr;
+    g.offs = (const uint64_t *)s->d_goffs.ptr;
+    g.jobs = (const sptgb_adm_job *)s->d_gjobs.ptr;
+    g.njobs = G;
+    g.total = total;
+    g.err = (unsigned int *)s->d_gerr.ptr;
+    SPTGB_CUDA(sptgb_adm_check(&g, cs), module);
+
+    /* ||X||^2, lambda = 1, status = 0; initial factors and their Grams */
+    for (int l = NL_STEP; l < NL_ADM_END; ++l) list_clear(s, l);
+    for (uint32_t q = 0; q < G; ++q) {
+        const sptgb_adm_job *a = &s->h_gjobs[q];
+        list_add(s, NL_SQ, q, sptgb_sumsq_blocks(a->n));
+        list_add(s, NL_SQONE, q, 1);
+        for (uint32_t m = 0; m < a->nmodes; ++m) {
+            list_add(s, NL_GDN + (int)m, a->slot, sptgb_gram_blocks(a->ndims[m]));
+            list_add(s, NL_GONE + (int)m, a->slot, 1);
+        }
+    }
+    SPTGB_CHECK(lists_upload(s, NL_STEP, NL_ADM_END), module);
+    const sptgb_wlist sq = wl(s, NL_SQ), sqone = wl(s, NL_SQONE);
+    SPTGB_CUDA(sptgb_adm_normsq(s->ds, &g, &sq, &sqone, cs), module);
+    for (uint32_t q = 0; q < G; ++q) {
+        const job_t *j = &s->jobs[s->grp[q]];
+        const sptgb_slot *d = &s->hs[j->slot];
+        for (uint32_t m = 0; m < d->nmodes; ++m) {
+            const size_t bytes = (size_t)d->ndims[m] * d->stride * 4;
+            if (bytes)
+                SPTGB_CUDA(cudaMemcpyAsync(d->fac[m], j->init[m]->values, bytes, cudaMemcpyHostToDevice, cs), module);
+        }
+    }
+    for (int m = 0; m < maxN; ++m) {
+        const sptgb_wlist dn = wl(s, NL_GDN + m), one = wl(s, NL_GONE + m);
+        SPTGB_CUDA(sptgb_batch_gram(s->ds, &dn, &one, m, cs), module);
+    }
+    if (s->trace) {
+        SPTGB_CUDA(cudaStreamSynchronize(cs), module);
+        const double t1 = now_s();
+        s->t_admit_h2d += t1 - t0;
+        t0 = t1;
+    }
+
+    /* records, one sort of the whole group per mode */
+    for (int m = 0; m < maxN && total; ++m) {
+        uint32_t *perm = NULL;
+        SPTGB_CHECK(sort_group_mode(s, &g, m, jbits, rowbits[m], &perm), module);
+        SPTGB_CUDA(sptgb_adm_pack(&g, s->ds, m, perm, cs), module);
+    }
+
+    SPTGB_CUDA(cudaMemcpyAsync(s->h_gerr, s->d_gerr.ptr, (size_t)G * 4, cudaMemcpyDeviceToHost, cs), module);
+    SPTGB_CUDA(cudaStreamSynchronize(cs), module);
+    if (s->trace) {
+        s->t_admit_dev += now_s() - t0;
+        ++s->n_groups;
+    }
+    for (uint32_t q = 0; q < G; ++q) {
+        job_t *j = &s->jobs[s->grp[q]];
+        if (s->h_gerr[q]) {
+            spt_ComplainError(module, SPTERR_VALUE_ERROR, __FILE__, __LINE__,
+                              "a coordinate is not smaller than its mode size");
+            fail_job(s, j);
+        } else {
+            j->state = JOB_ACTIVE;
+        }
+    }
+    return 0;
+}
+
+/* ----------------------------------------------------- retirement -- */
+/* GetFinalLambda (matrix.c:557-573) for every slot in s->ret[0..R), results
+ * into the jobs' buffers, slots freed. */
+static int retire(sptgbServer *s, uint32_t R) {
+    const char *module = "GPU server retire";
+    if (R == 0) return 0;
+    const double t0 = s->trace ? now_s() : 0.0;
+    for (int l = NL_RDN; l < NLISTS; ++l) list_clear(s, l);
+    int maxN = 0;
+    for (uint32_t r = 0; r < R; ++r) {
+        const sptgb_slot *d = &s->hs[s->ret[r]];
+        for (uint32_t m = 0; m < d->nmodes; ++m) {
+            list_add(s, NL_RDN + (int)m, s->ret[r], sptgb_colnorm_blocks(d->ndims[m]));
+            list_add(s, NL_RONE + (int)m, s->ret[r], 1);
+        }
+        if ((int)d->nmodes > maxN) maxN = (int)d->nmodes;
+    }
+    SPTGB_CHECK(lists_upload(s, NL_RDN, NLISTS), module);
+    for (int m = 0; m < maxN; ++m) {
+        const sptgb_wlist dn = wl(s, NL_RDN + m), one = wl(s, NL_RONE + m);
+        SPTGB_CUDA(sptgb_batch_final_lambda(s->ds, &dn, &one, m, s->cs), module);
+    }
+    for (uint32_t r = 0; r < R; ++r) {
+        const sptgb_slot *d = &s->hs[s->ret[r]];
+        job_t *j = &s->jobs[s->slot_job[s->ret[r]]];
+        for (uint32_t m = 0; m < d->nmodes; ++m) {
+            const size_t bytes = (size_t)d->ndims[m] * d->stride * 4;
+            if (bytes)
+                SPTGB_CUDA(cudaMemcpyAsync(j->out[m]->values, d->fac[m], bytes, cudaMemcpyDeviceToHost, s->cs), module);
+        }
+        SPTGB_CUDA(cudaMemcpyAsync(j->lambda, d->lambda, d->rank * 4, cudaMemcpyDeviceToHost, s->cs), module);
+        if (j->niters)
+            SPTGB_CUDA(cudaMemcpyAsync(j->fits, d->fits, (size_t)j->niters * 8, cudaMemcpyDeviceToHost, s->cs), module);
+    }
+    SPTGB_CUDA(cudaStreamSynchronize(s->cs), module);
+    const double t = now_s();
+    for (uint32_t r = 0; r < R; ++r) {
+        job_t *j = &s->jobs[s->slot_job[s->ret[r]]];
+        j->t_done = t;
+        j->state = JOB_DONE;
+        j->slot = -1;
+        push_completed(s, j->ticket);
+        release(s, s->ret[r]);
+    }
+    if (s->trace) {
+        s->t_retire += now_s() - t0;
+        ++s->n_retire_calls;
+    }
+    return 0;
 }
 
 /* ------------------------------------------------------ autotuning -- */
 static int autotune(sptgbServer *s) {
     static const uint32_t cand[4] = {64, 128, 256, 512};
+    const char *module = "GPU server tune";
     cudaEvent_t e0, e1;
-    SPTGB_CUDA(cudaEventCreate(&e0), "GPU server tune");
-    SPTGB_CUDA(cudaEventCreate(&e1), "GPU server tune");
+    SPTGB_CUDA(cudaEventCreate(&e0), module);
+    SPTGB_CUDA(cudaEventCreate(&e1), module);
     for (int g = 0; g < 4; ++g) {
         float best = 1e30f;
         uint32_t best_ul = s->ul[g];
@@ -369,16 +567,16 @@ static int autotune(sptgbServer *s) {
         if (!present) continue;
         for (int c = 0; c < 4; ++c) {
             s->ul[g] = cand[c];
-            lists_build(s);
-            SPTGB_CHECK(lists_upload(s), "GPU server tune");
+            step_lists_build(s);
+            SPTGB_CHECK(lists_upload(s, 0, NL_STEP), module);
             const sptgb_wlist w = wl(s, NL_MT + g);
             float ms = 0.f, tot = 0.f;
             for (int rep = 0; rep < 3; ++rep) {
-                cudaEventRecord(e0, s->cs);
-                SPTGB_CUDA(sptgb_batch_mttkrp(s->ds, &w, 0, g, cand[c], s->cs), "GPU server tune");
-                cudaEventRecord(e1, s->cs);
-                SPTGB_CUDA(cudaEventSynchronize(e1), "GPU server tune");
-                cudaEventElapsedTime(&ms, e0, e1);
+                SPTGB_CUDA(cudaEventRecord(e0, s->cs), module);
+                SPTGB_CUDA(sptgb_batch_mttkrp(s->ds, &w, 0, g, cand[c], s->cs), module);
+                SPTGB_CUDA(cudaEventRecord(e1, s->cs), module);
+                SPTGB_CUDA(cudaEventSynchronize(e1), module);
+                SPTGB_CUDA(cudaEventElapsedTime(&ms, e0, e1), module);
                 if (rep) tot += ms;
             }
             if (tot < best) {
@@ -395,6 +593,7 @@ static int autotune(sptgbServer *s) {
 }
 
 static int capture(sptgbServer *s) {
+    const char *module = "GPU server capture";
     if (s->have_graph) {
         cudaGraphExecDestroy(s->gexec);
         s->have_graph = 0;
@@ -409,14 +608,14 @@ static int capture(sptgbServer *s) {
     s->L.fit = wl(s, NL_FIT);
     s->L.fit_one = wl(s, NL_FITONE);
     cudaGraph_t graph;
-    SPTGB_CUDA(cudaStreamBeginCapture(s->cs, cudaStreamCaptureModeThreadLocal), "GPU server capture");
-    cudaError_t e = sptgb_batch_step(s->ds, &s->L, s->cs);
-    cudaError_t e2 = cudaStreamEndCapture(s->cs, &graph);
-    if (e != cudaSuccess) return sptgb_cuda_fail(e, "GPU server capture", __FILE__, __LINE__);
-    SPTGB_CUDA(e2, "GPU server capture");
-    e = cudaGraphInstantiate(&s->gexec, graph, 0);
+    SPTGB_CUDA(cudaStreamBeginCapture(s->cs, cudaStreamCaptureModeThreadLocal), module);
+    const cudaError_t e = sptgb_batch_step(s->ds, &s->L, s->cs);
+    const cudaError_t e2 = cudaStreamEndCapture(s->cs, &graph);
+    SPTGB_CUDA(e, module);
+    SPTGB_CUDA(e2, module);
+    const cudaError_t e3 = cudaGraphInstantiate(&s->gexec, graph, 0);
     cudaGraphDestroy(graph);
-    SPTGB_CUDA(e, "GPU server capture");
+    SPTGB_CUDA(e3, module);
     s->have_graph = 1;
     return 0;
 }
@@ -438,6 +637,7 @@ int sptgbServerCreate(sptgbServer **out, size_t hbm_budget_bytes, uint32_t max_s
     if (e == cudaSuccess) e = cudaMalloc((void **)&s->d_pre, (size_t)NLISTS * (s->cap + 1) * sizeof(uint64_t));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->cs, cudaStreamNonBlocking);
     if (e != cudaSuccess) r = sptgb_cuda_fail(e, "GPU server create", __FILE__, __LINE__);
+    const uint32_t gcap = s->cap < SERVE_GROUP_JOBS ? s->cap : SERVE_GROUP_JOBS;
     s->hs = (sptgb_slot *)calloc(s->cap, sizeof(sptgb_slot));
     s->slot_job = (int64_t *)malloc(s->cap * sizeof(int64_t));
     s->slot_off = (uint64_t *)calloc(s->cap, sizeof(uint64_t));
@@ -446,21 +646,28 @@ int sptgbServerCreate(sptgbServer **out, size_t hbm_budget_bytes, uint32_t max_s
     s->h_counts = (uint32_t *)calloc(NLISTS, sizeof(uint32_t));
     s->h_ids = (uint32_t *)calloc((size_t)NLISTS * s->cap, sizeof(uint32_t));
     s->h_pre = (uint64_t *)calloc((size_t)NLISTS * (s->cap + 1), sizeof(uint64_t));
+    s->grp = (uint32_t *)calloc(gcap, sizeof(uint32_t));
+    s->h_gjobs = (sptgb_adm_job *)calloc(gcap, sizeof(sptgb_adm_job));
+    s->h_goffs = (uint64_t *)calloc(gcap + 1, sizeof(uint64_t));
+    s->h_gerr = (unsigned int *)calloc(gcap, sizeof(unsigned int));
+    s->ret = (uint32_t *)calloc(s->cap, sizeof(uint32_t));
+    s->freecap = 64;
+    s->freel = (span_t *)malloc(s->freecap * sizeof(span_t));
     if (!r && (!s->hs || !s->slot_job || !s->slot_off || !s->slot_len || !s->slot_iters || !s->h_counts || !s->h_ids ||
-               !s->h_pre))
+               !s->h_pre || !s->grp || !s->h_gjobs || !s->h_goffs || !s->h_gerr || !s->ret || !s->freel))
         r = SPTERR_OS_ERROR;
     if (r) {
         sptgbServerFree(s);
         return r;
     }
     for (uint32_t i = 0; i < s->cap; ++i) s->slot_job[i] = -1;
-    s->freecap = 64;
-    s->freel = (span_t *)malloc(s->freecap * sizeof(span_t));
     s->freel[0].off = 0;
     s->freel[0].len = s->budget;
     s->nfree = 1;
     for (int g = 0; g < 4; ++g) s->ul[g] = 256;
     s->changed = 1;
+    const char *tr = getenv("SPTGB_TRACE");
+    s->trace = tr && tr[0] && tr[0] != '0';
     *out = s;
     return 0;
 }
@@ -472,7 +679,7 @@ int sptgbServerSubmit(sptgbServer *s, const sptSparseTensor *X, sptIndex rank, s
         spt_ComplainError(module, SPTERR_VALUE_ERROR, __FILE__, __LINE__, "order 3 or 4 and rank in [1, 64] required");
         return SPTERR_VALUE_ERROR;
     }
-    const uint32_t stride = ((rank - 1) / 8 + 1) * 8;
+    const uint32_t stride = stride_of(rank);
     for (uint32_t m = 0; m < X->nmodes; ++m)
         if (init[m]->nrows != X->ndims[m] || init[m]->stride != stride || out[m]->cap < X->ndims[m] ||
             out[m]->stride != stride) {
@@ -513,66 +720,81 @@ int sptgbServerSubmit(sptgbServer *s, const sptSparseTensor *X, sptIndex rank, s
 int sptgbServerStep(sptgbServer *s, uint32_t *active, uint32_t *queued) {
     const char *module = "GPU server step";
     SPTGB_CHECK(sptgb_ctx(), module);
-    /* admit queued jobs that fit, in submission order */
-    uint64_t keep = 0;
+    double t0 = s->trace ? now_s() : 0.0;
+    /* 1. admission group: queued jobs that fit, in submission order */
+    const uint32_t gcap = s->cap < SERVE_GROUP_JOBS ? s->cap : SERVE_GROUP_JOBS;
+    uint32_t G = 0;
+    uint64_t gnnz = 0, keep = 0;
+    uint32_t next_free = 0;
     for (uint64_t qi = 0; qi < s->nqueue; ++qi) {
         const uint64_t ji = s->queue[qi];
         job_t *j = &s->jobs[ji];
-        int slot = -1;
-        for (uint32_t i = 0; i < s->cap; ++i)
-            if (s->slot_job[i] < 0) {
-                slot = (int)i;
-                break;
-            }
-        uint64_t off = 0;
         if (j->bytes > s->budget) {
             spt_ComplainError(module, SPTERR_NO_MORE, __FILE__, __LINE__, "job larger than the HBM budget");
-            j->state = JOB_FAILED;
-            j->t_done = now_s();
+            fail_job(s, j);
             continue;
         }
-        if (slot < 0 || arena_alloc(s, j->bytes, &off) != 0) {
+        while (next_free < s->cap && s->slot_job[next_free] >= 0) ++next_free;
+        uint64_t off = 0;
+        if (G == gcap || next_free == s->cap || (G > 0 && gnnz + j->X->nnz > SERVE_GROUP_NNZ) ||
+            arena_alloc(s, j->bytes, &off) != 0) {
             s->queue[keep++] = ji;
             continue;
         }
+        const uint32_t slot = next_free;
         s->slot_off[slot] = off;
         s->slot_len[slot] = j->bytes;
         s->slot_job[slot] = (int64_t)ji;
         s->slot_iters[slot] = 0;
         ++s->nactive;
-        j->slot = slot;
-        j->state = JOB_ACTIVE;
+        j->slot = (int)slot;
+        s->grp[G++] = (uint32_t)ji;
+        gnnz += j->X->nnz;
         s->changed = 1;
-        const int r = admit(s, j, (uint32_t)slot);
-        if (r) {
-            j->state = JOB_FAILED;
-            j->t_done = now_s();
-            release(s, (uint32_t)slot);
-            continue;
-        }
-        if (j->niters == 0) SPTGB_CHECK(retire(s, (uint32_t)slot), module);
     }
     s->nqueue = keep;
+    if (s->trace) s->t_select += now_s() - t0;
+    if (G) {
+        const int r = admit_group(s, G);
+        if (r) {
+            for (uint32_t q = 0; q < G; ++q)
+                if (s->jobs[s->grp[q]].state == JOB_QUEUED) fail_job(s, &s->jobs[s->grp[q]]);
+            return r;
+        }
+        /* jobs with no iterations finish at once */
+        uint32_t R = 0;
+        for (uint32_t q = 0; q < G; ++q) {
+            const job_t *j = &s->jobs[s->grp[q]];
+            if (j->state == JOB_ACTIVE && j->niters == 0) s->ret[R++] = (uint32_t)j->slot;
+        }
+        SPTGB_CHECK(retire(s, R), module);
+    }
+    /* 2. one ALS iteration of every admitted job */
     if (s->nactive > 0) {
         if (!s->tuned) {
             SPTGB_CHECK(autotune(s), module);
             s->changed = 1;
-            if (s->have_graph) {
-                cudaGraphExecDestroy(s->gexec);
-                s->have_graph = 0;
-            }
         }
         if (s->changed) {
-            lists_build(s);
-            SPTGB_CHECK(lists_upload(s), module);
+            step_lists_build(s);
+            SPTGB_CHECK(lists_upload(s, 0, NL_STEP), module);
             s->changed = 0;
         }
         if (!s->have_graph) SPTGB_CHECK(capture(s), module);
+        if (s->trace) t0 = now_s();
         SPTGB_CUDA(cudaGraphLaunch(s->gexec, s->cs), module);
+        if (s->trace) {
+            SPTGB_CUDA(cudaStreamSynchronize(s->cs), module);
+            s->t_step += now_s() - t0;
+            ++s->n_steps;
+        }
+        /* 3. retirement */
+        uint32_t R = 0;
         for (uint32_t i = 0; i < s->cap; ++i) {
             if (s->slot_job[i] < 0) continue;
-            if (++s->slot_iters[i] >= s->jobs[s->slot_job[i]].niters) SPTGB_CHECK(retire(s, i), module);
+            if (++s->slot_iters[i] >= s->jobs[s->slot_job[i]].niters) s->ret[R++] = i;
         }
+        SPTGB_CHECK(retire(s, R), module);
     }
     if (active) *active = s->nactive;
     if (queued) *queued = (uint32_t)s->nqueue;
@@ -586,6 +808,13 @@ int sptgbServerDone(sptgbServer *s, uint64_t ticket, double *submit_s, double *d
     if (done_s) *done_s = j->t_done;
     if (j->state == JOB_FAILED) return -1;
     return j->state == JOB_DONE ? 1 : 0;
+}
+
+uint32_t sptgbServerCompleted(sptgbServer *s, uint64_t *tickets, uint32_t max) {
+    uint32_t n = 0;
+    while (n < max && s->finread < s->nfin) tickets[n++] = s->fin[s->finread++];
+    if (s->finread == s->nfin) s->finread = s->nfin = 0;
+    return n;
 }
 
 int sptgbServerDrain(sptgbServer *s) {
@@ -602,13 +831,29 @@ uint32_t sptgbServerUnitLength(const sptgbServer *s, int group) { return group >
 
 void sptgbServerFree(sptgbServer *s) {
     if (!s) return;
-    if (s->have_graph) cudaGraphExecDestroy(s->gexec);
+    if (s->trace)
+        fprintf(stderr,
+                "[sptgb server] select %.3f s | admit: host %.3f s, h2d+normsq+grams %.3f s, sort+pack %.3f s "
+                "(%llu groups) | steps %.3f s (%llu) | retire %.3f s (%llu)\n",
+                s->t_select, s->t_admit_host, s->t_admit_h2d, s->t_admit_dev, (unsigned long long)s->n_groups,
+                s->t_step, (unsigned long long)s->n_steps, s->t_retire, (unsigned long long)s->n_retire_calls);
     if (s->cs) cudaStreamSynchronize(s->cs);
+    if (s->have_graph) cudaGraphExecDestroy(s->gexec);
     if (s->arena) cudaFree(s->arena);
     if (s->ds) cudaFree(s->ds);
     if (s->d_counts) cudaFree(s->d_counts);
     if (s->d_ids) cudaFree(s->d_ids);
     if (s->d_pre) cudaFree(s->d_pre);
+    for (int m = 0; m < 4; ++m) sptgb_dbuf_release(&s->st_ind[m]);
+    sptgb_dbuf_release(&s->st_val);
+    for (int b = 0; b < 2; ++b) {
+        sptgb_dbuf_release(&s->keys[b]);
+        sptgb_dbuf_release(&s->perm[b]);
+    }
+    sptgb_dbuf_release(&s->rtmp);
+    sptgb_dbuf_release(&s->d_gjobs);
+    sptgb_dbuf_release(&s->d_goffs);
+    sptgb_dbuf_release(&s->d_gerr);
     if (s->cs) cudaStreamDestroy(s->cs);
     free(s->hs);
     free(s->slot_job);
@@ -618,8 +863,14 @@ void sptgbServerFree(sptgbServer *s) {
     free(s->h_counts);
     free(s->h_ids);
     free(s->h_pre);
+    free(s->grp);
+    free(s->h_gjobs);
+    free(s->h_goffs);
+    free(s->h_gerr);
+    free(s->ret);
     free(s->freel);
     free(s->jobs);
     free(s->queue);
+    free(s->fin);
     free(s);
 }

@@ -178,11 +178,13 @@ cudaError_t sptgb_colnorm_scale(float *A, uint32_t nrows, int rank, int stride, 
                                 double *ws, cudaStream_t s);
 
 /* ------------------------------------------------- batched CP-ALS --
- * Device descriptor of one tensor ("slot") of a batch.  Records for mode m
- * are 16-byte {row, a, b, value} (order 3) or {row, a, b, c} with the value in
- * val4[m] (order 4), a < b < c the other modes; sorted by (m, a, b, c). */
+ * Device descriptor of one tensor ("slot") of a batch, written once at
+ * admission.  Records for mode m are 16-byte {row, a, b, value} (order 3) or
+ * {row, a, b, c} with the value in val4[m] (order 4), a < b < c the other
+ * modes, grouped by row (stable in the submitted order within a row).
+ * status[0..3]: solve status per mode; status[4]: iterations completed. */
 typedef struct {
-    uint32_t nmodes, rank, stride, iter;
+    uint32_t nmodes, rank, stride, pad_;
     uint32_t ndims[4];
     uint64_t nnz;
     const void *rec[4];
@@ -209,8 +211,10 @@ typedef struct {
 /* One ALS iteration of every listed slot, as a fixed kernel sequence (graph
  * capturable: all sizes are read from device memory).  mt[m][g]: MTTKRP unit
  * lists of mode m for lane group g (W = 2, 4, 8, 16); dn[m]: slots with more
- * than m modes, items = row blocks; one[m]: the same slots, one item each;
- * zr[m]: row chunks to zero; fit: slots, items = fit blocks. */
+ * than m modes, items = solve row blocks (any count in [1, NBLK]: each block
+ * leaves one Gram partial); one[m]: the same slots in the same order, one item
+ * each; zr[m]: row chunks to zero; fit: slots, items = fit blocks; fit_one:
+ * the fit's slots in the same order, one item each. */
 typedef struct {
     sptgb_wlist mt[4][4];
     uint32_t ul[4];
@@ -225,6 +229,50 @@ uint32_t sptgb_batch_rows_per_block(void);
 uint32_t sptgb_batch_fit_rows_per_block(void);
 uint32_t sptgb_batch_zero_rows(void);
 uint32_t sptgb_batch_max_blocks(void);
+/* Admission of a group of jobs.  Their nonzeros are staged back to back
+ * (job j at [offs[j], offs[j+1])) in ind[m] / val, in the caller's order. */
+typedef struct {
+    uint64_t off, n;
+    uint32_t slot, nmodes;
+    uint32_t ndims[4];
+} sptgb_adm_job;
+typedef struct {
+    const uint32_t *ind[4];
+    const float *val;
+    const uint64_t *offs;        /* [njobs + 1] */
+    const sptgb_adm_job *jobs;   /* [njobs] */
+    uint32_t njobs;
+    uint64_t total;
+    unsigned int *err;           /* [njobs]: set to 1 when a coordinate is out of range */
+} sptgb_adm_group;
+/* err[j] for every job with a coordinate >= its mode size. */
+cudaError_t sptgb_adm_check(const sptgb_adm_group *g, cudaStream_t s);
+/* keys[p] for q = perm ? perm[p] : p, j = job of q, row = ind[mode][q]
+ * (0 for jobs of order <= mode):  kind 0: (j << rowbits) | row,
+ * kind 1: row,  kind 2: j. */
+cudaError_t sptgb_adm_keys(const sptgb_adm_group *g, int mode, int rowbits, int kind, const uint32_t *perm,
+                           uint32_t *keys, cudaStream_t s);
+/* Writes the mode-`mode` records (and order-4 values) of every job of order
+ * > mode into its slot, from the (job, row)-sorted permutation perm. */
+cudaError_t sptgb_adm_pack(const sptgb_adm_group *g, const sptgb_slot *slots, int mode, const uint32_t *perm,
+                           cudaStream_t s);
+/* ||X||^2 per job (sq: job ids, items = sum-of-squares blocks; one: same
+ * jobs, one item each), also clears status and sets lambda to 1. */
+cudaError_t sptgb_adm_normsq(const sptgb_slot *slots, const sptgb_adm_group *g, const sptgb_wlist *sq,
+                             const sptgb_wlist *one, cudaStream_t s);
+/* Gram of factor `mode` per listed slot (dn: slot ids, items = row blocks;
+ * one: same slots, one item each). */
+cudaError_t sptgb_batch_gram(const sptgb_slot *slots, const sptgb_wlist *dn, const sptgb_wlist *one, int mode,
+                             cudaStream_t s);
+/* GetFinalLambda of factor `mode` per listed slot (dn: items = column-norm
+ * blocks; one: one item each). */
+cudaError_t sptgb_batch_final_lambda(const sptgb_slot *slots, const sptgb_wlist *dn, const sptgb_wlist *one,
+                                     int mode, cudaStream_t s);
+/* Block counts the single-tensor kernels use, for identical partial sums. */
+uint32_t sptgb_sumsq_blocks(uint64_t n);
+uint32_t sptgb_colnorm_blocks(uint32_t nrows);
+uint32_t sptgb_gram_blocks(uint32_t nrows);
+
 /* Records of one mode for a batch slot: order 3 as sptgb_pack_records, order
  * 4 with idx[2] in the fourth word and the values copied to val4. */
 cudaError_t sptgb_pack_records4(const uint32_t *rows, const uint32_t *ia, const uint32_t *ib, const uint32_t *ic,

@@ -101,6 +101,33 @@ def test_generator_merge_mode_sums_duplicates():
     assert abs(v.astype(np.float64).sum() / 200_000 - 0.5) < 0.01
 
 
+def test_generator_wide_keys_beyond_64_bits():
+    """4 modes of 100,000 (68 coordinate bits): 128-bit keys, same contract."""
+    dims = [100_000, 99_000, 70_000, 65_000]
+    s = S.GenSpec()
+    s.seed = 9
+    s.nmodes = 4
+    for m, d in enumerate(dims):
+        s.ndims[m] = d
+    s.count = 20_000
+    s.merge_duplicates = 0
+    s.value_dist = S.VAL_U01
+    t = S.Tensor.generate(s)
+    i, v = t.arrays()
+    assert t.nnz == 20_000
+    assert all((i[m] < dims[m]).all() for m in range(4))
+    order = np.lexsort(i[::-1])
+    assert (order == np.arange(len(order))).all()          # lexicographically sorted
+    k = np.stack(i, 1)
+    assert (np.abs(np.diff(k, axis=0)).sum(1) > 0).all()   # no duplicates
+    assert (i[3] > 40_000).any() and (i[0] > 80_000).any()
+    t2 = S.Tensor.generate(s)
+    assert np.array_equal(t2.arrays()[0], i) and np.array_equal(t2.arrays()[1], v)
+    s.merge_duplicates = 1
+    with pytest.raises(S.SptError):
+        S.Tensor.generate(s)
+
+
 def test_generator_independent_of_thread_count():
     code = ("import sys; sys.path.insert(0, %r); sys.path.insert(0, %r); import hashlib, sptol_gb300 as S;"
             "from test_host import _spec; t = S.Tensor.generate(_spec(count=200000));"
