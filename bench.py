@@ -17,6 +17,8 @@ Workload (one "step" = MTTKRP of every mode, 0, 1, 2, on one GPU):
           launch duration from CUDA events on the launching stream.
   cpu_baseline  the oracle port of sptOmpMTTKRP_Reduce (all host threads) on
           a 10M-nonzero sample tensor of the same shape and distributions.
+  hicoo   the same tensor as HiCOO (blocks 2^7, kernels 2^17): conversion time
+          and sptMTTKRPHiCOO per mode (kernel time from CUDA events).
   serve   the batched / served CP-ALS stream: 4,096 requests of order 3 or 4
           (50/50), mode sizes log-uniform in [64, 100,000], nnz log-uniform in
           [1e3, 1e6] (at most half the index space, unique uniform
@@ -67,6 +69,7 @@ def parse():
     p.add_argument("--serve-requests", type=int, default=4096)
     p.add_argument("--plain-sample", type=int, default=256)
     p.add_argument("--skip-serve", action="store_true")
+    p.add_argument("--skip-hicoo", action="store_true")
     return p.parse_args()
 
 
@@ -227,6 +230,45 @@ def run_served(reqs, tensors, inits, outs, poisson, keep_fits):
     return {"solves_per_s": n / span, "makespan_s": span, "lat": lat, "fits": fits, "steps": steps,
             "launches": int(launches), "unit_lengths": units,
             "host_s": {"submit": round(t_sub, 3), "step": round(t_step, 3), "poll": round(t_poll, 3)}}
+
+
+def hicoo_leg(t, mats, ndims, nnz, reps):
+    """HiCOO (block 2^7, kernel 2^17) conversion and sptMTTKRPHiCOO of every
+    mode on the same tensor; kernel time from CUDA events around the HiCOO
+    kernel (output memset included), call time around the drop-in call."""
+    import sptol_gb300 as S
+    L = S.lib()
+    N = len(ndims)
+    c0 = time.time()
+    h = S.HiCOO(t, 7, 17)
+    conv_s = time.time() - c0
+    nb = int(h.s.bptr.len) - 1
+    arr = S._mat_array(mats)
+    L.sptgbHiCOOSetTiming(1)
+    kern, call = [], []
+    for m in range(N):
+        order = (ctypes.c_uint32 * N)(*([m] + [(m + i) % N for i in range(1, N)]))
+        mats[N].s.nrows = ndims[m]
+        if L.sptMTTKRPHiCOO(h.ptr(), arr, order, m):
+            raise RuntimeError("sptMTTKRPHiCOO failed")
+        ks, cs = [], []
+        for _ in range(reps):
+            a = time.perf_counter()
+            L.sptMTTKRPHiCOO(h.ptr(), arr, order, m)
+            cs.append(time.perf_counter() - a)
+            ks.append(float(L.sptgbHiCOOLastKernelMs()))
+        kern.append(float(np.median(ks)))
+        call.append(float(np.median(cs)) * 1e3)
+    L.sptgbHiCOOSetTiming(0)
+    h.free()
+    # the reference's HiCOO byte count per MTTKRP: values + 1-byte element
+    # indices per nonzero, bptr + block indices per block, factor rows
+    hb = nnz * (4 + N) + nb * (8 + 4 * N) + sum(d * RANK * 4 for d in ndims)
+    return {"sb_bits": 7, "sk_bits": 17, "blocks": nb, "convert_s": round(conv_s, 2),
+            "kernel_ms_by_mode": [round(x, 4) for x in kern], "call_ms_by_mode": [round(x, 2) for x in call],
+            "algorithmic_bytes_per_mttkrp": hb,
+            "kernel_gbs": round(N * hb / (sum(kern) / 1e3) / 1e9, 1),
+            "coo_bytes_gbs": round(N * algo_bytes(ndims, nnz, RANK) / (sum(kern) / 1e3) / 1e9, 1)}
 
 
 def serve_leg(args):
@@ -564,6 +606,11 @@ def run_ours(args, world, rank, local):
     e_s = reduce_max((time.perf_counter() - e0) / ke, world)
     e2e = world * bytes_step / e_s / 1e9
 
+    hicoo = None
+    if world == 1 and not args.skip_hicoo:
+        coo.free()
+        hicoo = hicoo_leg(t, mats, ndims, nnz, 3)
+
     serve = None
     if world == 1 and not args.skip_serve:
         coo.free()
@@ -592,6 +639,7 @@ def run_ours(args, world, rank, local):
             "nnz_per_s": round(world * K * 3 * nnz / (ms_max / 1e3), 1),
             "setup_s": {"generate": round(gen_s, 2), "upload_and_sort_3_modes": round(prep_s, 2)},
             "cpu_baseline": cpu,
+            "hicoo": hicoo,
             "serve": serve,
         }
         print(json.dumps(line), flush=True)

@@ -59,6 +59,9 @@ size_t      sptgbCooDeviceBytes(const sptgbCoo *t);
 void  sptgbCooSetTiming(sptgbCoo *t, int enable);
 float sptgbCooLastKernelMs(const sptgbCoo *t);
 void  sptgbCooFree(sptgbCoo *t);
+/* Same for the HiCOO MTTKRP kernel of sptMTTKRPHiCOO (process-wide). */
+void  sptgbHiCOOSetTiming(int enable);
+float sptgbHiCOOLastKernelMs(void);
 
 /* ----------------------------------------------------- synthetic tensors --
  * Seeded generator shared by the tests and the benchmark (SplitMix64

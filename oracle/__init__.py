@@ -63,6 +63,8 @@ def orc():
               C.c_uint32, C.c_uint32]
         L.orc_mttkrp_f32.argtypes = mt + [f32p]
         L.orc_mttkrp_f64.argtypes = mt + [f64p]
+        L.orc_omp_mttkrp_f64.argtypes = mt + [f64p, C.c_int]
+        L.orc_set_threads.argtypes = [C.c_int]
         L.orc_omp_mttkrp_reduce.argtypes = mt + [f32p, C.c_int, f32p]
         L.orc_mttkrp_hicoo_f32.argtypes = [C.c_uint32, C.c_uint64, u64p, C.POINTER(u32p), C.POINTER(u8p), f32p,
                                            C.c_int, C.POINTER(f32p), C.c_uint32, C.c_uint32, u32p, C.c_uint32,
@@ -190,7 +192,8 @@ def hicoo_build(ndims, inds_sorted, sb_bits, sk_bits):
 
 
 def mttkrp(ndims, inds, vals, mats, rank, mode, order=None, precision="f32", tk=None):
-    """Sequential FP32 (reference order), FP64, or OpenMP-reduce FP32 MTTKRP."""
+    """Sequential FP32 (reference order), FP64, FP64 over threads
+    ("f64_omp"), or OpenMP-reduce FP32 MTTKRP."""
     N, n = inds.shape
     order = _default_order(N, mode) if order is None else order
     stride = stride_of(rank)
@@ -204,6 +207,9 @@ def mttkrp(ndims, inds, vals, mats, rank, mode, order=None, precision="f32", tk=
     if precision == "f64":
         out = np.zeros((rows, stride), np.float64)
         L.orc_mttkrp_f64(*args, out.ctypes.data_as(f64p))
+    elif precision == "f64_omp":
+        out = np.zeros((rows, stride), np.float64)
+        L.orc_omp_mttkrp_f64(*args, out.ctypes.data_as(f64p), tk or os.cpu_count())
     elif precision == "omp":
         tk = tk or os.cpu_count()
         out = np.zeros((rows, stride), np.float32)
@@ -231,8 +237,10 @@ def mttkrp_hicoo(ndims, h, vals, sb_bits, mats, rank, mode, order=None):
     return out[:, :rank]
 
 
-def cpd_als(ndims, inds, vals, rank, niters, tol, init):
-    """FP64 CP-ALS restatement; init: list of [ndims[m], rank] float arrays."""
+def cpd_als(ndims, inds, vals, rank, niters, tol, init, tk=1):
+    """FP64 CP-ALS restatement; init: list of [ndims[m], rank] float arrays.
+    tk > 1 runs the MTTKRP, Gram and row solves on tk threads (per-thread
+    partial sums added in thread order)."""
     N, n = inds.shape
     stride = stride_of(rank)
     facs = []
@@ -247,8 +255,12 @@ def cpd_als(ndims, inds, vals, rank, niters, tol, init):
     lam = np.zeros(rank, np.float32)
     fits = np.full(niters, np.nan)
     done = C.c_uint32()
-    orc().orc_cpd_als_f64(N, ndp, n, ip, v.ctypes.data_as(f32p), rank, niters, tol, fp, stride,
-                          lam.ctypes.data_as(f32p), fits.ctypes.data_as(f64p), C.byref(done))
+    orc().orc_set_threads(int(tk))
+    try:
+        orc().orc_cpd_als_f64(N, ndp, n, ip, v.ctypes.data_as(f32p), rank, niters, tol, fp, stride,
+                              lam.ctypes.data_as(f32p), fits.ctypes.data_as(f64p), C.byref(done))
+    finally:
+        orc().orc_set_threads(1)
     return [f[:, :rank].copy() for f in fkeep], lam, fits, int(done.value)
 
 

@@ -284,6 +284,44 @@ void orc_mttkrp_f64(uint32_t nmodes, uint64_t nnz, const uint32_t *const *inds, 
     }
 }
 
+/* orc_mttkrp_f64 over threads: static schedule over nonzeros into
+ * per-thread FP64 outputs, added in thread order (the FP64 checker for
+ * tensors too large for one core). */
+void orc_omp_mttkrp_f64(uint32_t nmodes, uint64_t nnz, const uint32_t *const *inds, const float *vals,
+                        const float *const *mats, uint32_t stride, uint32_t R, const uint32_t *mats_order, uint32_t mode,
+                        uint32_t out_rows, double *out, int tk) {
+    const size_t csz = (size_t)out_rows * stride;
+    double *copies = (double *)calloc((size_t)tk * csz, sizeof(double));
+    if (!copies) return;
+#pragma omp parallel num_threads(tk)
+    {
+        const int t = omp_get_thread_num();
+        const uint64_t lo = nnz * (uint64_t)t / (uint64_t)tk, hi = nnz * (uint64_t)(t + 1) / (uint64_t)tk;
+        double *cp = copies + (size_t)t * csz;
+        double scratch[1024];
+        for (uint64_t x = lo; x < hi; ++x) {
+            const double entry = vals[x];
+            const uint32_t o1 = mats_order[1];
+            const float *r1 = mats[o1] + (size_t)inds[o1][x] * stride;
+            for (uint32_t r = 0; r < R; ++r) scratch[r] = entry * (double)r1[r];
+            for (uint32_t i = 2; i < nmodes; ++i) {
+                const uint32_t oi = mats_order[i];
+                const float *ri = mats[oi] + (size_t)inds[oi][x] * stride;
+                for (uint32_t r = 0; r < R; ++r) scratch[r] *= (double)ri[r];
+            }
+            double *o = cp + (size_t)inds[mode][x] * stride;
+            for (uint32_t r = 0; r < R; ++r) o[r] += scratch[r];
+        }
+    }
+#pragma omp parallel for schedule(static) num_threads(tk)
+    for (uint64_t i = 0; i < csz; ++i) {
+        double acc = 0.0;
+        for (int t = 0; t < tk; ++t) acc += copies[(size_t)t * csz + i];
+        out[i] = acc;
+    }
+    free(copies);
+}
+
 /* mttkrp_omp.c:401-476: privatised per-thread outputs, static schedule over
  * nonzeros, then a row-parallel reduction over threads. */
 void orc_omp_mttkrp_reduce(uint32_t nmodes, uint64_t nnz, const uint32_t *const *inds, const float *vals,
@@ -353,6 +391,13 @@ void orc_mttkrp_hicoo_f32(uint32_t nmodes, uint64_t nb, const uint64_t *bptr, co
  *   symmetric Grams, <X,K> from the last mode's MTTKRP (ktensor.c:173-257);
  *   GetFinalLambda (matrix.c:557-573) at the end.
  * Factors enter and leave as FP32 arrays of ndims[m] x stride. */
+/* Threads of the FP64 CP-ALS restatement (orc_set_threads); 1 keeps the
+ * sequential loops that the reference trace is pinned with.  Row solves are
+ * independent per row; with more threads the Gram and MTTKRP sums are split
+ * into per-thread partials added in thread order. */
+static int orc_threads = 1;
+void orc_set_threads(int t) { orc_threads = t < 1 ? 1 : t; }
+
 static int solve_rows_f64(double *H, int R, double *X, uint64_t nrows, int ld) {
     /* Cholesky H = L L^T in place (lower). */
     double *L = (double *)malloc((size_t)R * R * sizeof(double));
@@ -373,6 +418,7 @@ static int solve_rows_f64(double *H, int R, double *X, uint64_t nrows, int ld) {
         }
     }
     if (spd) {
+#pragma omp parallel for schedule(static) num_threads(orc_threads)
         for (uint64_t i = 0; i < nrows; ++i) {
             double *x = X + i * ld;
             for (int r = 0; r < R; ++r) {
@@ -409,6 +455,7 @@ static int solve_rows_f64(double *H, int R, double *X, uint64_t nrows, int ld) {
                 for (int j = k + 1; j < R; ++j) L[i * R + j] -= L[i * R + k] * L[k * R + j];
             }
     }
+#pragma omp parallel for schedule(static) num_threads(orc_threads)
     for (uint64_t i = 0; i < nrows; ++i) {
         double *x = X + i * ld;
         for (int k = 0; k < R; ++k) {
@@ -430,9 +477,25 @@ static int solve_rows_f64(double *H, int R, double *X, uint64_t nrows, int ld) {
 
 static void gram_f64(const double *A, uint64_t nrows, int R, int ld, double *G) {
     memset(G, 0, (size_t)R * R * sizeof(double));
-    for (uint64_t i = 0; i < nrows; ++i)
-        for (int p = 0; p < R; ++p)
-            for (int q = p; q < R; ++q) G[p * R + q] += A[i * ld + p] * A[i * ld + q];
+    if (orc_threads == 1) {
+        for (uint64_t i = 0; i < nrows; ++i)
+            for (int p = 0; p < R; ++p)
+                for (int q = p; q < R; ++q) G[p * R + q] += A[i * ld + p] * A[i * ld + q];
+    } else {
+        const int tk = orc_threads;
+        double *part = (double *)calloc((size_t)tk * R * R, sizeof(double));
+#pragma omp parallel num_threads(tk)
+        {
+            const int t = omp_get_thread_num();
+            double *g = part + (size_t)t * R * R;
+            for (uint64_t i = nrows * (uint64_t)t / tk; i < nrows * (uint64_t)(t + 1) / tk; ++i)
+                for (int p = 0; p < R; ++p)
+                    for (int q = p; q < R; ++q) g[p * R + q] += A[i * ld + p] * A[i * ld + q];
+        }
+        for (int t = 0; t < tk; ++t)
+            for (int e = 0; e < R * R; ++e) G[e] += part[(size_t)t * R * R + e];
+        free(part);
+    }
     for (int p = 0; p < R; ++p)
         for (int q = 0; q < p; ++q) G[p * R + q] = G[q * R + p];
 }
@@ -464,12 +527,38 @@ int orc_cpd_als_f64(uint32_t nmodes, const uint32_t *ndims, uint64_t nnz, const 
             order[0] = m;
             for (uint32_t i = 1; i < nmodes; ++i) order[i] = (m + i) % nmodes;
             memset(M, 0, (size_t)ndims[m] * R * sizeof(double));
-            for (uint64_t x = 0; x < nnz; ++x) {
-                for (uint32_t r = 0; r < R; ++r) sc[r] = vals[x] * A[order[1]][(size_t)inds[order[1]][x] * R + r];
-                for (uint32_t i = 2; i < nmodes; ++i)
-                    for (uint32_t r = 0; r < R; ++r) sc[r] *= A[order[i]][(size_t)inds[order[i]][x] * R + r];
-                double *o = M + (size_t)inds[m][x] * R;
-                for (uint32_t r = 0; r < R; ++r) o[r] += sc[r];
+            if (orc_threads == 1) {
+                for (uint64_t x = 0; x < nnz; ++x) {
+                    for (uint32_t r = 0; r < R; ++r) sc[r] = vals[x] * A[order[1]][(size_t)inds[order[1]][x] * R + r];
+                    for (uint32_t i = 2; i < nmodes; ++i)
+                        for (uint32_t r = 0; r < R; ++r) sc[r] *= A[order[i]][(size_t)inds[order[i]][x] * R + r];
+                    double *o = M + (size_t)inds[m][x] * R;
+                    for (uint32_t r = 0; r < R; ++r) o[r] += sc[r];
+                }
+            } else {
+                const int tk = orc_threads;
+                const size_t csz = (size_t)ndims[m] * R;
+                double *cp = (double *)calloc((size_t)tk * csz, sizeof(double));
+#pragma omp parallel num_threads(tk)
+                {
+                    const int t = omp_get_thread_num();
+                    double *o0 = cp + (size_t)t * csz, s2[1024];
+                    for (uint64_t x = nnz * (uint64_t)t / tk; x < nnz * (uint64_t)(t + 1) / tk; ++x) {
+                        for (uint32_t r = 0; r < R; ++r)
+                            s2[r] = vals[x] * A[order[1]][(size_t)inds[order[1]][x] * R + r];
+                        for (uint32_t i = 2; i < nmodes; ++i)
+                            for (uint32_t r = 0; r < R; ++r) s2[r] *= A[order[i]][(size_t)inds[order[i]][x] * R + r];
+                        double *o = o0 + (size_t)inds[m][x] * R;
+                        for (uint32_t r = 0; r < R; ++r) o[r] += s2[r];
+                    }
+                }
+#pragma omp parallel for schedule(static) num_threads(tk)
+                for (uint64_t i = 0; i < csz; ++i) {
+                    double acc = 0.0;
+                    for (int t = 0; t < tk; ++t) acc += cp[(size_t)t * csz + i];
+                    M[i] = acc;
+                }
+                free(cp);
             }
             for (uint32_t e = 0; e < R * R; ++e) {
                 double v = 1.0;

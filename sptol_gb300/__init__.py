@@ -148,6 +148,8 @@ def _declare(L):
         "sptgbCooSetTiming": (None, [C.c_void_p, C.c_int]),
         "sptgbCooLastKernelMs": (C.c_float, [C.c_void_p]),
         "sptgbCooFree": (None, [C.c_void_p]),
+        "sptgbHiCOOSetTiming": (None, [C.c_int]),
+        "sptgbHiCOOLastKernelMs": (C.c_float, []),
         "sptgbServerCreate": (C.c_int, [C.POINTER(C.c_void_p), C.c_size_t, C.c_uint32]),
         "sptgbServerSubmit": (C.c_int, [C.c_void_p, T, C.c_uint32, C.c_uint32, MM, MM, f32p,
                                         C.POINTER(C.c_double), u64p]),

@@ -1,6 +1,17 @@
 // HiCOO MTTKRP for sm_103a (sptMTTKRPHiCOO, src/sptensor/hicoo/mttkrp.c:53-144).
 //
-// A worker (W lanes, one float4 column group per lane) owns one HiCOO block
+// Window kernel (k_hicoo_win, orders 3 and 4): the blocks are visited in the
+// order of their block index in the output mode (a stable device sort of
+// binds[mode], sptgb_hicoo_schedule), so all blocks writing one output window
+// of 2^sb rows are consecutive.  The nonzeros, in that order, are split
+// evenly over persistent CTAs; a CTA accumulates the products of each window
+// it visits in a shared-memory tile (2^sb rows x stride, shared atomics) and
+// writes the tile once: plain stores when it covers the whole window, vector
+// atomics when the window continues in a neighbouring CTA.  Skewed (power-
+// law) rows thus cost shared-memory atomics, not contended global ones.
+//
+// Block kernel (k_mttkrp_hicoo, any order; used without a schedule): a
+// worker (W lanes, one float4 column group per lane) owns one HiCOO block
 // at a time.  Element coordinates are rebuilt as (binds << sb_bits) + einds
 // (hicoo/mttkrp.c:109); the product runs over mats_order[1..N-1] in order.
 // Consecutive elements of a block that hit the same output row are summed in
@@ -75,6 +86,170 @@ __global__ void __launch_bounds__(BLOCK) k_mttkrp_hicoo(sptgb_hicoo_args a) {
     }
 }
 
+// Block k (position in the schedule) holding schedule position p.
+__device__ __forceinline__ uint64_t block_at(const uint32_t *pnnz, uint64_t lo, uint64_t hi, uint32_t p) {
+    while (hi - lo > 1) {   // last k in [lo, hi) with pnnz[k] <= p
+        const uint64_t mid = (lo + hi) >> 1;
+        if (pnnz[mid] <= p) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+template <int W, int NP>
+__global__ void __launch_bounds__(BLOCK) k_hicoo_win(sptgb_hicoo_args a, uint32_t chunk, uint32_t total) {
+    extern __shared__ float tile[];   // [1 << sb][stride]
+    const int sl = (threadIdx.x & 31) % W;
+    const int wk = threadIdx.x / W;          // worker in this CTA
+    constexpr int NW = BLOCK / W;
+    const uint32_t rows_w = 1u << a.sb_bits;
+    const uint32_t st = a.stride, st4 = st / 4;
+    const bool col_ok = (uint32_t)(sl * 4) < st;
+    const int c0 = sl * 4;
+    const bool m0 = c0 + 0 < (int)a.rank, m1 = c0 + 1 < (int)a.rank;
+    const bool m2 = c0 + 2 < (int)a.rank, m3 = c0 + 3 < (int)a.rank;
+    const uint32_t mode = a.mode;
+    uint32_t pm[NP];
+#pragma unroll
+    for (int i = 0; i < NP; ++i) pm[i] = a.order[i + 1];
+
+    const uint64_t lo64 = (uint64_t)blockIdx.x * chunk;
+    if (lo64 >= total) return;
+    const uint32_t lo = (uint32_t)lo64, hi = (uint32_t)min((uint64_t)total, lo64 + chunk);
+    for (uint32_t i = threadIdx.x; i < rows_w * st; i += BLOCK) tile[i] = 0.f;
+    // first window: last w with pnnz[wst[w]] <= lo
+    uint32_t wlo = 0, whi = a.nwin;
+    while (whi - wlo > 1) {
+        const uint32_t mid = (wlo + whi) >> 1;
+        if (a.pnnz[a.wst[mid]] <= lo) wlo = mid;
+        else whi = mid;
+    }
+    uint32_t w = wlo;
+    uint32_t q = lo;
+    __syncthreads();
+    while (q < hi) {
+        const uint64_t k0 = a.wst[w], k1 = a.wst[w + 1];
+        const uint32_t wbeg = a.pnnz[k0], wend = a.pnnz[k1];
+        const uint32_t s0 = q > wbeg ? q : wbeg, s1 = hi < wend ? hi : wend;
+        const uint32_t per = (s1 - s0 + NW - 1) / NW;
+        uint32_t p = s0 + wk * per;
+        const uint32_t pend = min(p + per, s1);
+        if (p < pend) {
+            uint64_t k = block_at(a.pnnz, k0, k1, p);
+            uint32_t b = a.perm[k];
+            uint64_t e = a.bptr[b] + (p - a.pnnz[k]);
+            uint32_t kend = a.pnnz[k + 1];
+            uint32_t base_m = a.binds[mode][b] << a.sb_bits, base[NP];
+#pragma unroll
+            for (int i = 0; i < NP; ++i) base[i] = a.binds[pm[i]][b] << a.sb_bits;
+            // consecutive elements of one output row are summed in registers
+            // and added to the tile when the row changes
+            uint32_t cur = NONE;
+            float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+            auto put = [&]() {
+                if (cur == NONE || !col_ok) return;
+                float *t = tile + cur * st + c0;
+                if (m0) atomicAdd(t + 0, acc.x);
+                if (m1) atomicAdd(t + 1, acc.y);
+                if (m2) atomicAdd(t + 2, acc.z);
+                if (m3) atomicAdd(t + 3, acc.w);
+            };
+            for (; p < pend; ++p, ++e) {
+                while (p == kend) {   // next non-empty block
+                    ++k;
+                    b = a.perm[k];
+                    e = a.bptr[b];
+                    kend = a.pnnz[k + 1];
+                    base_m = a.binds[mode][b] << a.sb_bits;
+#pragma unroll
+                    for (int i = 0; i < NP; ++i) base[i] = a.binds[pm[i]][b] << a.sb_bits;
+                }
+                const uint32_t rl = a.einds[mode][e];
+                uint32_t ri[NP];
+                bool inside = base_m + rl < a.out_rows && rl < rows_w;
+#pragma unroll
+                for (int i = 0; i < NP; ++i) {
+                    ri[i] = base[i] + a.einds[pm[i]][e];
+                    inside &= ri[i] < a.ndims[pm[i]];
+                }
+                if (!inside) {
+                    if (sl == 0) atomicOr(a.err, 1u);
+                    continue;
+                }
+                if (!col_ok) continue;
+                const float v = a.vals[e];
+                float4 pr = make_float4(v, v, v, v);
+#pragma unroll
+                for (int i = 0; i < NP; ++i) {
+                    const float4 f = __ldg(reinterpret_cast<const float4 *>(a.fac[pm[i]] + (size_t)ri[i] * st) + sl);
+                    pr.x *= f.x;
+                    pr.y *= f.y;
+                    pr.z *= f.z;
+                    pr.w *= f.w;
+                }
+                if (rl != cur) {
+                    put();
+                    cur = rl;
+                    acc = make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+                acc.x += pr.x;
+                acc.y += pr.y;
+                acc.z += pr.z;
+                acc.w += pr.w;
+            }
+            put();
+        }
+        __syncthreads();
+        // one write of the window: plain when this CTA covered all of it
+        const bool owned = s0 == wbeg && s1 == wend;
+        const uint32_t row0 = a.binds[mode][a.perm[k0]] << a.sb_bits;
+        float4 *t4 = reinterpret_cast<float4 *>(tile);
+        for (uint32_t i = threadIdx.x; i < rows_w * st4; i += BLOCK) {
+            const uint32_t r = i / st4, c = i % st4;
+            const float4 v = t4[i];
+            t4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (row0 + r >= a.out_rows) continue;
+            float4 *o = reinterpret_cast<float4 *>(a.out + (size_t)(row0 + r) * st) + c;
+            if (owned) *o = v;
+            else if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f) atomicAdd(o, v);
+        }
+        __syncthreads();
+        q = s1;
+        ++w;
+    }
+}
+
+__global__ void k_block_sizes(const uint32_t *__restrict__ perm, const uint64_t *__restrict__ bptr, uint64_t nb,
+                              uint32_t *__restrict__ sizes) {
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < nb; k += (uint64_t)gridDim.x * blockDim.x)
+        sizes[k] = (uint32_t)(bptr[perm[k] + 1] - bptr[perm[k]]);
+}
+
+template <int W, int NP>
+cudaError_t launch_win(const sptgb_hicoo_args &a, cudaStream_t s) {
+    static int nsm = 0;
+    const size_t smem = ((size_t)1 << a.sb_bits) * a.stride * sizeof(float);
+    if (smem > 200 * 1024) return cudaErrorInvalidValue;
+    if (nsm == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaFuncSetAttribute(k_hicoo_win<W, NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    }
+    int per = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_hicoo_win<W, NP>, BLOCK, smem);
+    if (per < 1) per = 1;
+    if (a.nnz == 0 || a.nnz >= 0xffffffffull) return a.nnz ? cudaErrorInvalidValue : cudaSuccess;
+    const uint32_t total = (uint32_t)a.nnz;
+    // about two waves of CTAs with equal numbers of nonzeros
+    const uint64_t grid = (uint64_t)nsm * per * 2;
+    const uint32_t chunk = (uint32_t)((total + grid - 1) / grid);
+    const uint32_t ngrid = (total + chunk - 1) / chunk;
+    k_hicoo_win<W, NP><<<ngrid, BLOCK, smem, s>>>(a, chunk, total);
+    sptgb_count_launch(1);
+    return cudaGetLastError();
+}
+
 template <int W>
 cudaError_t launch(const sptgb_hicoo_args &a, cudaStream_t s) {
     static int max_blocks = 0;
@@ -102,9 +277,59 @@ extern "C" cudaError_t sptgb_mttkrp_hicoo(const sptgb_hicoo_args *a, cudaStream_
     cudaError_t e = cudaMemsetAsync(a->out, 0, (size_t)a->out_rows * a->stride * sizeof(float), s);
     if (e != cudaSuccess || a->nb == 0) return e;
     const uint32_t c4 = a->stride / 4;
+    if (a->perm && (a->nmodes == 3 || a->nmodes == 4)) {
+        if (a->nmodes == 3) {
+            if (c4 <= 2) return launch_win<2, 2>(*a, s);
+            if (c4 <= 4) return launch_win<4, 2>(*a, s);
+            if (c4 <= 8) return launch_win<8, 2>(*a, s);
+            if (c4 <= 16) return launch_win<16, 2>(*a, s);
+            return launch_win<32, 2>(*a, s);
+        }
+        if (c4 <= 2) return launch_win<2, 3>(*a, s);
+        if (c4 <= 4) return launch_win<4, 3>(*a, s);
+        if (c4 <= 8) return launch_win<8, 3>(*a, s);
+        if (c4 <= 16) return launch_win<16, 3>(*a, s);
+        return launch_win<32, 3>(*a, s);
+    }
     if (c4 <= 2) return launch<2>(*a, s);
     if (c4 <= 4) return launch<4>(*a, s);
     if (c4 <= 8) return launch<8>(*a, s);
     if (c4 <= 16) return launch<16>(*a, s);
     return launch<32>(*a, s);
+}
+
+extern "C" cudaError_t sptgb_hicoo_schedule(const uint32_t *binds_mode, const uint64_t *bptr, uint64_t nb,
+                                            int window_bits, const sptgb_hicoo_sched_scratch *w, uint32_t *perm,
+                                            uint32_t *pnnz, uint64_t *wst, uint32_t *nwin_out, cudaStream_t s) {
+    *nwin_out = 0;
+    if (nb == 0) return cudaMemsetAsync(pnnz, 0, sizeof(uint32_t), s);
+    cudaError_t e = cudaMemcpyAsync(w->keys[0], binds_mode, nb * 4, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = sptgb_iota_u32(w->vals[0], nb, 0, s);
+    uint32_t *keys[2] = {w->keys[0], w->keys[1]}, *vals[2] = {w->vals[0], w->vals[1]};
+    int which = 0;
+    if (e == cudaSuccess && window_bits > 0) e = sptgb_radix_sort_u32(keys, vals, nb, window_bits, w->rtmp, &which, s);
+    if (e != cudaSuccess) return e;
+    const uint32_t *skeys = keys[which];
+    e = cudaMemcpyAsync(perm, vals[which], nb * 4, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return e;
+    uint64_t g = (nb + 255) / 256;
+    if (g > 152 * 16) g = 152 * 16;
+    k_block_sizes<<<(unsigned)g, 256, 0, s>>>(perm, bptr, nb, w->flags);
+    sptgb_count_launch(1);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = sptgb_exclusive_scan_u32(w->flags, pnnz, nb, pnnz + nb, w->stmp, s);
+    const uint32_t *ia[1] = {skeys};
+    if (e == cudaSuccess) e = sptgb_mark_groups(ia, 1, 0, nb, w->flags, s);
+    uint32_t *dn = w->pos + nb;   // pos has nb + 1 entries
+    if (e == cudaSuccess) e = sptgb_exclusive_scan_u32(w->flags, w->pos, nb, dn, w->stmp, s);
+    if (e == cudaSuccess) e = sptgb_compact_starts(w->flags, w->pos, nb, wst, s);
+    uint32_t nwin = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&nwin, dn, sizeof nwin, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return e;
+    const uint64_t end = nb;
+    e = cudaMemcpyAsync(wst + nwin, &end, sizeof end, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    *nwin_out = nwin;
+    return e;
 }

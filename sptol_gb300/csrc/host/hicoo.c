@@ -243,6 +243,27 @@ int sptSetKernelPointers(sptNnzIndexVector *kptr, sptSparseTensor *tsr, const sp
 }
 
 /* ------------------------------------------------------- HiCOO MTTKRP -- */
+/* Kernel timing of the HiCOO MTTKRP (sptgbHiCOOSetTiming); guarded by the
+ * workspace lock like every use of the library stream. */
+static int g_hicoo_timing = 0;
+static cudaEvent_t g_hicoo_ev[2];
+static float g_hicoo_ms = 0.f;
+
+void sptgbHiCOOSetTiming(int enable) {
+    sptgb_lock();
+    if (enable && !g_hicoo_timing && sptgb_ctx() == 0) {
+        if (cudaEventCreate(&g_hicoo_ev[0]) == cudaSuccess && cudaEventCreate(&g_hicoo_ev[1]) == cudaSuccess)
+            g_hicoo_timing = 1;
+    } else if (!enable && g_hicoo_timing) {
+        cudaEventDestroy(g_hicoo_ev[0]);
+        cudaEventDestroy(g_hicoo_ev[1]);
+        g_hicoo_timing = 0;
+    }
+    sptgb_unlock();
+}
+
+float sptgbHiCOOLastKernelMs(void) { return g_hicoo_ms; }
+
 static int hicoo_mttkrp(sptSparseTensorHiCOO const *h, sptMatrix *mats[], sptIndex const *mats_order, sptIndex mode,
                         const char *module) {
     const sptIndex N = h->nmodes;
@@ -325,12 +346,44 @@ static int hicoo_mttkrp(sptSparseTensorHiCOO const *h, sptMatrix *mats[], sptInd
     for (sptIndex m = 0; m < N; ++m) a.ndims[m] = h->ndims[m];
     H(sptgb_dbuf_reserve(&g_ws.flag, 2 * sizeof(unsigned int)));
     a.err = (unsigned int *)g_ws.flag.ptr;
+    a.nnz = n;
+    /* orders 3 and 4: output-window schedule of this mode, then the window kernel */
+    if ((N == 3 || N == 4) && nb && n < 0xffffffffull && ((size_t)1 << h->sb_bits) * stride * 4 <= 200 * 1024) {
+        sptgb_hicoo_sched_scratch w;
+        for (int i = 0; i < 2; ++i) {
+            H(sptgb_dbuf_reserve(&g_ws.keys[i], nb * 4));
+            H(sptgb_dbuf_reserve(&g_ws.perm[i], nb * 4));
+            w.keys[i] = (uint32_t *)g_ws.keys[i].ptr;
+            w.vals[i] = (uint32_t *)g_ws.perm[i].ptr;
+        }
+        H(sptgb_dbuf_reserve(&g_ws.rtmp, sptgb_radix_tmp_bytes(nb)));
+        H(sptgb_dbuf_reserve(&g_ws.misc[2], (2 * nb + 1) * 4));
+        H(sptgb_dbuf_reserve(&g_ws.misc[3], (2 * nb + 1) * 4));
+        H(sptgb_dbuf_reserve(&g_ws.misc[4], (nb + 1) * 8));
+        H(sptgb_dbuf_reserve(&g_ws.misc[5], sptgb_scan_tmp_bytes(nb)));
+        w.rtmp = g_ws.rtmp.ptr;
+        w.stmp = g_ws.misc[5].ptr;
+        w.flags = (uint32_t *)g_ws.misc[2].ptr;
+        w.pos = w.flags + nb;
+        uint32_t *perm = (uint32_t *)g_ws.misc[3].ptr, *pnnz = perm + nb;
+        const uint32_t maxb = h->ndims[mode] ? (h->ndims[mode] - 1) >> h->sb_bits : 0;
+        uint32_t nwin = 0;
+        C(sptgb_hicoo_schedule(a.binds[mode], a.bptr, nb, sptgb_bitwidth(maxb), &w, perm, pnnz,
+                               (uint64_t *)g_ws.misc[4].ptr, &nwin, s));
+        a.perm = perm;
+        a.pnnz = pnnz;
+        a.wst = (const uint64_t *)g_ws.misc[4].ptr;
+        a.nwin = nwin;
+    }
     C(cudaMemsetAsync(a.err, 0, sizeof(unsigned int), s));
+    if (g_hicoo_timing) C(cudaEventRecord(g_hicoo_ev[0], s));
     C(sptgb_mttkrp_hicoo(&a, s));
+    if (g_hicoo_timing) C(cudaEventRecord(g_hicoo_ev[1], s));
     unsigned int herr = 0;
     C(cudaMemcpyAsync(&herr, a.err, sizeof herr, cudaMemcpyDeviceToHost, s));
     if (tmpI) C(cudaMemcpyAsync(mats[N]->values, g_ws.out.ptr, (size_t)tmpI * stride * 4, cudaMemcpyDeviceToHost, s));
     C(cudaStreamSynchronize(s));
+    if (g_hicoo_timing) C(cudaEventElapsedTime(&g_hicoo_ms, g_hicoo_ev[0], g_hicoo_ev[1]));
     if (herr) {
         spt_ComplainError(module, SPTERR_VALUE_ERROR, __FILE__, __LINE__,
                           "a coordinate is not smaller than its mode size");

@@ -134,8 +134,27 @@ typedef struct {
     uint32_t        sb_bits;
     uint32_t        ndims[SPTGB_MAX_MODES];    /* elements outside are skipped and flagged */
     unsigned int   *err;                       /* device flag, set to 1 on an out-of-range element */
+    /* output-window schedule of `mode` (sptgb_hicoo_schedule); perm == NULL
+     * runs the block-parallel kernel with per-row atomics instead */
+    const uint32_t *perm;                      /* [nb] blocks ordered by binds[mode] (stable) */
+    const uint32_t *pnnz;                      /* [nb+1] exclusive prefix of block sizes in that order */
+    const uint64_t *wst;                       /* [nwin+1] first position of each output window; wst[nwin] = nb */
+    uint32_t        nwin;
+    uint64_t        nnz;                       /* = bptr[nb]; below 2^32 for the window kernel */
 } sptgb_hicoo_args;
 cudaError_t sptgb_mttkrp_hicoo(const sptgb_hicoo_args *a, cudaStream_t s);
+/* Output-window schedule of one mode: blocks stably sorted by their block
+ * index in `mode` (keys = binds_mode, window_bits significant bits), the
+ * prefix of their sizes and the start of each run of equal keys.  Scratch:
+ * keys/vals double buffers [nb] each, radix tmp, flags/pos [nb], scan tmp.
+ * *nwin_out is read back (the stream is synchronised).  nnz < 2^32. */
+typedef struct {
+    uint32_t *keys[2], *vals[2], *flags, *pos;
+    void *rtmp, *stmp;
+} sptgb_hicoo_sched_scratch;
+cudaError_t sptgb_hicoo_schedule(const uint32_t *binds_mode, const uint64_t *bptr, uint64_t nb, int window_bits,
+                                 const sptgb_hicoo_sched_scratch *w, uint32_t *perm, uint32_t *pnnz, uint64_t *wst,
+                                 uint32_t *nwin_out, cudaStream_t s);
 
 /* ---------------------------------------------------- dense CP-ALS --
  * FP64 pieces; matrices are row-major with `stride` floats per row. */

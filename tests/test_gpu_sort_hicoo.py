@@ -114,6 +114,31 @@ def test_hicoo_skewed_against_oracle():
         assert rel_fro(out, ref) <= 1e-5
 
 
+@pytest.mark.parametrize("rank,sb", [(64, 8), (5, 4)])
+def test_hicoo_window_kernel_4d_skewed_against_oracle(rank, sb):
+    """Order 4, power-law modes (hot output windows split over many CTAs),
+    the widest tile (2^8 rows x 64) and an odd rank with small blocks."""
+    spec = S.GenSpec()
+    spec.seed = 8
+    spec.nmodes = 4
+    for m, d in enumerate([300_000, 5_000, 40_000, 300]):
+        spec.ndims[m] = d
+    spec.coord_dist[0] = spec.coord_dist[2] = S.DIST_ZIPF
+    spec.zipf_s[0] = spec.zipf_s[2] = 1.3
+    spec.count = 400_000
+    spec.value_dist = S.VAL_UPM1
+    t = S.Tensor.generate(spec)
+    ndims = t.ndims
+    h = S.HiCOO(t, sb, sb + 6)
+    i2, v2 = t.arrays()
+    mats = S.new_factors(ndims, rank, seed=6)
+    facs = [m.array()[: ndims[k]].copy() for k, m in enumerate(mats[:4])]
+    for mode in range(4):
+        out = S.mttkrp_hicoo(h, mats, mode)
+        ref = O.mttkrp(ndims, i2, v2, facs, rank, mode, precision="f64")
+        assert rel_fro(out, ref) <= 1e-5, (mode, rel_fro(out, ref))
+
+
 def test_morton_sort_matches_oracle_within_kernels():
     rng = np.random.default_rng(2)
     ndims = [5000, 3000, 700]

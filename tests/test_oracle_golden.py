@@ -106,3 +106,16 @@ def test_reference_library_agrees_with_oracle_on_fresh_inputs():
     for mode in range(3):
         r, _ = O.ref_mttkrp(ndims, inds, vals, mats, 8, mode)
         assert np.array_equal(r, O.mttkrp(ndims, inds, vals, mats, 8, mode))
+
+
+def test_threaded_fp64_oracle_equals_sequential():
+    rng = np.random.default_rng(0)
+    nd = [50, 40, 30, 20]
+    n = 20000
+    inds = np.stack([rng.integers(0, d, n) for d in nd]).astype(np.uint32)
+    vals = rng.random(n, dtype=np.float32)
+    mats = [rng.random((d, 16), dtype=np.float32) for d in nd]
+    for m in range(4):
+        a = O.mttkrp(nd, inds, vals, mats, 16, m, precision="f64")
+        b = O.mttkrp(nd, inds, vals, mats, 16, m, precision="f64_omp", tk=4)
+        assert np.abs(a - b).max() <= 1e-13 * np.abs(a).max()
