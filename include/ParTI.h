@@ -279,6 +279,23 @@ int sptOmpCpdAls(sptSparseTensor const *const spten, sptIndex const rank, sptInd
 int sptCudaCpdAls(sptSparseTensor const *const spten, sptIndex const rank, sptIndex const niters,
                   double const tol, sptKruskalTensor *ktensor);
 
+/* Rank matrices and rank Kruskal tensors (matrices.h:69-74, ktensors.h:43-45). */
+int  sptNewRankMatrix(sptRankMatrix *mtx, sptIndex const nrows, sptElementIndex const ncols);
+int  sptRandomizeRankMatrix(sptRankMatrix *mtx, sptIndex const nrows, sptElementIndex const ncols);
+int  sptConstantRankMatrix(sptRankMatrix *mtx, sptValue const val);
+void sptFreeRankMatrix(sptRankMatrix *mtx);
+int  sptNewRankKruskalTensor(sptRankKruskalTensor *ktsr, sptIndex nmodes, const sptIndex ndims[],
+                             sptElementIndex rank);
+void sptFreeRankKruskalTensor(sptRankKruskalTensor *ktsr);
+
+/* CP-ALS over a HiCOO tensor (cpds.h:46-59, src/sptensor/hicoo/cpd.c:149-195):
+ * the same loop with the HiCOO MTTKRP; factors are rank matrices.  The
+ * OpenMP variant's tk and balanced arguments are accepted and ignored. */
+int sptCpdAlsHiCOO(sptSparseTensorHiCOO const *const hitsr, sptIndex const rank, sptIndex const niters,
+                   double const tol, sptRankKruskalTensor *ktensor);
+int sptOmpCpdAlsHiCOO(sptSparseTensorHiCOO const *const hitsr, sptIndex const rank, sptIndex const niters,
+                      double const tol, const int tk, int balanced, sptRankKruskalTensor *ktensor);
+
 #ifdef __cplusplus
 }
 #endif

@@ -59,6 +59,22 @@ size_t      sptgbCooDeviceBytes(const sptgbCoo *t);
 void  sptgbCooSetTiming(sptgbCoo *t, int enable);
 float sptgbCooLastKernelMs(const sptgbCoo *t);
 void  sptgbCooFree(sptgbCoo *t);
+/* ------------------------------------------------ resident HiCOO tensor --
+ * The HiCOO arrays uploaded once; per output mode, the output-window
+ * schedule (blocks ordered by their block index in that mode) is built on
+ * the device on first use.  Orders 3 and 4 run the window kernel, others
+ * the block kernel.  Same argument meaning as sptgbCooMTTKRP. */
+typedef struct sptgbHicoo sptgbHicoo;
+int  sptgbHicooCreate(sptgbHicoo **out, const sptSparseTensorHiCOO *h, void *stream);
+int  sptgbHicooPrepareMode(sptgbHicoo *t, sptIndex mode, void *stream);
+int  sptgbHicooMTTKRP(sptgbHicoo *t, sptIndex mode, const sptIndex *mats_order, const float *const *d_mats,
+                      sptIndex rank, sptIndex stride, float *d_out, void *stream);
+size_t sptgbHicooDeviceBytes(const sptgbHicoo *t);
+void sptgbHicooFree(sptgbHicoo *t);
+/* CP-ALS over a HiCOO tensor from caller factors (rank matrices); results
+ * as sptgbCpdAls. */
+int sptgbCpdAlsHiCOO(sptSparseTensorHiCOO const *h, sptIndex rank, sptIndex niters, double tol,
+                     sptRankMatrix **mats, sptValue *lambda, double *fits, sptIndex *iters_done);
 /* Same for the HiCOO MTTKRP kernel of sptMTTKRPHiCOO (process-wide). */
 void  sptgbHiCOOSetTiming(int enable);
 float sptgbHiCOOLastKernelMs(void);

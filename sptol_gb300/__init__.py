@@ -16,7 +16,7 @@ import numpy as np
 __all__ = [
     "lib", "Tensor", "Matrix", "HiCOO", "GenSpec", "mttkrp", "mttkrp_hicoo", "cpd_als",
     "new_factors", "SptError", "DIST_UNIFORM", "DIST_ZIPF", "VAL_U01", "VAL_UPM1", "VAL_LOGNORMAL",
-    "VAL_PLANTED", "DeviceCoo", "Server",
+    "VAL_PLANTED", "DeviceCoo", "DeviceHicoo", "Server", "RankMatrix", "cpd_als_hicoo",
 ]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -66,6 +66,16 @@ class SparseTensorS(C.Structure):
 class MatrixS(C.Structure):
     _fields_ = [("nrows", C.c_uint32), ("ncols", C.c_uint32), ("cap", C.c_uint32), ("stride", C.c_uint32),
                 ("values", f32p)]
+
+
+class RankMatrixS(C.Structure):
+    _fields_ = [("nrows", C.c_uint32), ("ncols", C.c_uint8), ("cap", C.c_uint32), ("stride", C.c_uint8),
+                ("values", f32p)]
+
+
+class RankKruskalS(C.Structure):
+    _fields_ = [("nmodes", C.c_uint32), ("rank", C.c_uint8), ("ndims", u32p), ("lambda_", f32p),
+                ("fit", C.c_double), ("factors", C.POINTER(C.POINTER(RankMatrixS)))]
 
 
 class HiCOOS(C.Structure):
@@ -149,6 +159,19 @@ def _declare(L):
         "sptgbCooLastKernelMs": (C.c_float, [C.c_void_p]),
         "sptgbCooFree": (None, [C.c_void_p]),
         "sptgbHiCOOSetTiming": (None, [C.c_int]),
+        "sptNewRankMatrix": (C.c_int, [C.POINTER(RankMatrixS), C.c_uint32, C.c_uint8]),
+        "sptFreeRankMatrix": (None, [C.POINTER(RankMatrixS)]),
+        "sptNewRankKruskalTensor": (C.c_int, [C.POINTER(RankKruskalS), C.c_uint32, u32p, C.c_uint8]),
+        "sptFreeRankKruskalTensor": (None, [C.POINTER(RankKruskalS)]),
+        "sptCpdAlsHiCOO": (C.c_int, [H, C.c_uint32, C.c_uint32, C.c_double, C.POINTER(RankKruskalS)]),
+        "sptgbCpdAlsHiCOO": (C.c_int, [H, C.c_uint32, C.c_uint32, C.c_double, C.POINTER(C.POINTER(RankMatrixS)),
+                                       f32p, C.POINTER(C.c_double), u32p]),
+        "sptgbHicooCreate": (C.c_int, [C.POINTER(C.c_void_p), H, C.c_void_p]),
+        "sptgbHicooPrepareMode": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p]),
+        "sptgbHicooMTTKRP": (C.c_int, [C.c_void_p, C.c_uint32, u32p, C.POINTER(C.c_void_p), C.c_uint32,
+                                       C.c_uint32, C.c_void_p, C.c_void_p]),
+        "sptgbHicooDeviceBytes": (C.c_size_t, [C.c_void_p]),
+        "sptgbHicooFree": (None, [C.c_void_p]),
         "sptgbHiCOOLastKernelMs": (C.c_float, []),
         "sptgbServerCreate": (C.c_int, [C.POINTER(C.c_void_p), C.c_size_t, C.c_uint32]),
         "sptgbServerSubmit": (C.c_int, [C.c_void_p, T, C.c_uint32, C.c_uint32, MM, MM, f32p,
@@ -555,6 +578,87 @@ class Server:
     def free(self):
         if self.h:
             lib().sptgbServerFree(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class RankMatrix:
+    """An sptRankMatrix allocated by sptNewRankMatrix (8-bit column count)."""
+
+    def __init__(self, nrows, ncols):
+        self.s = RankMatrixS()
+        _check(lib().sptNewRankMatrix(C.byref(self.s), nrows, ncols), "sptNewRankMatrix")
+        self._owned = True
+
+    @classmethod
+    def from_array(cls, a):
+        a = np.asarray(a, dtype=np.float32)
+        m = cls(a.shape[0], a.shape[1])
+        m.array()[:, : a.shape[1]] = a
+        return m
+
+    def array(self):
+        s = self.s
+        return np.ctypeslib.as_array(s.values, shape=(int(s.cap), int(s.stride)))
+
+    def view(self):
+        return self.array()[: int(self.s.nrows), : int(self.s.ncols)]
+
+    def free(self):
+        if self._owned:
+            lib().sptFreeRankMatrix(C.byref(self.s))
+            self._owned = False
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def cpd_als_hicoo(h, rank, niters, tol, init):
+    """sptgbCpdAlsHiCOO from caller factors `init` (N arrays ndims[m] x rank).
+    Returns (factors, lambda, fits, iterations run)."""
+    L = lib()
+    N = int(h.s.nmodes)
+    mats = [RankMatrix.from_array(a) for a in init]
+    arr = (C.POINTER(RankMatrixS) * N)(*[C.pointer(m.s) for m in mats])
+    lam = np.zeros(rank, np.float32)
+    fits = np.zeros(niters, np.float64)
+    done = C.c_uint32()
+    _check(L.sptgbCpdAlsHiCOO(h.ptr(), rank, niters, tol, arr, lam.ctypes.data_as(f32p),
+                              fits.ctypes.data_as(C.POINTER(C.c_double)), C.byref(done)), "sptgbCpdAlsHiCOO")
+    return [m.view().copy() for m in mats], lam, fits, int(done.value)
+
+
+class DeviceHicoo:
+    """sptgbHicoo handle: HiCOO arrays resident on the device, per-mode
+    output-window schedules."""
+
+    def __init__(self, h, stream=None):
+        self.h = C.c_void_p()
+        _check(lib().sptgbHicooCreate(C.byref(self.h), h.ptr(), stream), "sptgbHicooCreate")
+        self.nmodes = int(h.s.nmodes)
+
+    def prepare(self, mode, stream=None):
+        _check(lib().sptgbHicooPrepareMode(self.h, mode, stream), "sptgbHicooPrepareMode")
+
+    def mttkrp(self, mode, mats_order, dev_ptrs, rank, stride, out_ptr, stream=None):
+        order, op = _u32(mats_order)
+        arr = (C.c_void_p * len(dev_ptrs))(*dev_ptrs)
+        _check(lib().sptgbHicooMTTKRP(self.h, mode, op, arr, rank, stride, out_ptr, stream), "sptgbHicooMTTKRP")
+
+    def nbytes(self):
+        return int(lib().sptgbHicooDeviceBytes(self.h))
+
+    def free(self):
+        if self.h:
+            lib().sptgbHicooFree(self.h)
             self.h = C.c_void_p()
 
     def __del__(self):

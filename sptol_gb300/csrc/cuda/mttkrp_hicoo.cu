@@ -250,6 +250,20 @@ cudaError_t launch_win(const sptgb_hicoo_args &a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+// *err = 1 when an element's coordinate is outside its mode or its element
+// offset is not below 2^sb (one thread per block).
+__global__ void k_hicoo_check(const uint64_t *__restrict__ bptr, sptgb_hicoo_args a, uint64_t nb) {
+    for (uint64_t b = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; b < nb; b += (uint64_t)gridDim.x * blockDim.x) {
+        bool bad = false;
+        for (uint64_t e = bptr[b]; e < bptr[b + 1] && !bad; ++e)
+            for (uint32_t m = 0; m < a.nmodes; ++m) {
+                const uint32_t el = a.einds[m][e];
+                bad |= (el >> a.sb_bits) != 0 || (a.binds[m][b] << a.sb_bits) + el >= a.ndims[m];
+            }
+        if (bad) *a.err = 1u;
+    }
+}
+
 template <int W>
 cudaError_t launch(const sptgb_hicoo_args &a, cudaStream_t s) {
     static int max_blocks = 0;
@@ -332,4 +346,13 @@ extern "C" cudaError_t sptgb_hicoo_schedule(const uint32_t *binds_mode, const ui
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     *nwin_out = nwin;
     return e;
+}
+
+extern "C" cudaError_t sptgb_hicoo_check(const sptgb_hicoo_args *a, cudaStream_t s) {
+    if (a->nb == 0) return cudaSuccess;
+    uint64_t g = (a->nb + 255) / 256;
+    if (g > 152 * 16) g = 152 * 16;
+    k_hicoo_check<<<(unsigned)g, 256, 0, s>>>(a->bptr, *a, a->nb);
+    sptgb_count_launch(1);
+    return cudaGetLastError();
 }

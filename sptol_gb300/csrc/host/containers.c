@@ -387,6 +387,84 @@ void sptFreeMatrix(sptMatrix *mtx) {
     mtx->ncols = 0;
 }
 
+/* ------------------------------------------------ rank matrix (u8 cols) --
+ * rankmatrix.c:38-133: the same row-major layout with 8-bit column count and
+ * stride; padding columns are zeroed here (the reference leaves them
+ * uninitialised). */
+int sptNewRankMatrix(sptRankMatrix *mtx, sptIndex const nrows, sptElementIndex const ncols) {
+    mtx->nrows = nrows;
+    mtx->ncols = ncols;
+    mtx->cap = nrows != 0 ? nrows : 1;
+    mtx->stride = (sptElementIndex)(((ncols - 1) / 8 + 1) * 8);
+    mtx->values = NULL;
+    int r = posix_memalign((void **)&mtx->values, 8 * sizeof(sptValue),
+                           (size_t)mtx->cap * mtx->stride * sizeof(sptValue));
+    if (r != 0 || !mtx->values) {
+        errno = r ? r : ENOMEM;
+        CHECK_OS(1, "RankMtx New");
+    }
+    memset(mtx->values, 0, (size_t)mtx->cap * mtx->stride * sizeof(sptValue));
+    return 0;
+}
+
+int sptRandomizeRankMatrix(sptRankMatrix *mtx, sptIndex const nrows, sptElementIndex const ncols) {
+    const uint64_t base = sptgb_seed_next();
+    for (sptIndex i = 0; i < nrows; ++i)
+        for (sptElementIndex j = 0; j < ncols; ++j) {
+            const uint64_t z = mix64(base + 0x9E3779B97F4A7C15ULL * ((uint64_t)i * ncols + j + 1));
+            float v = 3.0f * (float)((z >> 40) * (1.0 / 16777216.0));
+            if (z & 1) v = -v;
+            mtx->values[(size_t)i * mtx->stride + j] = v;
+        }
+    return 0;
+}
+
+int sptConstantRankMatrix(sptRankMatrix *mtx, sptValue const val) {
+    for (sptIndex i = 0; i < mtx->nrows; ++i)
+        for (sptElementIndex j = 0; j < mtx->ncols; ++j) mtx->values[(size_t)i * mtx->stride + j] = val;
+    return 0;
+}
+
+void sptFreeRankMatrix(sptRankMatrix *mtx) {
+    free(mtx->values);
+    mtx->values = NULL;
+    mtx->nrows = 0;
+    mtx->ncols = 0;
+    mtx->cap = 0;
+    mtx->stride = 0;
+}
+
+/* rankktensor.c:33-88 */
+int sptNewRankKruskalTensor(sptRankKruskalTensor *k, sptIndex nmodes, const sptIndex ndims[], sptElementIndex rank) {
+    k->nmodes = nmodes;
+    k->rank = rank;
+    k->ndims = malloc(nmodes * sizeof(sptIndex));
+    CHECK_OS(!k->ndims, "RankKruskal New");
+    for (sptIndex i = 0; i < nmodes; ++i) k->ndims[i] = ndims[i];
+    k->lambda = malloc((rank ? rank : 1) * sizeof(sptValue));
+    CHECK_OS(!k->lambda, "RankKruskal New");
+    k->fit = 0.0;
+    k->factors = NULL;
+    return 0;
+}
+
+void sptFreeRankKruskalTensor(sptRankKruskalTensor *k) {
+    k->rank = 0;
+    k->fit = 0.0;
+    free(k->ndims);
+    free(k->lambda);
+    if (k->factors) {
+        for (sptIndex i = 0; i < k->nmodes; ++i)
+            if (k->factors[i]) {
+                sptFreeRankMatrix(k->factors[i]);
+                free(k->factors[i]);
+            }
+        free(k->factors);
+    }
+    k->factors = NULL;
+    k->nmodes = 0;
+}
+
 /* ---------------------------------------------------- Kruskal tensor -- */
 int sptNewKruskalTensor(sptKruskalTensor *k, sptIndex nmodes, const sptIndex ndims[], sptIndex rank) {
     k->nmodes = nmodes;

@@ -57,4 +57,22 @@ struct sptgbCoo {
     float last_ms;
 };
 
+struct sptgbHicoo {
+    sptIndex nmodes;
+    sptIndex ndims[SPTGB_MAX_MODES];
+    uint64_t nnz, nb;
+    int sb_bits;
+    uint64_t *bptr;
+    uint32_t *binds[SPTGB_MAX_MODES];
+    uint8_t *einds[SPTGB_MAX_MODES];
+    float *vals;
+    /* output-window schedule per mode (orders 3 and 4) */
+    uint32_t *perm[SPTGB_MAX_MODES], *pnnz[SPTGB_MAX_MODES];
+    uint64_t *wst[SPTGB_MAX_MODES];
+    uint32_t nwin[SPTGB_MAX_MODES];
+    int ready[SPTGB_MAX_MODES];
+    unsigned int *err;
+    size_t bytes;
+};
+
 #endif

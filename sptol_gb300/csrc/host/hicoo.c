@@ -404,3 +404,176 @@ int sptOmpMTTKRPHiCOO(sptSparseTensorHiCOO const *const hitsr, sptMatrix *mats[]
     (void)nt;
     return hicoo_mttkrp(hitsr, mats, mats_order, mode, "GPU HiCOO SpTns MTTKRP");
 }
+
+/* ------------------------------------------------ resident HiCOO tensor -- */
+static int hicoo_window_ok(const sptgbHicoo *t, sptIndex stride) {
+    return (t->nmodes == 3 || t->nmodes == 4) && t->nb && t->nnz < 0xffffffffull &&
+           ((size_t)1 << t->sb_bits) * stride * 4 <= 200 * 1024;
+}
+
+void sptgbHicooFree(sptgbHicoo *t) {
+    if (!t) return;
+    if (t->bptr) cudaFree(t->bptr);
+    for (int m = 0; m < SPTGB_MAX_MODES; ++m) {
+        if (t->binds[m]) cudaFree(t->binds[m]);
+        if (t->einds[m]) cudaFree(t->einds[m]);
+        if (t->perm[m]) cudaFree(t->perm[m]);
+        if (t->wst[m]) cudaFree(t->wst[m]);
+    }
+    if (t->vals) cudaFree(t->vals);
+    if (t->err) cudaFree(t->err);
+    free(t);
+}
+
+size_t sptgbHicooDeviceBytes(const sptgbHicoo *t) { return t ? t->bytes : 0; }
+
+int sptgbHicooCreate(sptgbHicoo **out, const sptSparseTensorHiCOO *h, void *stream) {
+    const char *module = "GPU HiCOO create";
+    *out = NULL;
+    const sptIndex N = h->nmodes;
+    if (N < 2 || N > SPTGB_MAX_MODES || h->sb_bits > 8) {
+        spt_ComplainError(module, SPTERR_VALUE_ERROR, __FILE__, __LINE__, "unsupported order or block size");
+        return SPTERR_VALUE_ERROR;
+    }
+    const uint64_t nb = h->bptr.len ? h->bptr.len - 1 : 0, n = h->nnz;
+    int bad = h->values.len < n || (nb && (h->bptr.data[0] != 0 || h->bptr.data[nb] != n));
+    for (uint64_t b = 0; b < nb && !bad; ++b) bad = h->bptr.data[b + 1] < h->bptr.data[b];
+    for (sptIndex m = 0; m < N && !bad; ++m) bad = h->binds[m].len < nb || h->einds[m].len < n;
+    if (bad) {
+        spt_ComplainError(module, SPTERR_VALUE_ERROR, __FILE__, __LINE__, "inconsistent HiCOO arrays");
+        return SPTERR_VALUE_ERROR;
+    }
+    SPTGB_CHECK(sptgb_ctx(), module);
+    const cudaStream_t s = stream ? (cudaStream_t)stream : 0;
+    sptgbHicoo *t = (sptgbHicoo *)calloc(1, sizeof *t);
+    if (!t) return SPTERR_OS_ERROR;
+    t->nmodes = N;
+    for (sptIndex m = 0; m < N; ++m) t->ndims[m] = h->ndims[m];
+    t->nnz = n;
+    t->nb = nb;
+    t->sb_bits = h->sb_bits;
+    int r = 0;
+    cudaError_t e = cudaMalloc((void **)&t->bptr, (nb + 1) * 8);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&t->vals, (n ? n : 1) * 4);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&t->err, 16);
+    for (sptIndex m = 0; m < N && e == cudaSuccess; ++m) {
+        e = cudaMalloc((void **)&t->binds[m], (nb ? nb : 1) * 4);
+        if (e == cudaSuccess) e = cudaMalloc((void **)&t->einds[m], n ? n : 1);
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(t->bptr, h->bptr.data, (nb + 1) * 8, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && n) e = cudaMemcpyAsync(t->vals, h->values.data, n * 4, cudaMemcpyHostToDevice, s);
+    for (sptIndex m = 0; m < N && e == cudaSuccess; ++m) {
+        if (nb) e = cudaMemcpyAsync(t->binds[m], h->binds[m].data, nb * 4, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess && n) e = cudaMemcpyAsync(t->einds[m], h->einds[m].data, n, cudaMemcpyHostToDevice, s);
+    }
+    t->bytes = (nb + 1) * 8 + n * 4 + (size_t)N * (nb * 4 + n);
+    /* every element inside its mode, element offsets below 2^sb */
+    if (e == cudaSuccess) e = cudaMemsetAsync(t->err, 0, 16, s);
+    if (e == cudaSuccess && nb) {
+        sptgb_hicoo_args a;
+        memset(&a, 0, sizeof a);
+        a.bptr = t->bptr;
+        for (sptIndex m = 0; m < N; ++m) {
+            a.binds[m] = t->binds[m];
+            a.einds[m] = t->einds[m];
+            a.ndims[m] = t->ndims[m];
+        }
+        a.nmodes = N;
+        a.nb = nb;
+        a.sb_bits = (uint32_t)t->sb_bits;
+        a.err = t->err;
+        e = sptgb_hicoo_check(&a, s);
+    }
+    unsigned int herr = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, t->err, sizeof herr, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) r = sptgb_cuda_fail(e, module, __FILE__, __LINE__);
+    else if (herr) {
+        spt_ComplainError(module, SPTERR_VALUE_ERROR, __FILE__, __LINE__, "a coordinate is not smaller than its mode size");
+        r = SPTERR_VALUE_ERROR;
+    }
+    if (r) {
+        sptgbHicooFree(t);
+        return r;
+    }
+    *out = t;
+    return 0;
+}
+
+int sptgbHicooPrepareMode(sptgbHicoo *t, sptIndex mode, void *stream) {
+    const char *module = "GPU HiCOO prepare";
+    if (mode >= t->nmodes) return SPTERR_VALUE_ERROR;
+    if (t->ready[mode] || !hicoo_window_ok(t, 8)) return 0;
+    const cudaStream_t s = stream ? (cudaStream_t)stream : 0;
+    const uint64_t nb = t->nb;
+    cudaError_t e = cudaMalloc((void **)&t->perm[mode], (2 * nb + 1) * 4);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&t->wst[mode], (nb + 1) * 8);
+    if (e != cudaSuccess) return sptgb_cuda_fail(e, module, __FILE__, __LINE__);
+    t->pnnz[mode] = t->perm[mode] + nb;
+    t->bytes += (2 * nb + 1) * 4 + (nb + 1) * 8;
+    int r = 0;
+    sptgb_lock();
+    sptgb_hicoo_sched_scratch w;
+    for (int i = 0; i < 2 && !r; ++i) {
+        r = sptgb_dbuf_reserve(&g_ws.keys[i], nb * 4);
+        if (!r) r = sptgb_dbuf_reserve(&g_ws.perm[i], nb * 4);
+        w.keys[i] = (uint32_t *)g_ws.keys[i].ptr;
+        w.vals[i] = (uint32_t *)g_ws.perm[i].ptr;
+    }
+    if (!r) r = sptgb_dbuf_reserve(&g_ws.rtmp, sptgb_radix_tmp_bytes(nb));
+    if (!r) r = sptgb_dbuf_reserve(&g_ws.misc[2], (2 * nb + 1) * 4);
+    if (!r) r = sptgb_dbuf_reserve(&g_ws.misc[5], sptgb_scan_tmp_bytes(nb));
+    if (!r) {
+        w.rtmp = g_ws.rtmp.ptr;
+        w.stmp = g_ws.misc[5].ptr;
+        w.flags = (uint32_t *)g_ws.misc[2].ptr;
+        w.pos = w.flags + nb;
+        const uint32_t maxb = t->ndims[mode] ? (t->ndims[mode] - 1) >> t->sb_bits : 0;
+        e = sptgb_hicoo_schedule(t->binds[mode], t->bptr, nb, sptgb_bitwidth(maxb), &w, t->perm[mode], t->pnnz[mode],
+                                 t->wst[mode], &t->nwin[mode], s);
+        if (e != cudaSuccess) r = sptgb_cuda_fail(e, module, __FILE__, __LINE__);
+    }
+    sptgb_unlock();
+    if (!r) t->ready[mode] = 1;
+    return r;
+}
+
+int sptgbHicooMTTKRP(sptgbHicoo *t, sptIndex mode, const sptIndex *mats_order, const float *const *d_mats,
+                     sptIndex rank, sptIndex stride, float *d_out, void *stream) {
+    const char *module = "GPU HiCOO MTTKRP";
+    const sptIndex N = t->nmodes;
+    if (mode >= N || rank < 1 || stride % 8 || stride > 128 || rank > stride) return SPTERR_VALUE_ERROR;
+    for (sptIndex i = 1; i < N; ++i)
+        if (mats_order[i] >= N) return SPTERR_VALUE_ERROR;
+    const cudaStream_t s = stream ? (cudaStream_t)stream : 0;
+    if (hicoo_window_ok(t, stride) && !t->ready[mode]) SPTGB_CHECK(sptgbHicooPrepareMode(t, mode, stream), module);
+    sptgb_hicoo_args a;
+    memset(&a, 0, sizeof a);
+    a.bptr = t->bptr;
+    for (sptIndex m = 0; m < N; ++m) {
+        a.binds[m] = t->binds[m];
+        a.einds[m] = t->einds[m];
+        a.ndims[m] = t->ndims[m];
+        a.fac[m] = d_mats[m];
+    }
+    a.vals = t->vals;
+    a.out = d_out;
+    a.nb = t->nb;
+    a.out_rows = t->ndims[mode];
+    a.nmodes = N;
+    a.mode = mode;
+    for (sptIndex i = 0; i < N; ++i) a.order[i] = mats_order[i];
+    a.rank = rank;
+    a.stride = stride;
+    a.sb_bits = (uint32_t)t->sb_bits;
+    a.err = t->err + 1;   /* checked once at creation; this flag is not read */
+    a.nnz = t->nnz;
+    if (hicoo_window_ok(t, stride)) {
+        a.perm = t->perm[mode];
+        a.pnnz = t->pnnz[mode];
+        a.wst = t->wst[mode];
+        a.nwin = t->nwin[mode];
+    }
+    SPTGB_CUDA(sptgb_mttkrp_hicoo(&a, s), module);
+    return 0;
+}

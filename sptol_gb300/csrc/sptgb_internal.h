@@ -143,6 +143,9 @@ typedef struct {
     uint64_t        nnz;                       /* = bptr[nb]; below 2^32 for the window kernel */
 } sptgb_hicoo_args;
 cudaError_t sptgb_mttkrp_hicoo(const sptgb_hicoo_args *a, cudaStream_t s);
+/* *a->err = 1 when an element lies outside its mode or its element offset is
+ * not below 2^sb_bits (a->bptr, binds, einds, ndims, nmodes, nb used). */
+cudaError_t sptgb_hicoo_check(const sptgb_hicoo_args *a, cudaStream_t s);
 /* Output-window schedule of one mode: blocks stably sorted by their block
  * index in `mode` (keys = binds_mode, window_bits significant bits), the
  * prefix of their sizes and the start of each run of equal keys.  Scratch:

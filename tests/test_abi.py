@@ -51,6 +51,9 @@ int main(void) {
   O(sptSparseTensorHiCOO, knnzs) O(sptSparseTensorHiCOO, bptr) O(sptSparseTensorHiCOO, binds)
   O(sptSparseTensorHiCOO, einds) O(sptSparseTensorHiCOO, values)
   O(sptKruskalTensor, lambda) O(sptKruskalTensor, fit) O(sptKruskalTensor, factors)
+  P(sptRankKruskalTensor) O(sptRankKruskalTensor, rank) O(sptRankKruskalTensor, lambda)
+  O(sptRankKruskalTensor, fit) O(sptRankKruskalTensor, factors)
+  O(sptRankMatrix, ncols) O(sptRankMatrix, cap) O(sptRankMatrix, stride) O(sptRankMatrix, values)
   return 0;
 }
 """

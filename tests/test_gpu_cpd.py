@@ -91,3 +91,88 @@ def test_rank_above_64_is_rejected():
     with pytest.raises(S.SptError) as e:
         S.cpd_als(t, 65, 1, 0.0, init)
     assert e.value.code == 3
+
+
+@pytest.mark.parametrize("case", ["cpd_3d", "cpd_4d"])
+def test_hicoo_cpd_fits_match_reference(case):
+    """sptgbCpdAlsHiCOO (HiCOO MTTKRP inside the same loop) from the same
+    initial factors: the reference's per-iteration fits within 1e-4."""
+    g = golden(case)
+    ndims = [int(x) for x in g["ndims"]]
+    rank, niters = int(g["rank"]), int(g["niters"])
+    N = len(ndims)
+    t = S.Tensor.from_arrays(ndims, g["inds"], g["vals"])
+    h = S.HiCOO(t, 2, 4)
+    init = [g["init%d" % m] for m in range(N)]
+    facs, lam, fits, it = S.cpd_als_hicoo(h, rank, niters, 0.0, init)
+    assert it == niters
+    assert np.abs(fits - g["fits"]).max() <= FIT_TOL, (fits, g["fits"])
+    for f in facs:
+        assert np.allclose(np.linalg.norm(f.astype(np.float64), axis=0), 1.0, atol=1e-4)
+
+
+def test_hicoo_cpd_matches_coo_cpd_on_skewed_tensor():
+    spec = S.GenSpec()
+    spec.seed = 21
+    spec.nmodes = 3
+    for m, d in enumerate([40_000, 20_000, 3_000]):
+        spec.ndims[m] = d
+    spec.coord_dist[0] = spec.coord_dist[1] = S.DIST_ZIPF
+    spec.zipf_s[0] = spec.zipf_s[1] = 1.2
+    spec.count = 300_000
+    spec.value_dist = S.VAL_U01
+    t = S.Tensor.generate(spec)
+    ndims = t.ndims
+    rng = np.random.default_rng(22)
+    init = [rng.random((d, 16), dtype=np.float32) for d in ndims]
+    _, lam_c, fits_c, _ = S.cpd_als(t, 16, 6, 0.0, init)
+    h = S.HiCOO(t, 7, 12)
+    _, lam_h, fits_h, _ = S.cpd_als_hicoo(h, 16, 6, 0.0, init)
+    assert np.abs(fits_h - fits_c).max() <= FIT_TOL, (fits_h, fits_c)
+
+
+def test_drop_in_cpd_als_hicoo_fills_rank_kruskal_tensor():
+    g = golden("cpd_3d")
+    ndims = [int(x) for x in g["ndims"]]
+    t = S.Tensor.from_arrays(ndims, g["inds"], g["vals"])
+    h = S.HiCOO(t, 2, 4)
+    L = S.lib()
+    k = S.RankKruskalS()
+    nd = (C.c_uint32 * 3)(*ndims)
+    assert L.sptNewRankKruskalTensor(C.byref(k), 3, nd, 4) == 0
+    assert L.sptCpdAlsHiCOO(h.ptr(), 4, 5, 0.0, C.byref(k)) == 0
+    assert np.isfinite(k.fit) and 0.0 < k.fit < 1.0
+    for m in range(3):
+        f = k.factors[m].contents
+        a = np.ctypeslib.as_array(f.values, shape=(int(f.cap), int(f.stride)))[: ndims[m], :4]
+        assert np.allclose(np.linalg.norm(a.astype(np.float64), axis=0), 1.0, atol=1e-4)
+    assert not k.factors[3]
+    L.sptFreeRankKruskalTensor(C.byref(k))
+
+
+@pytest.mark.parametrize("dims,sb", [([3000, 2000, 500], 7), ([300, 200, 100, 50], 4)])
+def test_resident_hicoo_mttkrp_equals_drop_in(dims, sb):
+    torch = pytest.importorskip("torch")
+    spec = S.GenSpec()
+    spec.seed = 31
+    spec.nmodes = len(dims)
+    for m, d in enumerate(dims):
+        spec.ndims[m] = d
+    spec.count = 100_000
+    spec.value_dist = S.VAL_UPM1
+    t = S.Tensor.generate(spec)
+    h = S.HiCOO(t, sb, sb + 3)
+    N = len(dims)
+    rank = 16
+    mats = S.new_factors(dims, rank, seed=3)
+    dev = [torch.from_numpy(mats[m].array()[: dims[m]].copy()).cuda() for m in range(N)]
+    out = torch.zeros((max(dims), 16), device="cuda")
+    dh = S.DeviceHicoo(h)
+    for mode in range(N):
+        order = [mode] + [(mode + i) % N for i in range(1, N)]
+        ref = S.mttkrp_hicoo(h, mats, mode, mats_order=order)
+        dh.mttkrp(mode, order, [d.data_ptr() for d in dev], rank, 16, out.data_ptr())
+        torch.cuda.synchronize()
+        got = out[: dims[mode], :rank].cpu().numpy()
+        assert np.abs(got - ref).max() <= 1e-5 * np.abs(ref).max()
+    dh.free()
