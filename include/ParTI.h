@@ -263,6 +263,11 @@ int sptMTTKRPHiCOO(sptSparseTensorHiCOO const *const hitsr, sptMatrix *mats[], s
 int sptOmpMTTKRPHiCOO(sptSparseTensorHiCOO const *const hitsr, sptMatrix *mats[], sptIndex const mats_order[],
                       sptIndex const mode, const int nt);
 
+/* Text tensor input (load.c:31-84): nmodes, sizes, then per nonzero the
+ * indices (start_index based) and the value; parsed on the GPU, result equal
+ * to the reference's (zero values removed as collect.c:29-49 does). */
+int sptLoadSparseTensor(sptSparseTensor *tsr, sptIndex start_index, FILE *fp);
+
 /* ------------------------------------------------------ Kruskal / CP-ALS -- */
 int  sptNewKruskalTensor(sptKruskalTensor *ktsr, sptIndex nmodes, const sptIndex ndims[], sptIndex rank);
 void sptFreeKruskalTensor(sptKruskalTensor *ktsr);

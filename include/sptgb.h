@@ -59,6 +59,12 @@ size_t      sptgbCooDeviceBytes(const sptgbCoo *t);
 void  sptgbCooSetTiming(sptgbCoo *t, int enable);
 float sptgbCooLastKernelMs(const sptgbCoo *t);
 void  sptgbCooFree(sptgbCoo *t);
+/* sptLoadSparseTensor, then (on the device) a lexicographic sort with
+ * duplicate coordinates summed in file order and zero sums dropped; the
+ * result is marked sorted.  No counterpart in the reference (its loader keeps
+ * duplicates). */
+int sptgbLoadSparseTensorMerged(sptSparseTensor *tsr, sptIndex start_index, FILE *fp);
+
 /* ------------------------------------------------ resident HiCOO tensor --
  * The HiCOO arrays uploaded once; per output mode, the output-window
  * schedule (blocks ordered by their block index in that mode) is built on

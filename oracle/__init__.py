@@ -65,6 +65,7 @@ def orc():
         L.orc_mttkrp_f64.argtypes = mt + [f64p]
         L.orc_omp_mttkrp_f64.argtypes = mt + [f64p, C.c_int]
         L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_load_tns.argtypes = [C.c_char_p, C.c_uint32, u32p, u32p, C.c_uint64, C.POINTER(u32p), f32p, u64p]
         L.orc_omp_mttkrp_reduce.argtypes = mt + [f32p, C.c_int, f32p]
         L.orc_mttkrp_hicoo_f32.argtypes = [C.c_uint32, C.c_uint64, u64p, C.POINTER(u32p), C.POINTER(u8p), f32p,
                                            C.c_int, C.POINTER(f32p), C.c_uint32, C.c_uint32, u32p, C.c_uint32,
@@ -366,3 +367,22 @@ def ref_cpd_trace(ndims, inds, vals, rank, niters, init):
         "loop_factors": [f[:, :rank].copy() for f in lk], "loop_lambda": lam_loop, "fits": fits,
         "step_factors": [f[:, :rank].copy() for f in sk], "step_lambda": lam_step, "step_fit": step_fit.value,
     }
+
+
+def load_tns(path, start_index=1):
+    """The reference's text reader (load.c + collect.c) restated: returns
+    (ndims, inds [N, nnz], vals) or raises ValueError with the reader's code."""
+    size = os.path.getsize(path)
+    cap = size // 2 + 2
+    N = C.c_uint32()
+    nd = (C.c_uint32 * 8)()
+    arrs = [np.zeros(cap, np.uint32) for _ in range(8)]
+    ptrs = (u32p * 8)(*[a.ctypes.data_as(u32p) for a in arrs])
+    vals = np.zeros(cap, np.float32)
+    nnz = C.c_uint64()
+    rc = orc().orc_load_tns(path.encode(), start_index, C.byref(N), nd, cap, ptrs, vals.ctypes.data_as(f32p),
+                            C.byref(nnz))
+    if rc != 0:
+        raise ValueError("reader returned %d" % rc)
+    n = int(nnz.value)
+    return [int(nd[m]) for m in range(N.value)], np.stack([a[:n] for a in arrs[: N.value]]), vals[:n].copy()

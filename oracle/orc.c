@@ -16,6 +16,7 @@
 #include <math.h>
 #include <omp.h>
 #include <stdint.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -665,4 +666,63 @@ double orc_fit_exact(uint32_t nmodes, const uint32_t *ndims, uint64_t nnz, const
     double res = normX2 + normK - 2.0 * inner;
     if (res > 0.0) res = sqrt(res);
     return 1.0 - res / sqrt(normX2);
+}
+
+/* load.c:31-84 then collect.c:29-49: the reference's fscanf reader (stops at
+ * the first token that does not convert; an index below start_index is an
+ * error, -1) and its zero removal by moving the last nonzero in.  inds[m]
+ * and vals hold `cap` entries. */
+int orc_load_tns(const char *path, uint32_t start_index, uint32_t *nmodes_out, uint32_t *ndims_out, uint64_t cap,
+                 uint32_t *const *inds, float *vals, uint64_t *nnz_out) {
+    FILE *fp = fopen(path, "r");
+    if (!fp) return -2;
+    uint32_t N = 0;
+    if (fscanf(fp, "%u", &N) != 1 || N < 1 || N > ORC_MAX_MODES) {
+        fclose(fp);
+        return -3;
+    }
+    for (uint32_t m = 0; m < N; ++m)
+        if (fscanf(fp, "%u", &ndims_out[m]) != 1) {
+            fclose(fp);
+            return -3;
+        }
+    *nmodes_out = N;
+    uint64_t nnz = 0;
+    int stop = 0, rc = 0;
+    while (!stop) {
+        uint32_t idx[ORC_MAX_MODES];
+        for (uint32_t m = 0; m < N; ++m) {
+            if (fscanf(fp, "%u", &idx[m]) != 1) {
+                stop = 1;
+                break;
+            }
+            if (idx[m] < start_index) {
+                rc = -1;
+                stop = 1;
+                break;
+            }
+        }
+        if (stop) break;
+        double v;
+        if (fscanf(fp, "%lf", &v) != 1) break;
+        if (nnz < cap) {
+            for (uint32_t m = 0; m < N; ++m) inds[m][nnz] = idx[m] - start_index;
+            vals[nnz] = (float)v;
+        }
+        ++nnz;
+    }
+    fclose(fp);
+    if (nnz > cap) return -4;
+    uint64_t i = 0;
+    while (i < nnz) {
+        if (vals[i] == 0) {
+            for (uint32_t m = 0; m < N; ++m) inds[m][i] = inds[m][nnz - 1];
+            vals[i] = vals[nnz - 1];
+            --nnz;
+        } else {
+            ++i;
+        }
+    }
+    *nnz_out = nnz;
+    return rc;
 }

@@ -199,6 +199,30 @@ cudaError_t sptgb_sumsq(const float *v, uint64_t n, double *out, double *ws, cud
 cudaError_t sptgb_colnorm_scale(float *A, uint32_t nrows, int rank, int stride, float *lambda_mul,
                                 double *ws, cudaStream_t s);
 
+/* ------------------------------------------------------ text ingest --
+ * Token-parallel parse of a whitespace-separated tensor body (ingest.cu). */
+typedef struct {
+    uint32_t nmodes, start_index;
+    uint64_t max_records;
+    uint32_t *inds[SPTGB_MAX_MODES];   /* [max_records] each, index - start_index */
+    float *vals;                       /* [max_records] */
+    uint64_t *first_bad;               /* device: smallest invalid token (init ~0) */
+    uint64_t *first_below;             /* device: smallest index token below start_index (init ~0) */
+    uint64_t *nslow;                   /* device: values left to the host parser */
+    uint64_t slow_cap;
+    uint64_t *slow_rec, *slow_off;     /* [slow_cap]: record and byte offset (from base_off) */
+    uint64_t base_off;                 /* byte offset of this chunk in the body */
+} sptgb_ingest_out;
+/* Token starts of buf[0, n): starts[0, *ntok) (device count). */
+cudaError_t sptgb_ingest_token_starts(const void *buf, uint64_t n, uint32_t *flags, uint32_t *pos, uint32_t *ntok,
+                                      void *scan_tmp, uint64_t *starts, cudaStream_t s);
+cudaError_t sptgb_ingest_parse(const void *buf, uint64_t n, const uint64_t *starts, uint64_t ntok, uint64_t base_tok,
+                               const sptgb_ingest_out *o, cudaStream_t s);
+/* Sum of vals[starts[g] .. starts[g+1]) in order for each group g < ng
+ * (starts[ng] = n), into out[g]. */
+cudaError_t sptgb_segment_sums(const uint64_t *starts, uint64_t ng, uint64_t n, const float *vals, float *out,
+                               cudaStream_t s);
+
 /* ------------------------------------------------- batched CP-ALS --
  * Device descriptor of one tensor ("slot") of a batch, written once at
  * admission.  Records for mode m are 16-byte {row, a, b, value} (order 3) or
