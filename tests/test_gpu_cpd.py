@@ -176,3 +176,17 @@ def test_resident_hicoo_mttkrp_equals_drop_in(dims, sb):
         got = out[: dims[mode], :rank].cpu().numpy()
         assert np.abs(got - ref).max() <= 1e-5 * np.abs(ref).max()
     dh.free()
+
+
+def test_order5_cpd_against_oracle():
+    rng = np.random.default_rng(55)
+    ndims = [30, 25, 20, 15, 10]
+    n = 30000
+    inds = np.unique(np.stack([rng.integers(0, d, 2 * n) for d in ndims]).astype(np.uint32), axis=1)
+    inds = inds[:, rng.permutation(inds.shape[1])[:n]]
+    vals = rng.random(inds.shape[1], dtype=np.float32)
+    t = S.Tensor.from_arrays(ndims, inds, vals)
+    init = [rng.random((d, 6), dtype=np.float32) for d in ndims]
+    facs, lam, fits, it = S.cpd_als(t, 6, 5, 0.0, init)
+    _, _, ofits, _ = O.cpd_als(ndims, inds, vals, 6, 5, 0.0, init)
+    assert np.abs(fits - ofits).max() <= FIT_TOL, (fits, ofits)

@@ -170,3 +170,25 @@ def test_c2_power_law_against_fp64():
         print("nnz %d mode %d  ours vs FP64 %.2e  reference-order FP32 vs FP64 %.2e  ours vs reference order %.2e"
               % (nnz, mode, ours, theirs, rel_fro(out, seq)))
         assert ours <= TOL
+
+
+@pytest.mark.parametrize("ndims", [[700, 500], [40, 30, 20, 10, 9], [12, 11, 10, 9, 8, 7], [6, 5, 5, 4, 4, 3, 3, 2]])
+@pytest.mark.parametrize("entry", ["sptMTTKRP", "sptCudaMTTKRP"])
+def test_orders_2_5_6_8_against_fp64(ndims, entry):
+    """Orders other than 3 and 4 run the generic segmented kernel (runtime
+    number of product modes): every mode, a non-default mats_order."""
+    rng = np.random.default_rng(len(ndims))
+    n = 20000
+    inds = np.unique(np.stack([rng.integers(0, d, 2 * n) for d in ndims]).astype(np.uint32), axis=1)
+    inds = inds[:, rng.permutation(inds.shape[1])[:n]]
+    vals = rng.uniform(-1, 1, inds.shape[1]).astype(np.float32)
+    t = S.Tensor.from_arrays(ndims, inds, vals)
+    rank = 12
+    N = len(ndims)
+    mats = S.new_factors(ndims, rank, seed=N)
+    facs = [mats[m].array()[: ndims[m]].copy() for m in range(N)]
+    for mode in range(N):
+        order = [mode] + [m for m in reversed(range(N)) if m != mode]
+        out = S.mttkrp(t, mats, mode, mats_order=order, entry=entry)
+        ref = O.mttkrp(ndims, inds, vals, facs, rank, mode, order=order, precision="f64")
+        assert rel_fro(out, ref) <= TOL, (ndims, mode)
