@@ -88,8 +88,10 @@ rs_downsweep(const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin,
              uint32_t *__restrict__ vout, uint64_t n, int shift, const uint32_t *__restrict__ counts,
              const uint32_t *__restrict__ totals, uint32_t ntiles) {
     __shared__ uint32_t s_cnt[RS_WARPS][256];
-    __shared__ uint32_t s_goff[256];
+    __shared__ uint32_t s_goff[256];     // global position of the tile's first element of each digit
+    __shared__ uint32_t s_tstart[256];   // tile-local position of the first element of each digit
     __shared__ uint32_t s_wtot[RS_WARPS];
+    __shared__ uint32_t s_key[RS_TILE], s_val[RS_TILE];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     // Global offset of each digit for this tile: exclusive scan of the digit
@@ -111,7 +113,10 @@ rs_downsweep(const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin,
     for (int i = lane; i < 256; i += 32) s_cnt[warp][i] = 0;
     __syncwarp();
 
-    const uint64_t wbase = (uint64_t)blockIdx.x * RS_TILE + (uint64_t)warp * (RS_ITEMS * 32);
+    // Stable rank of every element among equal digits: warp-local ranks from
+    // __match_any_sync, in warp order within the tile.
+    const uint64_t tbase = (uint64_t)blockIdx.x * RS_TILE;
+    const uint64_t wbase = tbase + (uint64_t)warp * (RS_ITEMS * 32);
     const unsigned lt_mask = (1u << lane) - 1u;
     uint32_t key[RS_ITEMS], val[RS_ITEMS], rank[RS_ITEMS];
 #pragma unroll
@@ -134,6 +139,8 @@ rs_downsweep(const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin,
         }
     }
     __syncthreads();
+    // per digit: offsets of the warps within the tile's run of that digit,
+    // then the tile-local start of every digit (exclusive scan over digits)
     {
         const int d = threadIdx.x;
         uint32_t run = 0;
@@ -143,18 +150,43 @@ rs_downsweep(const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin,
             s_cnt[w][d] = run;
             run += c;
         }
+        uint32_t x = run;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(FULL, x, o);
+            if (lane >= o) x += y;
+        }
+        __syncthreads();   // s_wtot is reused
+        if (lane == 31) s_wtot[warp] = x;
+        __syncthreads();
+        uint32_t before = 0;
+        for (int w = 0; w < warp; ++w) before += s_wtot[w];
+        s_tstart[d] = before + x - run;
     }
     __syncthreads();
+    // the tile in digit order in shared memory
 #pragma unroll
     for (int r = 0; r < RS_ITEMS; ++r) {
         const uint64_t k = wbase + (uint64_t)r * 32 + lane;
         if (k < n) {
             const uint32_t d = (key[r] >> shift) & 255u;
-            const uint64_t pos = (uint64_t)s_goff[d] + s_cnt[warp][d] + rank[r];
-            if (pos < n) {   // always true for consistent counts; keeps a bad count in bounds
-                kout[pos] = key[r];
-                vout[pos] = val[r];
+            const uint32_t lp = s_tstart[d] + s_cnt[warp][d] + rank[r];
+            if (lp < (uint32_t)RS_TILE) {   // always true for consistent counts
+                s_key[lp] = key[r];
+                s_val[lp] = val[r];
             }
+        }
+    }
+    __syncthreads();
+    // runs of equal digits go to consecutive global positions: coalesced writes
+    const uint32_t tn = (uint32_t)min((uint64_t)RS_TILE, n - tbase);
+    for (uint32_t i = threadIdx.x; i < tn; i += RS_THREADS) {
+        const uint32_t kk = s_key[i];
+        const uint32_t d = (kk >> shift) & 255u;
+        const uint64_t pos = (uint64_t)s_goff[d] + (i - s_tstart[d]);
+        if (pos < n) {   // always true for consistent counts; keeps a bad count in bounds
+            kout[pos] = kk;
+            vout[pos] = s_val[i];
         }
     }
 }
