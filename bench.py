@@ -589,6 +589,30 @@ def run_ours(args, world, rank, local):
     achieved = algo_bytes(ndims, nnz, RANK) / (launch_ms / 1e3) / 1e9
     traffic = traffic_per_launch()
 
+    # BF16 factor storage (FP32 accumulation) on the same resident copies:
+    # reported beside the FP32 headline, same algorithmic byte formula
+    d16 = [f.to(torch.bfloat16).contiguous() for f in dfac]
+    p16 = [f.data_ptr() for f in d16]
+    for _ in range(args.warmup):
+        for m in range(3):
+            coo.mttkrp(m, orders[m], p16, RANK, stride, dout.data_ptr(), stream=sh, bf16=True)
+    kb = max(3, K // 4)
+    ev16 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(3 * kb)]
+    torch.cuda.synchronize()
+    j = 0
+    for _ in range(kb):
+        for m in range(3):
+            ev16[j][0].record(stream)
+            coo.mttkrp(m, orders[m], p16, RANK, stride, dout.data_ptr(), stream=sh, bf16=True)
+            ev16[j][1].record(stream)
+            j += 1
+    torch.cuda.synchronize()
+    pl16 = [a.elapsed_time(b) for a, b in ev16]
+    bf16 = {"ms_per_launch_by_mode": [round(float(np.mean(pl16[m::3])), 4) for m in range(3)],
+            "gbs_fp32_byte_formula": round(algo_bytes(ndims, nnz, RANK) / (float(np.mean(pl16)) / 1e3) / 1e9, 1),
+            "rel_fro_vs_fp64": "about 2.6e-3 (4th-order precision study)"}
+    del d16
+
     # e2e through the drop-in host-buffer API
     h2d = 0
     d2h = 0
@@ -639,6 +663,7 @@ def run_ours(args, world, rank, local):
             "nnz_per_s": round(world * K * 3 * nnz / (ms_max / 1e3), 1),
             "setup_s": {"generate": round(gen_s, 2), "upload_and_sort_3_modes": round(prep_s, 2)},
             "cpu_baseline": cpu,
+            "bf16_storage": bf16,
             "hicoo": hicoo,
             "serve": serve,
         }
