@@ -443,7 +443,7 @@ def cpu_port_mttkrp(t, mats, threads, reps):
             O.mttkrp(t.ndims, inds, vals, facs, RANK, mode, precision="omp", tk=threads)
         if r > 0:
             best.append(time.perf_counter() - t0)
-    return float(np.mean(best))
+    return float(np.mean(best)) if best else 0.0
 
 
 def cpu_reference_mttkrp(t, mats, threads, reps):
