@@ -485,8 +485,18 @@ __device__ __forceinline__ void lambda_body(const double *__restrict__ gpart, co
     __shared__ double lam[RMAX];
     const int P = rank * (rank + 1) / 2;
     for (int i = threadIdx.x; i < P; i += blockDim.x) {
-        double s = 0.0;
-        for (int b = 0; b < nblk; ++b) s += gpart[(uint64_t)b * P + i];
+        // four independent running sums (blocks b = 0, 1, 2, 3 mod 4) keep
+        // several loads and FP64 adds in flight; combined in a fixed order
+        double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+        int b = 0;
+        for (; b + 4 <= nblk; b += 4) {
+            s0 += gpart[(uint64_t)(b + 0) * P + i];
+            s1 += gpart[(uint64_t)(b + 1) * P + i];
+            s2 += gpart[(uint64_t)(b + 2) * P + i];
+            s3 += gpart[(uint64_t)(b + 3) * P + i];
+        }
+        for (; b < nblk; ++b) s0 += gpart[(uint64_t)b * P + i];
+        const double s = (s0 + s1) + (s2 + s3);
         int p, q;
         pair_of(i, rank, &p, &q);
         G[p * rank + q] = s;
@@ -517,14 +527,24 @@ __device__ __forceinline__ void lambda_body(const double *__restrict__ gpart, co
     }
 }
 
+// X[i, j] /= lambda[j] for j < rank (padding columns untouched), one float4
+// of a row per thread: rows are stride floats, so float4 e of the matrix is
+// row e / (stride/4), columns 4 * (e % (stride/4)) + 0..3.
 __device__ __forceinline__ void scale_cols_body(float *__restrict__ X, uint32_t nrows, int rank, int stride,
                              const float *__restrict__ lambda, unsigned bid, unsigned nbk) {
-    const uint64_t total = (uint64_t)nrows * rank;
+    const uint32_t c4n = (uint32_t)stride / 4;
+    const uint64_t total = (uint64_t)nrows * c4n;
+    float4 *X4 = reinterpret_cast<float4 *>(X);
     for (uint64_t e = bid * (uint64_t)blockDim.x + threadIdx.x; e < total;
          e += (uint64_t)nbk * blockDim.x) {
-        const uint64_t i = e / rank;
-        const int j = (int)(e % rank);
-        X[i * stride + j] = X[i * stride + j] / lambda[j];
+        const int j = (int)((uint32_t)(e % c4n) * 4);
+        if (j >= rank) continue;
+        float4 v = X4[e];
+        v.x = v.x / lambda[j];
+        if (j + 1 < rank) v.y = v.y / lambda[j + 1];
+        if (j + 2 < rank) v.z = v.z / lambda[j + 2];
+        if (j + 3 < rank) v.w = v.w / lambda[j + 3];
+        X4[e] = v;
     }
 }
 
