@@ -144,6 +144,19 @@ typedef struct {
 
 typedef struct { sptIndex key; sptIndex value; } sptKeyValuePair;
 
+/* Semi-sparse tensor (structs.h:167-175): mode `mode` dense, the others
+ * sparse; nnz dense fibers of `stride` values (ndims[mode] rounded up to 8),
+ * inds[m] the fiber coordinates for m != mode (inds[mode] unused). */
+typedef struct {
+    sptIndex nmodes;
+    sptIndex *ndims;
+    sptIndex mode;
+    sptNnzIndex nnz;
+    sptIndexVector *inds;
+    sptIndex stride;
+    sptMatrix values;
+} sptSemiSparseTensor;
+
 /* Opaque timer (macros.h:38); this library's timers are CUDA events on the
  * library stream when use_cuda != 0, CLOCK_MONOTONIC otherwise. */
 typedef struct sptTagTimer *sptTimer;
@@ -203,6 +216,7 @@ void sptFreeNnzIndexVector(sptNnzIndexVector *vec);
  * include/includes/matrices.h (containers; the CP-ALS reductions run on the
  * GPU inside sptCpdAls). */
 int  sptNewMatrix(sptMatrix *mtx, sptIndex const nrows, sptIndex const ncols);
+int  sptResizeMatrix(sptMatrix *mtx, sptIndex const new_nrows);
 int  sptRandomizeMatrix(sptMatrix *mtx, sptIndex const nrows, sptIndex const ncols);
 int  sptIdentityMatrix(sptMatrix *mtx);
 int  sptConstantMatrix(sptMatrix *const mtx, sptValue const val);
@@ -262,6 +276,22 @@ int sptMTTKRPHiCOO(sptSparseTensorHiCOO const *const hitsr, sptMatrix *mats[], s
                    sptIndex const mode);
 int sptOmpMTTKRPHiCOO(sptSparseTensorHiCOO const *const hitsr, sptMatrix *mats[], sptIndex const mats_order[],
                       sptIndex const mode, const int nt);
+
+/* Semi-sparse tensors and sparse tensor times matrix (ssptensors.h:26-31,
+ * sptensors.h:136-139): Y = X x_mode U, one dense fiber of U->ncols values per
+ * distinct coordinate of the other modes.  X is sorted at `mode` (mode last)
+ * in place, as the reference does; the products are accumulated on the GPU
+ * in nonzero order with separately rounded multiplies and adds. */
+int  sptNewSemiSparseTensor(sptSemiSparseTensor *tsr, sptIndex nmodes, sptIndex mode, const sptIndex ndims[]);
+void sptFreeSemiSparseTensor(sptSemiSparseTensor *tsr);
+int  sptSemiSparseTensorToSparseTensor(sptSparseTensor *dest, const sptSemiSparseTensor *src, sptValue epsilon);
+int  sptSparseTensorMulMatrix(sptSemiSparseTensor *Y, sptSparseTensor *X, const sptMatrix *U, sptIndex const mode);
+int  sptOmpSparseTensorMulMatrix(sptSemiSparseTensor *Y, sptSparseTensor *X, const sptMatrix *U, sptIndex const mode);
+int  sptCudaSparseTensorMulMatrix(sptSemiSparseTensor *Y, sptSparseTensor *X, const sptMatrix *U,
+                                  sptIndex const mode);
+int  sptCudaSparseTensorMulMatrixOneKernel(sptSemiSparseTensor *Y, sptSparseTensor *X, const sptMatrix *U,
+                                           sptIndex const mode, sptIndex const impl_num,
+                                           sptNnzIndex const smen_size);
 
 /* Text tensor input (load.c:31-84): nmodes, sizes, then per nonzero the
  * indices (start_index based) and the value; parsed on the GPU, result equal

@@ -65,6 +65,9 @@ def orc():
         L.orc_mttkrp_f64.argtypes = mt + [f64p]
         L.orc_omp_mttkrp_f64.argtypes = mt + [f64p, C.c_int]
         L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_ttm.restype = C.c_uint64
+        L.orc_ttm.argtypes = [C.c_uint32, C.c_uint64, C.POINTER(u32p), f32p, C.c_uint32, f32p, C.c_uint32,
+                              C.c_uint32, C.c_uint32, C.POINTER(u32p), f32p]
         L.orc_load_tns.argtypes = [C.c_char_p, C.c_uint32, u32p, u32p, C.c_uint64, C.POINTER(u32p), f32p, u64p]
         L.orc_omp_mttkrp_reduce.argtypes = mt + [f32p, C.c_int, f32p]
         L.orc_mttkrp_hicoo_f32.argtypes = [C.c_uint32, C.c_uint64, u64p, C.POINTER(u32p), C.POINTER(u8p), f32p,
@@ -115,6 +118,9 @@ def ref():
         L.ref_cpd_trace.argtypes = [C.c_uint32, u32p, C.c_uint64, C.POINTER(u32p), f32p, C.c_uint32, C.c_uint32,
                                     C.POINTER(f32p), C.c_uint32, C.POINTER(f32p), f32p, f64p, C.POINTER(f32p), f32p,
                                     f64p]
+        L.ref_ttm.restype = C.c_uint64
+        L.ref_ttm.argtypes = [C.c_uint32, u32p, C.c_uint64, C.POINTER(u32p), f32p, C.c_uint32, f32p, C.c_uint32,
+                              C.c_uint32, C.POINTER(u32p), f32p, u32p]
         _REF = L
     return _REF
 
@@ -386,3 +392,48 @@ def load_tns(path, start_index=1):
         raise ValueError("reader returned %d" % rc)
     n = int(nnz.value)
     return [int(nd[m]) for m in range(N.value)], np.stack([a[:n] for a in arrs[: N.value]]), vals[:n].copy()
+
+
+def ttm(ndims, inds, vals, U, mode, sort=True):
+    """Sparse tensor times matrix as the reference computes it: the tensor
+    sorted with `mode` last (sort=False: taken in the given order, as the
+    reference does when the tensor's sortorder already says so), a dense
+    fiber per run of equal coordinates in the other modes.  Returns (fiber
+    coordinates [N, nfib] (row `mode` zero), Y [nfib, ncols], the
+    permutation applied)."""
+    N, n = inds.shape
+    order = [m for m in range(N) if m != mode] + [mode]
+    p = sort_lex(inds, order) if sort else np.arange(n)
+    si = np.ascontiguousarray(inds[:, p])
+    sv = np.ascontiguousarray(vals[p], np.float32)
+    U = np.asarray(U, np.float32)
+    ncols = U.shape[1]
+    ustride = stride_of(ncols)
+    Up = np.zeros((U.shape[0], ustride), np.float32)
+    Up[:, :ncols] = U
+    keep, ip = _rows(list(si), u32p, np.uint32)
+    fib = [np.zeros(max(n, 1), np.uint32) for _ in range(N)]
+    fp = (u32p * N)(*[f.ctypes.data_as(u32p) for f in fib])
+    Y = np.zeros((max(n, 1), ustride), np.float32)
+    nf = orc().orc_ttm(N, n, ip, sv.ctypes.data_as(f32p), mode, Up.ctypes.data_as(f32p), ustride, ncols, ustride,
+                       fp, Y.ctypes.data_as(f32p))
+    return np.stack([f[:nf] for f in fib]), Y[:nf, :ncols], p
+
+
+def ref_ttm(ndims, inds, vals, U, mode):
+    """The reference's own sptSparseTensorMulMatrix (tensor marked unsorted).
+    Returns (fiber coordinates, Y [nfib, ncols], sorted inds, sorted vals)."""
+    N, n = inds.shape
+    si = [np.ascontiguousarray(a, np.uint32).copy() for a in inds]
+    sp = (u32p * N)(*[a.ctypes.data_as(u32p) for a in si])
+    sv = np.ascontiguousarray(vals, np.float32).copy()
+    U = np.ascontiguousarray(U, np.float32)
+    ncols = U.shape[1]
+    fib = [np.zeros(max(n, 1), np.uint32) for _ in range(N)]
+    fp = (u32p * N)(*[f.ctypes.data_as(u32p) for f in fib])
+    Y = np.zeros((max(n, 1), stride_of(ncols)), np.float32)
+    ys = C.c_uint32()
+    nd, ndp = _u32(ndims)
+    nf = ref().ref_ttm(N, ndp, n, sp, sv.ctypes.data_as(f32p), mode, U.ctypes.data_as(f32p), U.shape[0], ncols, fp,
+                       Y.ctypes.data_as(f32p), C.byref(ys))
+    return np.stack([f[:nf] for f in fib]), Y[:nf, :ncols], np.stack(si), sv

@@ -726,3 +726,29 @@ int orc_load_tns(const char *path, uint32_t start_index, uint32_t *nmodes_out, u
     *nnz_out = nnz;
     return rc;
 }
+
+/* setinds.c:33-71 and mmul.c:37-97 on a tensor already sorted at `mode`
+ * (mode last): fiber f starts where a coordinate other than `mode` differs
+ * from the fiber's first nonzero; Y[f, k] accumulates v * U[i_mode, k] in
+ * nonzero order.  fib[m] receive the fiber coordinates (m != mode).
+ * Returns the number of fibers. */
+uint64_t orc_ttm(uint32_t N, uint64_t nnz, const uint32_t *const *inds, const float *vals, uint32_t mode,
+                 const float *U, uint32_t ustride, uint32_t ncols, uint32_t ystride, uint32_t *const *fib, float *Y) {
+    uint64_t nf = 0, head = nnz;
+    for (uint64_t i = 0; i < nnz; ++i) {
+        int diff = head == nnz;
+        for (uint32_t m = 0; m < N && !diff; ++m)
+            if (m != mode && inds[m][i] != inds[m][head]) diff = 1;
+        if (diff) {
+            for (uint32_t m = 0; m < N; ++m)
+                if (m != mode) fib[m][nf] = inds[m][i];
+            for (uint32_t k = 0; k < ystride; ++k) Y[nf * ystride + k] = 0.f;
+            head = i;
+            ++nf;
+        }
+        const uint32_t r = inds[mode][i];
+        float *y = Y + (nf - 1) * ystride;
+        for (uint32_t k = 0; k < ncols; ++k) y[k] += vals[i] * U[(size_t)r * ustride + k];
+    }
+    return nf;
+}

@@ -263,3 +263,31 @@ int ref_cpd_trace(uint32_t nmodes, const uint32_t *ndims, uint64_t nnz, uint32_t
     sptFreeSparseTensor(&X);
     return 0;
 }
+
+/* The reference's sptSparseTensorMulMatrix (mmul.c:37-97) on a tensor marked
+ * unsorted (sortorder all zero, as its text loader leaves it).  Writes the
+ * sorted coordinates/values back, the fiber coordinates (fib[m], m != mode)
+ * and Y (nfib x ystride); returns the number of fibers. */
+uint64_t ref_ttm(uint32_t nmodes, const uint32_t *ndims, uint64_t nnz, uint32_t *const *inds, float *vals,
+                 uint32_t mode, const float *U, uint32_t urows, uint32_t ncols, uint32_t *const *fib, float *Y,
+                 uint32_t *ystride_out) {
+    sptSparseTensor X;
+    build_tensor(&X, nmodes, ndims, nnz, inds, vals);
+    for (uint32_t m = 0; m < nmodes; ++m) X.sortorder[m] = 0;
+    sptMatrix Um;
+    sptNewMatrix(&Um, urows, ncols);
+    for (uint32_t i = 0; i < urows; ++i) memcpy(Um.values + (size_t)i * Um.stride, U + (size_t)i * ncols, ncols * 4);
+    sptSemiSparseTensor Yt;
+    sptSparseTensorMulMatrix(&Yt, &X, &Um, mode);
+    for (uint32_t m = 0; m < nmodes; ++m) memcpy(inds[m], X.inds[m].data, nnz * 4);
+    memcpy(vals, X.values.data, nnz * 4);
+    for (uint32_t m = 0; m < nmodes; ++m)
+        if (m != mode) memcpy(fib[m], Yt.inds[m].data, Yt.nnz * 4);
+    memcpy(Y, Yt.values.values, (size_t)Yt.nnz * Yt.stride * 4);
+    *ystride_out = Yt.stride;
+    const uint64_t nf = Yt.nnz;
+    sptFreeSemiSparseTensor(&Yt);
+    sptFreeMatrix(&Um);
+    sptFreeSparseTensor(&X);
+    return nf;
+}

@@ -68,6 +68,11 @@ class MatrixS(C.Structure):
                 ("values", f32p)]
 
 
+class SemiSparseS(C.Structure):
+    _fields_ = [("nmodes", C.c_uint32), ("ndims", u32p), ("mode", C.c_uint32), ("nnz", C.c_uint64),
+                ("inds", C.POINTER(IndexVector)), ("stride", C.c_uint32), ("values", MatrixS)]
+
+
 class RankMatrixS(C.Structure):
     _fields_ = [("nrows", C.c_uint32), ("ncols", C.c_uint8), ("cap", C.c_uint32), ("stride", C.c_uint8),
                 ("values", f32p)]
@@ -159,6 +164,10 @@ def _declare(L):
         "sptgbCooLastKernelMs": (C.c_float, [C.c_void_p]),
         "sptgbCooFree": (None, [C.c_void_p]),
         "sptgbHiCOOSetTiming": (None, [C.c_int]),
+        "sptSparseTensorMulMatrix": (C.c_int, [C.POINTER(SemiSparseS), T, M, C.c_uint32]),
+        "sptCudaSparseTensorMulMatrix": (C.c_int, [C.POINTER(SemiSparseS), T, M, C.c_uint32]),
+        "sptFreeSemiSparseTensor": (None, [C.POINTER(SemiSparseS)]),
+        "sptSemiSparseTensorToSparseTensor": (C.c_int, [T, C.POINTER(SemiSparseS), C.c_float]),
         "sptNewRankMatrix": (C.c_int, [C.POINTER(RankMatrixS), C.c_uint32, C.c_uint8]),
         "sptFreeRankMatrix": (None, [C.POINTER(RankMatrixS)]),
         "sptNewRankKruskalTensor": (C.c_int, [C.POINTER(RankKruskalS), C.c_uint32, u32p, C.c_uint8]),

@@ -1,6 +1,8 @@
 """Pins the oracle (the C restatement in oracle/orc.c) to the reference's own
 outputs stored in tests/golden: bit-exact sorts, HiCOO arrays and MTTKRP
 (same summation order), CP-ALS fits within 1e-6."""
+import os
+
 import numpy as np
 import pytest
 
@@ -119,3 +121,23 @@ def test_threaded_fp64_oracle_equals_sequential():
         a = O.mttkrp(nd, inds, vals, mats, 16, m, precision="f64")
         b = O.mttkrp(nd, inds, vals, mats, 16, m, precision="f64_omp", tk=4)
         assert np.abs(a - b).max() <= 1e-13 * np.abs(a).max()
+
+
+@pytest.mark.skipif(not os.path.isdir("/root/reference/src"), reason="reference sources not present")
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_ttm_oracle_equals_reference(mode):
+    """The TTM restatement against the reference's own sptSparseTensorMulMatrix
+    (built here from its sources): sorted tensor, fibers and values bit-exact."""
+    rng = np.random.default_rng(40 + mode)
+    ndims = [30, 20, 15]
+    inds = np.unique(np.stack([rng.integers(0, d, 6000) for d in ndims]).astype(np.uint32), axis=1)
+    inds = inds[:, rng.permutation(inds.shape[1])[:3000]]
+    vals = rng.uniform(-1, 1, inds.shape[1]).astype(np.float32)
+    U = rng.uniform(-1, 1, (ndims[mode], 11)).astype(np.float32)
+    fib, Y, p = O.ttm(ndims, inds, vals, U, mode)
+    rfib, rY, rinds, rvals = O.ref_ttm(ndims, inds, vals, U, mode)
+    assert np.array_equal(inds[:, p], rinds) and np.array_equal(vals[p], rvals)
+    for m in range(3):
+        if m != mode:
+            assert np.array_equal(fib[m], rfib[m])
+    assert np.array_equal(Y.view(np.uint32), rY.view(np.uint32))
