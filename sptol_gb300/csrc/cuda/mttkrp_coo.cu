@@ -169,14 +169,15 @@ k_mttkrp_seg(sptgb_mttkrp_args a, uint32_t unit_len, uint64_t nunits) {
 template <int W, bool BF16, bool FULL>
 __global__ void __launch_bounds__(BLOCK, 3)
 k_mttkrp_rec(const uint4 *__restrict__ rec, const void *__restrict__ Fa, const void *__restrict__ Fb,
-             float *__restrict__ out, uint64_t nnz, uint32_t stride, uint32_t rank, uint32_t ul, uint64_t nunits) {
+             float *__restrict__ out, uint64_t nnz, uint32_t stride, uint32_t rank, uint32_t ul, uint64_t u0,
+             uint64_t nunits) {
     const int sl = (threadIdx.x & 31) % W;
     const uint32_t elem = BF16 ? 2u : 4u;
     const char *F[2] = {static_cast<const char *>(Fa) + (size_t)sl * 4 * elem,
                         static_cast<const char *>(Fb) + (size_t)sl * 4 * elem};
     const uint64_t worker = ((uint64_t)blockIdx.x * BLOCK + threadIdx.x) / W;
     const uint64_t nworkers = ((uint64_t)gridDim.x * BLOCK) / W;
-    for (uint64_t u = worker; u < nunits; u += nworkers) {
+    for (uint64_t u = u0 + worker; u < nunits; u += nworkers) {
         const uint64_t start = u * ul;
         const uint32_t len = (uint32_t)min((uint64_t)ul, nnz - start);
         sptgb_mttkrp::unit<BF16, FULL, 2>(rec, nullptr, F, stride * elem, out, nnz, start, len, stride, rank, sl);
@@ -184,10 +185,16 @@ k_mttkrp_rec(const uint4 *__restrict__ rec, const void *__restrict__ Fa, const v
 }
 
 __global__ void k_pack_records(const uint32_t *__restrict__ rows, const uint32_t *__restrict__ ia,
-                               const uint32_t *__restrict__ ib, const float *__restrict__ vals, uint4 *__restrict__ rec,
-                               uint64_t n) {
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
-        rec[i] = make_uint4(rows[i], ia[i], ib[i], __float_as_uint(vals[i]));
+                               const uint32_t *__restrict__ ib, const float *__restrict__ vals, uint32_t lim_a,
+                               uint32_t lim_b, unsigned int *__restrict__ bad, uint4 *__restrict__ rec, uint64_t n) {
+    unsigned int b = 0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t a = ia[i], c = ib[i];
+        const bool ok = a < lim_a && c < lim_b;
+        b |= !ok;
+        rec[i] = make_uint4(rows[i], ok ? a : 0u, ok ? c : 0u, __float_as_uint(vals[i]));
+    }
+    if (__any_sync(0xffffffffu, b) && (threadIdx.x & 31) == 0 && bad) atomicOr(bad, 1u);
 }
 
 // Zero every row that two neighbouring units share, before the main kernel
@@ -249,16 +256,20 @@ cudaError_t launch_rec_k(const sptgb_mttkrp_args &a, cudaStream_t s) {
         max_blocks = (per_sm < 1 ? 1 : per_sm) * nsm;
     }
     // 256-nonzero units: enough of them to balance a power-law row distribution
-    const uint32_t ul = 256;
+    const uint32_t ul = SPTGB_REC_UNIT;
     const uint64_t nunits = (a.nnz + ul - 1) / ul;
+    const uint64_t u1 = a.unit_end && a.unit_end < nunits ? a.unit_end : nunits;
+    if (a.unit_begin >= u1) return cudaSuccess;
     const uint64_t wpb = BLOCK / W;
-    uint64_t blocks = (nunits + wpb - 1) / wpb;
+    uint64_t blocks = (u1 - a.unit_begin + wpb - 1) / wpb;
     if (blocks > (uint64_t)max_blocks) blocks = max_blocks;
-    cudaError_t e = cudaMemsetAsync(a.out, 0, (size_t)a.out_rows * a.stride * sizeof(float), s);
-    if (e != cudaSuccess) return e;
+    if (!a.out_zeroed) {
+        cudaError_t e = cudaMemsetAsync(a.out, 0, (size_t)a.out_rows * a.stride * sizeof(float), s);
+        if (e != cudaSuccess) return e;
+    }
     k_mttkrp_rec<W, BF16, FULL><<<(unsigned)blocks, BLOCK, 0, s>>>(static_cast<const uint4 *>(a.rec), a.fac[0],
                                                                   a.fac[1], a.out, a.nnz, a.stride, a.rank, ul,
-                                                                  nunits);
+                                                                  a.unit_begin, u1);
     sptgb_count_launch(1);
     return cudaGetLastError();
 }
@@ -291,12 +302,37 @@ cudaError_t dispatch_w(const sptgb_mttkrp_args &a, cudaStream_t s) {
 
 }  // namespace
 
+__global__ void k_rec_chunk_bounds(const uint4 *__restrict__ rec, uint64_t n, uint32_t rows, int k,
+                                   uint32_t *__restrict__ out) {
+    const int c = threadIdx.x + 1;
+    if (c >= k) return;
+    const uint32_t r = (uint32_t)((uint64_t)rows * c / k);
+    uint64_t lo = 0, hi = n;   // first position with rec.x >= r
+    while (lo < hi) {
+        const uint64_t mid = (lo + hi) / 2;
+        if (rec[mid].x < r) lo = mid + 1;
+        else hi = mid;
+    }
+    const uint64_t u = lo / SPTGB_REC_UNIT;
+    out[2 * (c - 1)] = (uint32_t)u;
+    out[2 * (c - 1) + 1] = u ? rec[u * SPTGB_REC_UNIT - 1].x : 0u;
+}
+
+extern "C" cudaError_t sptgb_rec_chunk_bounds(const void *rec, uint64_t n, uint32_t rows, int k, uint32_t *out,
+                                              cudaStream_t s) {
+    if (k < 2 || k > 8 || n == 0) return cudaErrorInvalidValue;
+    k_rec_chunk_bounds<<<1, 32, 0, s>>>(static_cast<const uint4 *>(rec), n, rows, k, out);
+    sptgb_count_launch(1);
+    return cudaGetLastError();
+}
+
 extern "C" cudaError_t sptgb_pack_records(const uint32_t *rows, const uint32_t *ia, const uint32_t *ib,
-                                          const float *vals, void *rec, uint64_t n, cudaStream_t s) {
+                                          const float *vals, uint32_t lim_a, uint32_t lim_b, unsigned int *bad,
+                                          void *rec, uint64_t n, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     uint64_t g = (n + 255) / 256;
     if (g > 152ull * 16) g = 152ull * 16;
-    k_pack_records<<<(unsigned)g, 256, 0, s>>>(rows, ia, ib, vals, static_cast<uint4 *>(rec), n);
+    k_pack_records<<<(unsigned)g, 256, 0, s>>>(rows, ia, ib, vals, lim_a, lim_b, bad, static_cast<uint4 *>(rec), n);
     sptgb_count_launch(1);
     return cudaGetLastError();
 }

@@ -462,6 +462,14 @@ extern "C" cudaError_t sptgb_iota_u32(uint32_t *p, uint64_t n, uint32_t start, c
     return cudaGetLastError();
 }
 
+extern "C" cudaError_t sptgb_gather_records(const void *src, const uint32_t *perm, void *dst, uint64_t n,
+                                            cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_gather<uint4><<<grid_for(n, 256), 256, 0, s>>>(static_cast<const uint4 *>(src), perm, static_cast<uint4 *>(dst), n);
+    sptgb_count_launch(1);
+    return cudaGetLastError();
+}
+
 extern "C" cudaError_t sptgb_gather_u32(const uint32_t *in, const uint32_t *perm, uint32_t *out, uint64_t n,
                                         cudaStream_t s) {
     if (n == 0) return cudaSuccess;

@@ -18,6 +18,7 @@ static pthread_once_t g_once = PTHREAD_ONCE_INIT;
 static int g_init_err = 0;
 static int g_device = 0;
 static cudaStream_t g_stream = NULL;
+static cudaStream_t g_copy_stream = NULL;   /* host-buffer uploads that overlap device work on g_stream */
 static _Atomic uint64_t g_launches = 0;
 static uint64_t g_seed = 0x5eed5eedULL;
 static int g_quiet = -1;
@@ -85,6 +86,7 @@ static void ctx_init_once(void) {
     if (s) g_seed = strtoull(s, NULL, 0);
     cudaError_t e = cudaSetDevice(g_device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g_copy_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) g_init_err = sptgb_cuda_fail(e, "SpTns GPU init", __FILE__, __LINE__);
 }
 
@@ -101,6 +103,7 @@ int sptgb_ctx(void) {
 }
 
 cudaStream_t sptgb_stream(void) { return g_stream; }
+cudaStream_t sptgb_copy_stream(void) { return g_copy_stream; }
 
 void sptgb_count_launch(unsigned n) { atomic_fetch_add(&g_launches, (uint64_t)n); }
 

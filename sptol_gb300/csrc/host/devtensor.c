@@ -20,6 +20,19 @@ sptgb_workspace g_ws = {PTHREAD_MUTEX_INITIALIZER};
 void sptgb_lock(void) { pthread_mutex_lock(&g_ws.lock); }
 void sptgb_unlock(void) { pthread_mutex_unlock(&g_ws.lock); }
 
+int sptgb_ws_sync_objects(void) {
+    if (!g_ws.hflag) {
+        void *h = NULL;
+        SPTGB_CUDA(cudaMallocHost(&h, 16 * sizeof(unsigned int)), "SpTns GPU alloc");
+        g_ws.hflag = (unsigned int *)h;
+    }
+    for (int i = 0; i < 4; ++i)
+        if (!g_ws.ev[i]) SPTGB_CUDA(cudaEventCreateWithFlags(&g_ws.ev[i], cudaEventDisableTiming), "SpTns GPU init");
+    for (int i = 0; i < 8; ++i)
+        if (!g_ws.cev[i]) SPTGB_CUDA(cudaEventCreateWithFlags(&g_ws.cev[i], cudaEventDisableTiming), "SpTns GPU init");
+    return 0;
+}
+
 int sptgb_bitwidth(uint64_t x) {
     int b = 0;
     while (x) {
@@ -378,7 +391,7 @@ int sptgbCooPrepareMode(sptgbCoo *t, sptIndex mode, void *stream) {
         cudaError_t e = cudaMalloc(&t->mrec[mode], (n ? n : 1) * 16);
         if (e == cudaSuccess)
             e = sptgb_pack_records(t->minds[mode][mode], t->minds[mode][a], t->minds[mode][b], t->mvals[mode],
-                                   t->mrec[mode], n, s);
+                                   0xffffffffu, 0xffffffffu, NULL, t->mrec[mode], n, s);
         if (e != cudaSuccess) r = sptgb_cuda_fail(e, "GPU COO prepare", __FILE__, __LINE__);
         t->bytes += (size_t)n * 16;
     }

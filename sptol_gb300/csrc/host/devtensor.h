@@ -16,10 +16,16 @@ typedef struct {
     sptgb_dbuf keys[2], perm[2], rtmp;
     sptgb_dbuf fac[SPTGB_MAX_MODES], out;
     sptgb_dbuf flag, misc[8];
+    unsigned int *hflag;            /* pinned, 16 words: flags and row numbers read back without
+                                       blocking the host */
+    cudaEvent_t ev[4];              /* ordering between the compute and the copy stream */
+    cudaEvent_t cev[8];             /* one per output chunk of a host-buffer MTTKRP */
 } sptgb_workspace;
 extern sptgb_workspace g_ws;
 
 void sptgb_lock(void);
+/* Pinned flag words and the two events above, created on first use (lock held). */
+int  sptgb_ws_sync_objects(void);
 void sptgb_unlock(void);
 int  sptgb_quiet(void);
 int  sptgb_bitwidth(uint64_t x);

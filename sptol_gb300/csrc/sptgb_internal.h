@@ -22,6 +22,7 @@ extern "C" {
 /* ----------------------------------------------------------- context -- */
 int          sptgb_ctx(void);            /* lazy init; returns SptError code */
 cudaStream_t sptgb_stream(void);
+cudaStream_t sptgb_copy_stream(void);
 void         sptgb_count_launch(unsigned n);
 
 /* Records the error in the thread-local last-error slot and prints it like
@@ -84,11 +85,30 @@ typedef struct {
     int             bf16;                      /* factors stored as bf16 */
     const void     *rec;                       /* order 3: [nnz] 16-byte records {row, idx[0], idx[1], value}
                                                   (sptgb_pack_records); used instead of rows/idx/vals */
+    /* Order 3 only: run units [unit_begin, unit_end) of SPTGB_REC_UNIT
+     * nonzeros (unit_end 0 = all) into an output that is already zero when
+     * out_zeroed.  Ranges launched one after another on one stream give the
+     * same result as one launch; rows below the first row of a later range
+     * are final once the earlier ranges are done. */
+    uint64_t        unit_begin, unit_end;
+    int             out_zeroed;
 } sptgb_mttkrp_args;
+#define SPTGB_REC_UNIT 256u
+/* Row-quantile split of sorted records into k ranges (1 < k <= 8): for
+ * c = 1..k-1, out[2(c-1)] = the unit holding the first record whose row is
+ * >= c*rows/k (rounded down to a unit boundary) and out[2(c-1)+1] = the row
+ * of the record just before that unit (0 when the unit is 0). */
+cudaError_t sptgb_rec_chunk_bounds(const void *rec, uint64_t n, uint32_t rows, int k, uint32_t *out, cudaStream_t s);
 cudaError_t sptgb_mttkrp_coo(const sptgb_mttkrp_args *a, cudaStream_t s);
-/* rec[i] = {rows[i], ia[i], ib[i], bits of vals[i]} for the order-3 kernel. */
+/* rec[i] = {rows[i], ia[i], ib[i], bits of vals[i]} for the order-3 kernel.
+ * An ia / ib coordinate at or above lim_a / lim_b is replaced by 0 and, when
+ * `bad` is given, sets *bad = 1 (so the product kernel only sees rows that
+ * exist; the caller reports the error). */
 cudaError_t sptgb_pack_records(const uint32_t *rows, const uint32_t *ia, const uint32_t *ib, const float *vals,
-                               void *rec, uint64_t n, cudaStream_t s);
+                               uint32_t lim_a, uint32_t lim_b, unsigned int *bad, void *rec, uint64_t n,
+                               cudaStream_t s);
+/* dst[i] = src[perm[i]] for 16-byte records. */
+cudaError_t sptgb_gather_records(const void *src, const uint32_t *perm, void *dst, uint64_t n, cudaStream_t s);
 
 /* ---------------------------------------------------- HiCOO pieces -- */
 /* flags[i] = 1 when nonzero i starts a new group (coordinates >> bits differ

@@ -106,6 +106,52 @@ def test_out_of_range_coordinate_is_rejected():
     assert e.value.code == 3
 
 
+@pytest.mark.parametrize("N", [3, 4])
+@pytest.mark.parametrize("entry", ["sptMTTKRP", "sptCudaMTTKRP"])
+def test_out_of_range_in_every_mode_then_a_valid_call(N, entry):
+    """A coordinate at its mode size, in the output mode or in a multiplied
+    mode, sorted or not, fails the call; the next valid call is exact."""
+    rng = np.random.default_rng(40 + N)
+    ndims = [300, 200, 100, 50][:N]
+    nnz = 5000
+    inds = np.stack([rng.integers(0, d, nnz) for d in ndims]).astype(np.uint32)
+    vals = rng.uniform(-1, 1, nnz).astype(np.float32)
+    facs = [rng.uniform(-1, 1, (d, 8)).astype(np.float32) for d in ndims]
+    mats = [S.Matrix.from_array(f) for f in facs] + [S.Matrix(max(ndims), 8)]
+    for bad_mode in range(N):
+        for where in (0, nnz // 2, nnz - 1):
+            bad = inds.copy()
+            bad[bad_mode, where] = ndims[bad_mode]
+            t = S.Tensor.from_arrays(ndims, bad, vals)
+            for mode in range(N):
+                with pytest.raises(S.SptError) as e:
+                    S.mttkrp(t, mats, mode, entry=entry)
+                assert e.value.code == 3, (bad_mode, where, mode)
+    t = S.Tensor.from_arrays(ndims, inds, vals)
+    for mode in range(N):
+        out = S.mttkrp(t, mats, mode, entry=entry)
+        assert rel_fro(out, O.mttkrp(ndims, inds, vals, facs, 8, mode)) <= TOL
+
+
+def test_unsorted_order3_records_through_the_permutation():
+    """Order 3, nonzeros in random order: the sort overlaps the uploads and
+    whole records are gathered through the permutation; every mode and a
+    non-default mats_order match the oracle."""
+    g = golden("mttkrp_3d_r16")
+    ndims = [int(x) for x in g["ndims"]]
+    rank = int(g["rank"])
+    p = np.random.default_rng(6).permutation(g["vals"].shape[0])
+    inds, vals = g["inds"][:, p], g["vals"][p]
+    t = S.Tensor.from_arrays(ndims, inds, vals)
+    mats = _with_out(_mats(g, 3, rank), ndims, rank)
+    facs = [g["mat%d" % m] for m in range(3)]
+    for mode in range(3):
+        for order in ([mode] + [m for m in (0, 1, 2) if m != mode], [mode] + [m for m in (2, 1, 0) if m != mode]):
+            out = S.mttkrp(t, mats, mode, mats_order=order, entry="sptCudaMTTKRP")
+            ref = O.mttkrp(ndims, inds, vals, facs, rank, mode, order=order)
+            assert rel_fro(out, ref) <= TOL
+
+
 def _c1_tensor():
     spec = S.GenSpec()
     spec.seed = 0
@@ -192,3 +238,30 @@ def test_orders_2_5_6_8_against_fp64(ndims, entry):
         out = S.mttkrp(t, mats, mode, mats_order=order, entry=entry)
         ref = O.mttkrp(ndims, inds, vals, facs, rank, mode, order=order, precision="f64")
         assert rel_fro(out, ref) <= TOL, (ndims, mode)
+
+
+@pytest.mark.parametrize("shuffled", [False, True])
+def test_chunked_result_copy_with_a_row_across_chunks(shuffled):
+    """Order 3, >= 4M nonzeros through the host-buffer entry: the kernel runs
+    in unit ranges and finished rows are copied back while later ranges run.
+    One row holds ~30% of the nonzeros, so it crosses range boundaries;
+    every mode against the FP64 oracle."""
+    rng = np.random.default_rng(77)
+    n = 4_500_000
+    ndims = [3000, 2500, 400]
+    r0 = rng.integers(0, ndims[0], n)
+    r0[rng.random(n) < 0.3] = 1500
+    inds = np.stack([r0, rng.integers(0, ndims[1], n), rng.integers(0, ndims[2], n)]).astype(np.uint32)
+    order = np.lexsort(inds[::-1])
+    if shuffled:
+        order = rng.permutation(n)
+    inds = np.ascontiguousarray(inds[:, order])
+    vals = rng.uniform(-1, 1, n).astype(np.float32)
+    rank = 16
+    facs = [rng.uniform(-1, 1, (d, rank)).astype(np.float32) for d in ndims]
+    t = S.Tensor.from_arrays(ndims, inds, vals)
+    mats = [S.Matrix.from_array(f) for f in facs] + [S.Matrix(max(ndims), rank)]
+    for mode in range(3):
+        out = S.mttkrp(t, mats, mode, entry="sptCudaMTTKRP")
+        ref = O.mttkrp(ndims, inds, vals, facs, rank, mode, precision="f64_omp")
+        assert rel_fro(out, ref) <= TOL, mode
