@@ -219,10 +219,280 @@ __global__ void __launch_bounds__(BLOCK) k_hicoo_win(sptgb_hicoo_args a, uint32_
     }
 }
 
+// Order 3 (k_hicoo_win2).  Same schedule and equal-nonzero CTA ranges as
+// k_hicoo_win, with two changes.
+//  * Decoding: each worker owns a contiguous share of its positions, and its
+//    W lanes decode W consecutive schedule positions together: they load the
+//    next W block boundaries (pnnz) at once and each lane finds its block
+//    with a log2(W)-step search over them through shuffles (exact with empty
+//    blocks), so the block and element loads of the 32 positions of a warp
+//    are in flight together instead of one dependent chain per element.  The
+//    decoded records {row, row of factor a, row of factor b, value} go through
+//    shared memory to the worker, which issues the factor-row gathers of a
+//    batch of them before using any.
+//  * Windows: only heavy windows (at least SPTGB_HICOO_HEAVY nonzeros, the
+//    hot rows of a power-law mode) are summed in the shared-memory tile and
+//    written once.  A run of consecutive light windows is one flat range: the
+//    running row sum of a worker goes to the output with a vector atomic when
+//    the row changes, with no per-window barrier or tile write, so the many
+//    small windows of a long tail cost no more than their nonzeros.
+struct Win2Ctx {
+    const uint8_t *e_m, *e_a, *e_b;
+    const uint32_t *b_m, *b_a, *b_b;
+    const char *Fa, *Fb;
+    size_t rb;
+    uint32_t lim_a, lim_b, rows_w, st;
+    int sl, wk, c0;
+    bool col_ok, m0, m1, m2, m3;
+};
+
+// One worker's positions [r_beg, r_end) of the blocks [klo, khi) of the
+// schedule.  TILE: rows are window rows (row0 + r) summed in `tile`;
+// otherwise output rows, flushed with vector atomics.
+template <int W, bool TILE>
+__device__ __forceinline__ void win2_range(const sptgb_hicoo_args &a, const Win2Ctx &x, uint4 *s_rec, float *tile,
+                                           uint32_t row0, uint64_t klo, uint64_t khi, uint32_t r_beg,
+                                           uint32_t r_end) {
+    constexpr int EB = W < 4 ? W : 4;   // records per gather batch
+    uint32_t cur = NONE;
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    auto put = [&]() {
+        if (cur == NONE || !x.col_ok) return;
+        if (TILE) {
+            float *t = tile + cur * x.st + x.c0;
+            if (x.m0) atomicAdd(t + 0, acc.x);
+            if (x.m1) atomicAdd(t + 1, acc.y);
+            if (x.m2) atomicAdd(t + 2, acc.z);
+            if (x.m3) atomicAdd(t + 3, acc.w);
+        } else {
+            const float4 v = make_float4(x.m0 ? acc.x : 0.f, x.m1 ? acc.y : 0.f, x.m2 ? acc.z : 0.f,
+                                         x.m3 ? acc.w : 0.f);
+            atomicAdd(reinterpret_cast<float4 *>(a.out + (size_t)cur * x.st) + x.sl, v);
+        }
+    };
+    uint64_t kb = klo;
+    uint32_t kst = 0;
+    if (r_beg < r_end) {
+        kb = block_at(a.pnnz, klo, khi, r_beg);
+        kst = a.pnnz[kb];
+    }
+    const uint32_t rounds = __reduce_max_sync(0xffffffffu, (r_end - r_beg + W - 1) / W);
+    for (uint32_t it = 0; it < rounds; ++it) {
+        const uint32_t p = r_beg + it * W + x.sl;
+        const bool valid = p < r_end;
+        // lane's block: kb + (boundaries pnnz[kb+1 ..] <= p), searched over
+        // the W boundaries the worker's lanes load; boundaries past khi read
+        // as 0xffffffff, so the loop ends after at most (khi - kb) / W + 1
+        // rounds (more than one only when blocks are empty)
+        uint64_t myk = kb;
+        uint32_t mystart = kst;
+        bool todo = valid;
+        uint64_t base = kb;
+        uint32_t bstart = kst;
+        for (uint32_t guard = 0; guard < (1u << 26) && __any_sync(0xffffffffu, todo); ++guard) {
+            const uint64_t idx = base + 1 + x.sl;
+            const uint32_t bv = idx <= khi ? a.pnnz[idx] : 0xffffffffu;
+            uint32_t c = 0;
+#pragma unroll
+            for (int step = W / 2; step >= 1; step >>= 1) {
+                const uint32_t t = __shfl_sync(0xffffffffu, bv, (int)(c + step - 1), W);
+                if (todo && t <= p) c += step;
+            }
+            const uint32_t last = __shfl_sync(0xffffffffu, bv, W - 1, W);
+            if (todo && c == W - 1 && last <= p) c = W;   // all W boundaries passed
+            const uint32_t prev = __shfl_sync(0xffffffffu, bv, (int)(c > 0 ? c - 1 : 0), W);
+            if (todo && c < W) {
+                myk = base + c;
+                mystart = c ? prev : bstart;
+                todo = false;
+            }
+            bstart = last;
+            base += W;
+        }
+        uint4 r = make_uint4(NONE, 0u, 0u, 0u);
+        if (valid && !todo) {
+            const uint32_t b = a.perm[myk];
+            const uint64_t e = a.bptr[b] + (p - mystart);
+            bool ok = e < a.nnz;
+            if (ok) {
+                const uint32_t rl = x.e_m[e];
+                const uint32_t row = TILE ? rl : (x.b_m[b] << a.sb_bits) + rl;
+                const uint32_t ra = (x.b_a[b] << a.sb_bits) + x.e_a[e];
+                const uint32_t rr = (x.b_b[b] << a.sb_bits) + x.e_b[e];
+                ok = rl < x.rows_w && (TILE ? row0 + rl : row) < a.out_rows && ra < x.lim_a && rr < x.lim_b;
+                if (ok) r = make_uint4(row, ra, rr, __float_as_uint(a.vals[e]));
+            }
+            if (!ok) atomicOr(a.err, 1u);
+        } else if (valid) {
+            atomicOr(a.err, 1u);
+        }
+        // the next round of this worker starts in its last lane's block
+        kb = __shfl_sync(0xffffffffu, myk, W - 1, W);
+        kst = __shfl_sync(0xffffffffu, mystart, W - 1, W);
+        s_rec[threadIdx.x & 31] = r;
+        __syncwarp();
+#pragma unroll
+        for (int j0 = 0; j0 < W; j0 += EB) {
+            uint4 q4[EB];
+            float4 fa[EB], fb[EB];
+#pragma unroll
+            for (int t = 0; t < EB; ++t) q4[t] = s_rec[x.wk * W + j0 + t];
+#pragma unroll
+            for (int t = 0; t < EB; ++t) {
+                const bool use = q4[t].x != NONE && x.col_ok;
+                fa[t] = use ? __ldg(reinterpret_cast<const float4 *>(x.Fa + (size_t)q4[t].y * x.rb))
+                            : make_float4(0.f, 0.f, 0.f, 0.f);
+                fb[t] = use ? __ldg(reinterpret_cast<const float4 *>(x.Fb + (size_t)q4[t].z * x.rb))
+                            : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+#pragma unroll
+            for (int t = 0; t < EB; ++t) {
+                if (q4[t].x == NONE) continue;
+                if (q4[t].x != cur) {
+                    put();
+                    cur = q4[t].x;
+                    acc = make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+                const float v = __uint_as_float(q4[t].w);
+                acc.x += v * fa[t].x * fb[t].x;
+                acc.y += v * fa[t].y * fb[t].y;
+                acc.z += v * fa[t].z * fb[t].z;
+                acc.w += v * fa[t].w * fb[t].w;
+            }
+        }
+        __syncwarp();
+    }
+    put();
+}
+
+template <int W>
+__global__ void __launch_bounds__(BLOCK, 3) k_hicoo_win2(sptgb_hicoo_args a, uint32_t chunk, uint32_t total) {
+    extern __shared__ float tile[];   // [1 << sb][stride]
+    constexpr int NWARP = BLOCK / 32;
+    constexpr int NWK = 32 / W;              // workers per warp
+    constexpr uint32_t NWC = BLOCK / W;      // workers per CTA
+    __shared__ uint4 s_rec[NWARP][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    Win2Ctx x;
+    x.sl = lane % W;
+    x.wk = lane / W;
+    x.rows_w = 1u << a.sb_bits;
+    x.st = a.stride;
+    x.col_ok = (uint32_t)(x.sl * 4) < x.st;
+    x.c0 = x.sl * 4;
+    x.m0 = x.c0 + 0 < (int)a.rank;
+    x.m1 = x.c0 + 1 < (int)a.rank;
+    x.m2 = x.c0 + 2 < (int)a.rank;
+    x.m3 = x.c0 + 3 < (int)a.rank;
+    const uint32_t mode = a.mode, pa = a.order[1], pb = a.order[2];
+    x.e_m = a.einds[mode];
+    x.e_a = a.einds[pa];
+    x.e_b = a.einds[pb];
+    x.b_m = a.binds[mode];
+    x.b_a = a.binds[pa];
+    x.b_b = a.binds[pb];
+    x.lim_a = a.ndims[pa];
+    x.lim_b = a.ndims[pb];
+    x.Fa = reinterpret_cast<const char *>(a.fac[pa]) + (size_t)x.sl * 16;
+    x.Fb = reinterpret_cast<const char *>(a.fac[pb]) + (size_t)x.sl * 16;
+    x.rb = (size_t)x.st * 4;
+    const uint32_t st4 = x.st / 4;
+    const uint32_t gw = (uint32_t)(warp * NWK + x.wk);
+
+    const uint64_t lo64 = (uint64_t)blockIdx.x * chunk;
+    if (lo64 >= total) return;
+    const uint32_t lo = (uint32_t)lo64, hi = (uint32_t)min((uint64_t)total, lo64 + chunk);
+    for (uint32_t i = threadIdx.x; i < x.rows_w * x.st; i += BLOCK) tile[i] = 0.f;
+    uint32_t wlo = 0, whi = a.nwin;   // first window: last w with pnnz[wst[w]] <= lo
+    while (whi - wlo > 1) {
+        const uint32_t mid = (wlo + whi) >> 1;
+        if (a.pnnz[a.wst[mid]] <= lo) wlo = mid;
+        else whi = mid;
+    }
+    uint32_t w = wlo;
+    uint32_t q = lo;
+    __syncthreads();
+    while (q < hi) {
+        const uint64_t k0 = a.wst[w], k1 = a.wst[w + 1];
+        const uint32_t wbeg = a.pnnz[k0], wend = a.pnnz[k1];
+        if (wend - wbeg < SPTGB_HICOO_HEAVY) {
+            // a run of light windows, up to the next heavy one
+            uint32_t hl = 0, hh = a.nheavy;   // first heavy window > w
+            while (hl < hh) {
+                const uint32_t mid = (hl + hh) >> 1;
+                if (a.heavy[mid] <= w) hl = mid + 1;
+                else hh = mid;
+            }
+            const uint32_t wh = hl < a.nheavy ? (uint32_t)a.heavy[hl] : a.nwin;
+            const uint64_t kend = a.wst[wh];
+            const uint32_t rend = a.pnnz[kend];
+            const uint32_t s0 = q, s1 = hi < rend ? hi : rend;
+            const uint32_t per = (s1 - s0 + NWC - 1) / NWC;
+            const uint32_t r_beg = s0 + min(s1 - s0, gw * per);
+            win2_range<W, false>(a, x, s_rec[warp], tile, 0u, k0, kend, r_beg, min(s1, r_beg + per));
+            q = s1;
+            w = wh;
+            continue;
+        }
+        const uint32_t s0 = q > wbeg ? q : wbeg, s1 = hi < wend ? hi : wend;
+        const uint32_t row0 = a.binds[mode][a.perm[k0]] << a.sb_bits;
+        const uint32_t per = (s1 - s0 + NWC - 1) / NWC;
+        const uint32_t r_beg = s0 + min(s1 - s0, gw * per);
+        win2_range<W, true>(a, x, s_rec[warp], tile, row0, k0, k1, r_beg, min(s1, r_beg + per));
+        __syncthreads();
+        // one write of the window: plain when this CTA covered all of it
+        const bool owned = s0 == wbeg && s1 == wend;
+        float4 *t4 = reinterpret_cast<float4 *>(tile);
+        for (uint32_t i = threadIdx.x; i < x.rows_w * st4; i += BLOCK) {
+            const uint32_t r = i / st4, c = i % st4;
+            const float4 v = t4[i];
+            t4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (row0 + r >= a.out_rows) continue;
+            float4 *o = reinterpret_cast<float4 *>(a.out + (size_t)(row0 + r) * x.st) + c;
+            if (owned) *o = v;
+            else if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f) atomicAdd(o, v);
+        }
+        __syncthreads();
+        q = s1;
+        ++w;
+    }
+}
+
+// flags[w] = 1 when output window w holds at least `heavy` nonzeros.
+__global__ void k_window_heavy(const uint64_t *__restrict__ wst, const uint32_t *__restrict__ pnnz, uint32_t nwin,
+                               uint32_t heavy, uint32_t *__restrict__ flags) {
+    for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < nwin; w += gridDim.x * blockDim.x)
+        flags[w] = pnnz[wst[w + 1]] - pnnz[wst[w]] >= heavy;
+}
+
 __global__ void k_block_sizes(const uint32_t *__restrict__ perm, const uint64_t *__restrict__ bptr, uint64_t nb,
                               uint32_t *__restrict__ sizes) {
     for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < nb; k += (uint64_t)gridDim.x * blockDim.x)
         sizes[k] = (uint32_t)(bptr[perm[k] + 1] - bptr[perm[k]]);
+}
+
+template <int W>
+cudaError_t launch_win2(const sptgb_hicoo_args &a, cudaStream_t s) {
+    static int nsm = 0;
+    const size_t smem = ((size_t)1 << a.sb_bits) * a.stride * sizeof(float);
+    if (smem > 180 * 1024) return cudaErrorInvalidValue;
+    if (nsm == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaFuncSetAttribute(k_hicoo_win2<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, 180 * 1024);
+    }
+    int per = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_hicoo_win2<W>, BLOCK, smem);
+    if (per < 1) per = 1;
+    if (a.nnz == 0 || a.nnz >= 0xffffffffull) return a.nnz ? cudaErrorInvalidValue : cudaSuccess;
+    const uint32_t total = (uint32_t)a.nnz;
+    const uint64_t grid = (uint64_t)nsm * per * 2;
+    const uint32_t chunk = (uint32_t)((total + grid - 1) / grid);
+    const uint32_t ngrid = (total + chunk - 1) / chunk;
+    k_hicoo_win2<W><<<ngrid, BLOCK, smem, s>>>(a, chunk, total);
+    sptgb_count_launch(1);
+    return cudaGetLastError();
 }
 
 template <int W, int NP>
@@ -293,11 +563,11 @@ extern "C" cudaError_t sptgb_mttkrp_hicoo(const sptgb_hicoo_args *a, cudaStream_
     const uint32_t c4 = a->stride / 4;
     if (a->perm && (a->nmodes == 3 || a->nmodes == 4)) {
         if (a->nmodes == 3) {
-            if (c4 <= 2) return launch_win<2, 2>(*a, s);
-            if (c4 <= 4) return launch_win<4, 2>(*a, s);
-            if (c4 <= 8) return launch_win<8, 2>(*a, s);
-            if (c4 <= 16) return launch_win<16, 2>(*a, s);
-            return launch_win<32, 2>(*a, s);
+            if (c4 <= 2) return launch_win2<2>(*a, s);
+            if (c4 <= 4) return launch_win2<4>(*a, s);
+            if (c4 <= 8) return launch_win2<8>(*a, s);
+            if (c4 <= 16) return launch_win2<16>(*a, s);
+            return launch_win2<32>(*a, s);
         }
         if (c4 <= 2) return launch_win<2, 3>(*a, s);
         if (c4 <= 4) return launch_win<4, 3>(*a, s);
@@ -314,8 +584,10 @@ extern "C" cudaError_t sptgb_mttkrp_hicoo(const sptgb_hicoo_args *a, cudaStream_
 
 extern "C" cudaError_t sptgb_hicoo_schedule(const uint32_t *binds_mode, const uint64_t *bptr, uint64_t nb,
                                             int window_bits, const sptgb_hicoo_sched_scratch *w, uint32_t *perm,
-                                            uint32_t *pnnz, uint64_t *wst, uint32_t *nwin_out, cudaStream_t s) {
+                                            uint32_t *pnnz, uint64_t *wst, uint32_t *nwin_out, uint64_t *heavy,
+                                            uint32_t *nheavy_out, cudaStream_t s) {
     *nwin_out = 0;
+    *nheavy_out = 0;
     if (nb == 0) return cudaMemsetAsync(pnnz, 0, sizeof(uint32_t), s);
     cudaError_t e = cudaMemcpyAsync(w->keys[0], binds_mode, nb * 4, cudaMemcpyDeviceToDevice, s);
     if (e == cudaSuccess) e = sptgb_iota_u32(w->vals[0], nb, 0, s);
@@ -344,7 +616,20 @@ extern "C" cudaError_t sptgb_hicoo_schedule(const uint32_t *binds_mode, const ui
     const uint64_t end = nb;
     e = cudaMemcpyAsync(wst + nwin, &end, sizeof end, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return e;
     *nwin_out = nwin;
+    // the heavy windows, ascending
+    uint64_t gw = (nwin + 255) / 256;
+    if (gw > 152 * 16) gw = 152 * 16;
+    k_window_heavy<<<(unsigned)gw, 256, 0, s>>>(wst, pnnz, nwin, SPTGB_HICOO_HEAVY, w->flags);
+    sptgb_count_launch(1);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = sptgb_exclusive_scan_u32(w->flags, w->pos, nwin, dn, w->stmp, s);
+    if (e == cudaSuccess) e = sptgb_compact_starts(w->flags, w->pos, nwin, heavy, s);
+    uint32_t nh = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&nh, dn, sizeof nh, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) *nheavy_out = nh;
     return e;
 }
 

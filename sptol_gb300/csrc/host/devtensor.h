@@ -74,8 +74,8 @@ struct sptgbHicoo {
     float *vals;
     /* output-window schedule per mode (orders 3 and 4) */
     uint32_t *perm[SPTGB_MAX_MODES], *pnnz[SPTGB_MAX_MODES];
-    uint64_t *wst[SPTGB_MAX_MODES];
-    uint32_t nwin[SPTGB_MAX_MODES];
+    uint64_t *wst[SPTGB_MAX_MODES];    /* [nb+1] window starts, then [nb] heavy window ids */
+    uint32_t nwin[SPTGB_MAX_MODES], nheavy[SPTGB_MAX_MODES];
     int ready[SPTGB_MAX_MODES];
     unsigned int *err;
     size_t bytes;

@@ -359,7 +359,7 @@ static int hicoo_mttkrp(sptSparseTensorHiCOO const *h, sptMatrix *mats[], sptInd
         H(sptgb_dbuf_reserve(&g_ws.rtmp, sptgb_radix_tmp_bytes(nb)));
         H(sptgb_dbuf_reserve(&g_ws.misc[2], (2 * nb + 1) * 4));
         H(sptgb_dbuf_reserve(&g_ws.misc[3], (2 * nb + 1) * 4));
-        H(sptgb_dbuf_reserve(&g_ws.misc[4], (nb + 1) * 8));
+        H(sptgb_dbuf_reserve(&g_ws.misc[4], (2 * nb + 1) * 8));
         H(sptgb_dbuf_reserve(&g_ws.misc[5], sptgb_scan_tmp_bytes(nb)));
         w.rtmp = g_ws.rtmp.ptr;
         w.stmp = g_ws.misc[5].ptr;
@@ -367,13 +367,16 @@ static int hicoo_mttkrp(sptSparseTensorHiCOO const *h, sptMatrix *mats[], sptInd
         w.pos = w.flags + nb;
         uint32_t *perm = (uint32_t *)g_ws.misc[3].ptr, *pnnz = perm + nb;
         const uint32_t maxb = h->ndims[mode] ? (h->ndims[mode] - 1) >> h->sb_bits : 0;
-        uint32_t nwin = 0;
-        C(sptgb_hicoo_schedule(a.binds[mode], a.bptr, nb, sptgb_bitwidth(maxb), &w, perm, pnnz,
-                               (uint64_t *)g_ws.misc[4].ptr, &nwin, s));
+        uint32_t nwin = 0, nheavy = 0;
+        uint64_t *wst = (uint64_t *)g_ws.misc[4].ptr;
+        C(sptgb_hicoo_schedule(a.binds[mode], a.bptr, nb, sptgb_bitwidth(maxb), &w, perm, pnnz, wst, &nwin,
+                               wst + nb + 1, &nheavy, s));
         a.perm = perm;
         a.pnnz = pnnz;
-        a.wst = (const uint64_t *)g_ws.misc[4].ptr;
+        a.wst = wst;
         a.nwin = nwin;
+        a.heavy = wst + nb + 1;
+        a.nheavy = nheavy;
     }
     C(cudaMemsetAsync(a.err, 0, sizeof(unsigned int), s));
     if (g_hicoo_timing) C(cudaEventRecord(g_hicoo_ev[0], s));
@@ -507,10 +510,10 @@ int sptgbHicooPrepareMode(sptgbHicoo *t, sptIndex mode, void *stream) {
     const cudaStream_t s = stream ? (cudaStream_t)stream : 0;
     const uint64_t nb = t->nb;
     cudaError_t e = cudaMalloc((void **)&t->perm[mode], (2 * nb + 1) * 4);
-    if (e == cudaSuccess) e = cudaMalloc((void **)&t->wst[mode], (nb + 1) * 8);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&t->wst[mode], (2 * nb + 1) * 8);
     if (e != cudaSuccess) return sptgb_cuda_fail(e, module, __FILE__, __LINE__);
     t->pnnz[mode] = t->perm[mode] + nb;
-    t->bytes += (2 * nb + 1) * 4 + (nb + 1) * 8;
+    t->bytes += (2 * nb + 1) * 4 + (2 * nb + 1) * 8;
     int r = 0;
     sptgb_lock();
     sptgb_hicoo_sched_scratch w;
@@ -530,7 +533,7 @@ int sptgbHicooPrepareMode(sptgbHicoo *t, sptIndex mode, void *stream) {
         w.pos = w.flags + nb;
         const uint32_t maxb = t->ndims[mode] ? (t->ndims[mode] - 1) >> t->sb_bits : 0;
         e = sptgb_hicoo_schedule(t->binds[mode], t->bptr, nb, sptgb_bitwidth(maxb), &w, t->perm[mode], t->pnnz[mode],
-                                 t->wst[mode], &t->nwin[mode], s);
+                                 t->wst[mode], &t->nwin[mode], t->wst[mode] + nb + 1, &t->nheavy[mode], s);
         if (e != cudaSuccess) r = sptgb_cuda_fail(e, module, __FILE__, __LINE__);
     }
     sptgb_unlock();
@@ -573,6 +576,8 @@ int sptgbHicooMTTKRP(sptgbHicoo *t, sptIndex mode, const sptIndex *mats_order, c
         a.pnnz = t->pnnz[mode];
         a.wst = t->wst[mode];
         a.nwin = t->nwin[mode];
+        a.heavy = t->wst[mode] + t->nb + 1;
+        a.nheavy = t->nheavy[mode];
     }
     SPTGB_CUDA(sptgb_mttkrp_hicoo(&a, s), module);
     return 0;

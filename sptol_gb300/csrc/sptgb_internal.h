@@ -160,6 +160,9 @@ typedef struct {
     const uint32_t *pnnz;                      /* [nb+1] exclusive prefix of block sizes in that order */
     const uint64_t *wst;                       /* [nwin+1] first position of each output window; wst[nwin] = nb */
     uint32_t        nwin;
+    const uint64_t *heavy;                     /* [nheavy] ascending ids of the windows holding at least
+                                                  SPTGB_HICOO_HEAVY nonzeros (order 3) */
+    uint32_t        nheavy;
     uint64_t        nnz;                       /* = bptr[nb]; below 2^32 for the window kernel */
 } sptgb_hicoo_args;
 cudaError_t sptgb_mttkrp_hicoo(const sptgb_hicoo_args *a, cudaStream_t s);
@@ -168,16 +171,19 @@ cudaError_t sptgb_mttkrp_hicoo(const sptgb_hicoo_args *a, cudaStream_t s);
 cudaError_t sptgb_hicoo_check(const sptgb_hicoo_args *a, cudaStream_t s);
 /* Output-window schedule of one mode: blocks stably sorted by their block
  * index in `mode` (keys = binds_mode, window_bits significant bits), the
- * prefix of their sizes and the start of each run of equal keys.  Scratch:
- * keys/vals double buffers [nb] each, radix tmp, flags/pos [nb], scan tmp.
- * *nwin_out is read back (the stream is synchronised).  nnz < 2^32. */
+ * prefix of their sizes, the start of each run of equal keys (a window) and
+ * the ascending list of windows with at least SPTGB_HICOO_HEAVY nonzeros
+ * (heavy, [nb] capacity).  Scratch: keys/vals double buffers [nb] each, radix
+ * tmp, flags/pos [nb], scan tmp.  *nwin_out and *nheavy_out are read back
+ * (the stream is synchronised).  nnz < 2^32. */
+#define SPTGB_HICOO_HEAVY 8192u
 typedef struct {
     uint32_t *keys[2], *vals[2], *flags, *pos;
     void *rtmp, *stmp;
 } sptgb_hicoo_sched_scratch;
 cudaError_t sptgb_hicoo_schedule(const uint32_t *binds_mode, const uint64_t *bptr, uint64_t nb, int window_bits,
                                  const sptgb_hicoo_sched_scratch *w, uint32_t *perm, uint32_t *pnnz, uint64_t *wst,
-                                 uint32_t *nwin_out, cudaStream_t s);
+                                 uint32_t *nwin_out, uint64_t *heavy, uint32_t *nheavy_out, cudaStream_t s);
 
 /* ---------------------------------------------------- dense CP-ALS --
  * FP64 pieces; matrices are row-major with `stride` floats per row. */

@@ -158,3 +158,78 @@ def test_empty_tensor_conversion():
     h = S.HiCOO(t, 2, 3)
     a = h.arrays()
     assert list(a["kptr"]) == [0, 1] and list(a["bptr"]) == [0, 0] and list(a["cptr"]) == [0, 1]
+
+
+def _skewed3(count, seed):
+    spec = S.GenSpec()
+    spec.seed = seed
+    spec.nmodes = 3
+    for m, d in enumerate([900_000, 400_000, 9_000]):
+        spec.ndims[m] = d
+    spec.coord_dist[0] = spec.coord_dist[1] = S.DIST_ZIPF
+    spec.zipf_s[0] = spec.zipf_s[1] = 1.2
+    spec.count = count
+    spec.value_dist = S.VAL_UPM1
+    return S.Tensor.generate(spec)
+
+
+@pytest.mark.parametrize("rank", [5, 16, 32, 64, 128])
+def test_hicoo_window_kernel_3d_every_worker_width(rank):
+    """Order 3 decodes 32 schedule positions per warp; worker widths 2..32
+    lanes (ranks 5..128), power-law output windows split over many CTAs."""
+    t = _skewed3(500_000, 21)
+    ndims = t.ndims
+    h = S.HiCOO(t, 7, 17)
+    i2, v2 = t.arrays()
+    mats = S.new_factors(ndims, rank, seed=9)
+    facs = [m.array()[: ndims[k]].copy() for k, m in enumerate(mats[:3])]
+    for mode in range(3):
+        out = S.mttkrp_hicoo(h, mats, mode)
+        ref = O.mttkrp(ndims, i2, v2, facs, rank, mode, precision="f64")
+        assert rel_fro(out, ref) <= 1e-5, (mode, rel_fro(out, ref))
+
+
+def test_hicoo_empty_blocks_in_a_caller_hicoo():
+    """A caller's HiCOO may hold empty blocks (repeated bptr entries), alone,
+    in a run of 100, inside windows and as windows of their own; the result is
+    that of the same nonzeros without them."""
+    t = _skewed3(200_000, 22)
+    ndims = t.ndims
+    h = S.HiCOO(t, 7, 17)
+    A = h.arrays()
+    i2, v2 = t.arrays()
+    rng = np.random.default_rng(23)
+    bptr = A["bptr"]
+    nb = len(bptr) - 1
+    at = np.sort(np.concatenate([rng.integers(0, nb + 1, 300), np.full(100, nb // 2)]))
+    src = np.minimum(at, nb - 1)
+    nbptr = np.insert(bptr, at, bptr[at]).astype(np.uint64)
+    nbinds = []
+    for m in range(3):
+        fill = A["binds"][m][src].copy()
+        fresh = rng.random(len(at)) < 0.5
+        fill[fresh] = rng.integers(0, (ndims[m] + 127) // 128, int(fresh.sum()))
+        nbinds.append(np.insert(A["binds"][m], at, fill).astype(np.uint32))
+    assert np.array_equal(np.diff(nbptr)[np.diff(nbptr) > 0], np.diff(bptr))
+    s2 = S.HiCOOS()
+    s2.nmodes = h.s.nmodes
+    s2.sortorder = h.s.sortorder
+    s2.ndims = h.s.ndims
+    s2.nnz = h.s.nnz
+    s2.sb_bits, s2.sk_bits, s2.sc_bits = h.s.sb_bits, h.s.sk_bits, h.s.sc_bits
+    s2.bptr = S.NnzIndexVector(len(nbptr), len(nbptr), nbptr.ctypes.data_as(S.u64p))
+    bv = (S.BlockIndexVector * 3)(*[S.BlockIndexVector(len(b), len(b), b.ctypes.data_as(S.u32p)) for b in nbinds])
+    s2.binds = C.cast(bv, C.POINTER(S.BlockIndexVector))
+    s2.einds = h.s.einds
+    s2.values = h.s.values
+    rank = 16
+    mats = S.new_factors(ndims, rank, seed=24)
+    facs = [m.array()[: ndims[k]].copy() for k, m in enumerate(mats[:3])]
+    for mode in range(3):
+        order, op = S._u32([mode] + [(mode + i) % 3 for i in (1, 2)])
+        mats[3].s.nrows = ndims[mode]
+        assert S.lib().sptMTTKRPHiCOO(C.byref(s2), S._mat_array(mats), op, mode) == 0
+        out = mats[3].array()[: ndims[mode], :rank].copy()
+        ref = O.mttkrp(ndims, i2, v2, facs, rank, mode, precision="f64")
+        assert rel_fro(out, ref) <= 1e-5, (mode, rel_fro(out, ref))
+    del bv, nbinds, nbptr
