@@ -244,6 +244,7 @@ struct Win2Ctx {
     uint32_t lim_a, lim_b, rows_w, st;
     int sl, wk, c0;
     bool col_ok, m0, m1, m2, m3;
+    uint32_t mrot;    // column mask m0 | m1 << 1 | m2 << 2 | m3 << 3 rotated right by wk mod 4
 };
 
 // One worker's positions [r_beg, r_end) of the blocks [klo, khi) of the
@@ -253,17 +254,25 @@ template <int W, bool TILE>
 __device__ __forceinline__ void win2_range(const sptgb_hicoo_args &a, const Win2Ctx &x, uint4 *s_rec, float *tile,
                                            uint32_t row0, uint64_t klo, uint64_t khi, uint32_t r_beg,
                                            uint32_t r_end) {
-    constexpr int EB = W < 4 ? W : 4;   // records per gather batch
+    constexpr int EB = 2;   // records per gather batch
     uint32_t cur = NONE;
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     auto put = [&]() {
         if (cur == NONE || !x.col_ok) return;
         if (TILE) {
+            // worker k adds its four columns starting at column k mod 4: at
+            // each step the workers of a warp hit four different bank classes
+            // (no bank conflict for a 32-float row, and no same-address
+            // serialisation when two workers hold the same row)
             float *t = tile + cur * x.st + x.c0;
-            if (x.m0) atomicAdd(t + 0, acc.x);
-            if (x.m1) atomicAdd(t + 1, acc.y);
-            if (x.m2) atomicAdd(t + 2, acc.z);
-            if (x.m3) atomicAdd(t + 3, acc.w);
+            float4 v = acc;   // rotated left by wk mod 4
+            if (x.wk & 1) v = make_float4(v.y, v.z, v.w, v.x);
+            if (x.wk & 2) v = make_float4(v.z, v.w, v.x, v.y);
+            const int r = x.wk & 3;
+            if (x.mrot & 1) atomicAdd(t + (r & 3), v.x);
+            if (x.mrot & 2) atomicAdd(t + ((r + 1) & 3), v.y);
+            if (x.mrot & 4) atomicAdd(t + ((r + 2) & 3), v.z);
+            if (x.mrot & 8) atomicAdd(t + ((r + 3) & 3), v.w);
         } else {
             const float4 v = make_float4(x.m0 ? acc.x : 0.f, x.m1 ? acc.y : 0.f, x.m2 ? acc.z : 0.f,
                                          x.m3 ? acc.w : 0.f);
@@ -366,7 +375,7 @@ __device__ __forceinline__ void win2_range(const sptgb_hicoo_args &a, const Win2
 }
 
 template <int W>
-__global__ void __launch_bounds__(BLOCK, 3) k_hicoo_win2(sptgb_hicoo_args a, uint32_t chunk, uint32_t total) {
+__global__ void __launch_bounds__(BLOCK, 5) k_hicoo_win2(sptgb_hicoo_args a, uint32_t chunk, uint32_t total) {
     extern __shared__ float tile[];   // [1 << sb][stride]
     constexpr int NWARP = BLOCK / 32;
     constexpr int NWK = 32 / W;              // workers per warp
@@ -384,6 +393,11 @@ __global__ void __launch_bounds__(BLOCK, 3) k_hicoo_win2(sptgb_hicoo_args a, uin
     x.m1 = x.c0 + 1 < (int)a.rank;
     x.m2 = x.c0 + 2 < (int)a.rank;
     x.m3 = x.c0 + 3 < (int)a.rank;
+    {
+        const uint32_t mb = (uint32_t)x.m0 | (uint32_t)x.m1 << 1 | (uint32_t)x.m2 << 2 | (uint32_t)x.m3 << 3;
+        const uint32_t r = (uint32_t)x.wk & 3u;
+        x.mrot = ((mb >> r) | (mb << (4 - r))) & 15u;
+    }
     const uint32_t mode = a.mode, pa = a.order[1], pb = a.order[2];
     x.e_m = a.einds[mode];
     x.e_a = a.einds[pa];
