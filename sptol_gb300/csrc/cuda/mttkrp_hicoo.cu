@@ -647,6 +647,26 @@ extern "C" cudaError_t sptgb_hicoo_schedule(const uint32_t *binds_mode, const ui
     return e;
 }
 
+// *bad = 1 unless bptr[0] == 0, bptr[nb] == nnz and bptr is non-decreasing.
+__global__ void k_bptr_check(const uint64_t *__restrict__ bptr, uint64_t nb, uint64_t nnz, unsigned int *bad) {
+    unsigned int b = 0;
+    const uint64_t i0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i0 == 0) b = bptr[0] != 0 || bptr[nb] != nnz;
+    for (uint64_t i = i0; i < nb; i += (uint64_t)gridDim.x * blockDim.x) b |= bptr[i + 1] < bptr[i];
+    if (__any_sync(0xffffffffu, b) && (threadIdx.x & 31) == 0) atomicOr(bad, 1u);
+}
+
+extern "C" cudaError_t sptgb_hicoo_check_bptr(const uint64_t *bptr, uint64_t nb, uint64_t nnz, unsigned int *bad,
+                                              cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(bad, 0, sizeof(unsigned int), s);
+    if (e != cudaSuccess || nb == 0) return e;
+    uint64_t g = (nb + 255) / 256;
+    if (g > 152 * 16) g = 152 * 16;
+    k_bptr_check<<<(unsigned)g, 256, 0, s>>>(bptr, nb, nnz, bad);
+    sptgb_count_launch(1);
+    return cudaGetLastError();
+}
+
 extern "C" cudaError_t sptgb_hicoo_check(const sptgb_hicoo_args *a, cudaStream_t s) {
     if (a->nb == 0) return cudaSuccess;
     uint64_t g = (a->nb + 255) / 256;

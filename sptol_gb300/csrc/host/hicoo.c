@@ -297,9 +297,9 @@ static int hicoo_mttkrp(sptSparseTensorHiCOO const *h, sptMatrix *mats[], sptInd
     const uint64_t n = h->nnz;
     const sptIndex tmpI = mats[mode]->nrows;
     /* Structural checks of the caller's HiCOO arrays, so that no kernel reads
-     * past them: bptr non-decreasing from 0 to nnz, vectors long enough. */
-    int bad = h->values.len < n || (nb && (h->bptr.data[0] != 0 || h->bptr.data[nb] != n)) || h->sb_bits > 8;
-    for (uint64_t b = 0; b < nb && !bad; ++b) bad = h->bptr.data[b + 1] < h->bptr.data[b];
+     * past them: vectors long enough here; bptr non-decreasing from 0 to nnz
+     * on the device, before any kernel uses it. */
+    int bad = h->values.len < n || h->sb_bits > 8;
     for (sptIndex m = 0; m < N && !bad; ++m) bad = h->binds[m].len < nb || h->einds[m].len < n;
     if (bad) {
         spt_ComplainError(module, SPTERR_VALUE_ERROR, __FILE__, __LINE__, "inconsistent HiCOO arrays");
@@ -347,6 +347,17 @@ static int hicoo_mttkrp(sptSparseTensorHiCOO const *h, sptMatrix *mats[], sptInd
     H(sptgb_dbuf_reserve(&g_ws.flag, 2 * sizeof(unsigned int)));
     a.err = (unsigned int *)g_ws.flag.ptr;
     a.nnz = n;
+    {   /* bptr non-decreasing from 0 to nnz, before the schedule or a kernel indexes with it */
+        unsigned int hbad = 0;
+        C(sptgb_hicoo_check_bptr(a.bptr, nb, n, a.err + 1, s));
+        C(cudaMemcpyAsync(&hbad, a.err + 1, sizeof hbad, cudaMemcpyDeviceToHost, s));
+        C(cudaStreamSynchronize(s));
+        if (hbad) {
+            spt_ComplainError(module, SPTERR_VALUE_ERROR, __FILE__, __LINE__, "inconsistent HiCOO arrays");
+            r = SPTERR_VALUE_ERROR;
+            goto out;
+        }
+    }
     /* orders 3 and 4: output-window schedule of this mode, then the window kernel */
     if ((N == 3 || N == 4) && nb && n < 0xffffffffull && ((size_t)1 << h->sb_bits) * stride * 4 <= 200 * 1024) {
         sptgb_hicoo_sched_scratch w;

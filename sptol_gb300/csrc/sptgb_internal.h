@@ -169,6 +169,10 @@ cudaError_t sptgb_mttkrp_hicoo(const sptgb_hicoo_args *a, cudaStream_t s);
 /* *a->err = 1 when an element lies outside its mode or its element offset is
  * not below 2^sb_bits (a->bptr, binds, einds, ndims, nmodes, nb used). */
 cudaError_t sptgb_hicoo_check(const sptgb_hicoo_args *a, cudaStream_t s);
+/* *bad = 1 unless bptr[0] == 0, bptr[nb] == nnz and bptr is non-decreasing
+ * (nb = 0: *bad = 0). */
+cudaError_t sptgb_hicoo_check_bptr(const uint64_t *bptr, uint64_t nb, uint64_t nnz, unsigned int *bad,
+                                   cudaStream_t s);
 /* Output-window schedule of one mode: blocks stably sorted by their block
  * index in `mode` (keys = binds_mode, window_bits significant bits), the
  * prefix of their sizes, the start of each run of equal keys (a window) and

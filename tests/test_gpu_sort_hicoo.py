@@ -211,25 +211,70 @@ def test_hicoo_empty_blocks_in_a_caller_hicoo():
         fill[fresh] = rng.integers(0, (ndims[m] + 127) // 128, int(fresh.sum()))
         nbinds.append(np.insert(A["binds"][m], at, fill).astype(np.uint32))
     assert np.array_equal(np.diff(nbptr)[np.diff(nbptr) > 0], np.diff(bptr))
+    s2, keep = _caller_hicoo(h, nbptr, nbinds)
+    rank = 16
+    mats = S.new_factors(ndims, rank, seed=24)
+    facs = [m.array()[: ndims[k]].copy() for k, m in enumerate(mats[:3])]
+    for mode in range(3):
+        assert _mttkrp_raw(s2, mats, mode) == 0
+        out = mats[3].array()[: ndims[mode], :rank].copy()
+        ref = O.mttkrp(ndims, i2, v2, facs, rank, mode, precision="f64")
+        assert rel_fro(out, ref) <= 1e-5, (mode, rel_fro(out, ref))
+    del keep
+
+
+def _caller_hicoo(h, bptr, binds):
+    """A HiCOO struct of the caller's own arrays: h's element indices and
+    values, the given bptr and block indices (kept alive by the caller)."""
     s2 = S.HiCOOS()
     s2.nmodes = h.s.nmodes
     s2.sortorder = h.s.sortorder
     s2.ndims = h.s.ndims
     s2.nnz = h.s.nnz
     s2.sb_bits, s2.sk_bits, s2.sc_bits = h.s.sb_bits, h.s.sk_bits, h.s.sc_bits
-    s2.bptr = S.NnzIndexVector(len(nbptr), len(nbptr), nbptr.ctypes.data_as(S.u64p))
-    bv = (S.BlockIndexVector * 3)(*[S.BlockIndexVector(len(b), len(b), b.ctypes.data_as(S.u32p)) for b in nbinds])
+    s2.bptr = S.NnzIndexVector(len(bptr), len(bptr), bptr.ctypes.data_as(S.u64p))
+    bv = (S.BlockIndexVector * len(binds))(
+        *[S.BlockIndexVector(len(b), len(b), b.ctypes.data_as(S.u32p)) for b in binds])
     s2.binds = C.cast(bv, C.POINTER(S.BlockIndexVector))
     s2.einds = h.s.einds
     s2.values = h.s.values
-    rank = 16
-    mats = S.new_factors(ndims, rank, seed=24)
+    return s2, (bv, bptr, binds)
+
+
+def _mttkrp_raw(s2, mats, mode):
+    N = int(s2.nmodes)
+    order, op = S._u32([mode] + [(mode + i) % N for i in range(1, N)])
+    mats[N].s.nrows = int(s2.ndims[mode])
+    return S.lib().sptMTTKRPHiCOO(C.byref(s2), S._mat_array(mats), op, mode)
+
+
+def test_inconsistent_block_pointers_are_rejected_then_a_valid_call():
+    """bptr decreasing somewhere, not starting at 0 or not ending at nnz: the
+    call fails (checked on the device before the schedule or a kernel uses
+    bptr); the same tensor with its own bptr then gives the right result."""
+    t = _skewed3(50_000, 25)
+    ndims = t.ndims
+    h = S.HiCOO(t, 7, 17)
+    A = h.arrays()
+    i2, v2 = t.arrays()
+    rank = 8
+    mats = S.new_factors(ndims, rank, seed=26)
+    binds = [b.astype(np.uint32) for b in A["binds"]]
+    good = A["bptr"].astype(np.uint64)
+    nb = len(good) - 1
+    bad_variants = []
+    b1 = good.copy(); b1[nb // 2] = b1[nb // 2 + 1] + 5; bad_variants.append(b1)   # decreasing
+    b2 = good.copy(); b2[0] = 1; bad_variants.append(b2)                         # does not start at 0
+    b3 = good.copy(); b3[nb] = good[nb] + 1000; bad_variants.append(b3)          # runs past nnz
+    for bp in bad_variants:
+        s2, keep = _caller_hicoo(h, bp, binds)
+        for mode in range(3):
+            assert _mttkrp_raw(s2, mats, mode) == 3
+        del keep
+    s2, keep = _caller_hicoo(h, good, binds)
     facs = [m.array()[: ndims[k]].copy() for k, m in enumerate(mats[:3])]
     for mode in range(3):
-        order, op = S._u32([mode] + [(mode + i) % 3 for i in (1, 2)])
-        mats[3].s.nrows = ndims[mode]
-        assert S.lib().sptMTTKRPHiCOO(C.byref(s2), S._mat_array(mats), op, mode) == 0
-        out = mats[3].array()[: ndims[mode], :rank].copy()
+        assert _mttkrp_raw(s2, mats, mode) == 0
         ref = O.mttkrp(ndims, i2, v2, facs, rank, mode, precision="f64")
-        assert rel_fro(out, ref) <= 1e-5, (mode, rel_fro(out, ref))
-    del bv, nbinds, nbptr
+        assert rel_fro(mats[3].array()[: ndims[mode], :rank], ref) <= 1e-5
+    del keep
