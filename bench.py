@@ -18,7 +18,10 @@ Workload (one "step" = MTTKRP of every mode, 0, 1, 2, on one GPU):
   cpu_baseline  the oracle port of sptOmpMTTKRP_Reduce (all host threads) on
           a 10M-nonzero sample tensor of the same shape and distributions.
   hicoo   the same tensor as HiCOO (blocks 2^7, kernels 2^17): conversion time
-          and sptMTTKRPHiCOO per mode (kernel time from CUDA events).
+          and sptMTTKRPHiCOO per mode (kernel time from CUDA events); its
+          cpu_baseline is the oracle port of
+          sptOmpMTTKRPHiCOO_MatrixTiling_Scheduled_Reduce (all host threads)
+          on the HiCOO form of the 10M-nonzero sample.
   serve   the batched / served CP-ALS stream: 4,096 requests of order 3 or 4
           (50/50), mode sizes log-uniform in [64, 100,000], nnz log-uniform in
           [1e3, 1e6] (at most half the index space, unique uniform
@@ -269,6 +272,40 @@ def hicoo_leg(t, mats, ndims, nnz, reps):
             "algorithmic_bytes_per_mttkrp": hb,
             "kernel_gbs": round(N * hb / (sum(kern) / 1e3) / 1e9, 1),
             "coo_bytes_gbs": round(N * algo_bytes(ndims, nnz, RANK) / (sum(kern) / 1e3) / 1e9, 1)}
+
+
+def hicoo_cpu_leg(sample_nnz, reps):
+    """sptOmpMTTKRPHiCOO_MatrixTiling_Scheduled_Reduce restated (oracle) with
+    all host threads on a bounded sample of the workload (HiCOO built by the
+    library's conversion): GB/s on the same HiCOO byte count as the GPU leg."""
+    import oracle as O
+    import sptol_gb300 as S
+    O.build(with_ref=False)
+    threads = os.cpu_count() or 1
+    t = S.Tensor.generate(spec_for(sample_nnz, seed=SEED + 1))
+    mats = S.new_factors(DIMS, RANK, seed=2)
+    h = S.HiCOO(t, 7, 17)
+    A = h.arrays()
+    nb = len(A["bptr"]) - 1
+    _, vals = t.arrays()
+    facs = [m.array()[: t.ndims[i]] for i, m in enumerate(mats[:3])]
+    rows = [O.kschr_rows(A, t.ndims, 17, m) for m in range(3)]
+    h.free()
+    copies = np.zeros(threads * max(t.ndims) * mats[0].s.stride, np.float32)
+    secs = []
+    for r in range(reps + 1):
+        t0 = time.perf_counter()
+        for m in range(3):
+            O.omp_mttkrp_hicoo_reduce(t.ndims, A, vals, 7, facs, RANK, m, threads, rows[m], copies=copies)
+        if r > 0:
+            secs.append(time.perf_counter() - t0)
+    step = float(np.mean(secs))
+    hb = t.nnz * 7 + nb * 20 + sum(d * RANK * 4 for d in t.ndims)
+    return {"value": round(3 * hb / step / 1e9, 3), "unit": "GB/s", "cores": threads, "kind": "port",
+            "sample": ("%d-nnz tensor of the same shape and distributions (%d HiCOO blocks), all 3 modes, %d reps "
+                       "after 1 warm-up, sptOmpMTTKRPHiCOO_MatrixTiling_Scheduled_Reduce with %d threads"
+                       % (t.nnz, nb, reps, threads)),
+            "seconds_per_step": step}
 
 
 def serve_leg(args):
@@ -634,6 +671,8 @@ def run_ours(args, world, rank, local):
     if world == 1 and not args.skip_hicoo:
         coo.free()
         hicoo = hicoo_leg(t, mats, ndims, nnz, 3)
+        if not args.skip_cpu:
+            hicoo["cpu_baseline"] = hicoo_cpu_leg(args.cpu_sample, 2)
 
     serve = None
     if world == 1 and not args.skip_serve:

@@ -73,6 +73,10 @@ def orc():
         L.orc_mttkrp_hicoo_f32.argtypes = [C.c_uint32, C.c_uint64, u64p, C.POINTER(u32p), C.POINTER(u8p), f32p,
                                            C.c_int, C.POINTER(f32p), C.c_uint32, C.c_uint32, u32p, C.c_uint32,
                                            C.c_uint32, f32p]
+        L.orc_omp_mttkrp_hicoo_reduce.argtypes = [C.c_uint32, u64p, C.POINTER(u32p), C.POINTER(u8p), f32p, C.c_int,
+                                                  u64p, C.c_uint32, u64p, u32p, C.c_uint32, C.POINTER(f32p),
+                                                  C.c_uint32, C.c_uint32, u32p, C.c_uint32, C.c_uint32, f32p, C.c_int,
+                                                  f32p]
         L.orc_cpd_als_f64.argtypes = [C.c_uint32, u32p, C.c_uint64, C.POINTER(u32p), f32p, C.c_uint32, C.c_uint32,
                                       C.c_double, C.POINTER(f32p), C.c_uint32, f32p, f64p, u32p]
         L.orc_fit_exact.argtypes = [C.c_uint32, u32p, C.c_uint64, C.POINTER(u32p), f32p, C.c_uint32,
@@ -225,6 +229,53 @@ def mttkrp(ndims, inds, vals, mats, rank, mode, order=None, precision="f32", tk=
     else:
         out = np.zeros((rows, stride), np.float32)
         L.orc_mttkrp_f32(*args, out.ctypes.data_as(f32p))
+    return out[:, :rank]
+
+
+def kschr_rows(h, ndims, sk_bits, mode):
+    """Kernel ids of every kernel row of `mode`, from either HiCOO layout:
+    nested lists (sptSparseTensorHiCOO.kschr as read back from the library)
+    or the flattened kschr_len / kschr arrays of hicoo_build."""
+    if "kschr_len" not in h:
+        return [np.asarray(r, np.uint32) for r in h["kschr"][mode]]
+    rows = [(d + (1 << sk_bits) - 1) >> sk_bits for d in ndims]
+    r0 = sum(rows[:mode])
+    lens = h["kschr_len"].astype(np.int64)
+    start = int(lens[:r0].sum())
+    out = []
+    for i in range(rows[mode]):
+        ln = int(lens[r0 + i])
+        out.append(h["kschr"][start:start + ln].astype(np.uint32))
+        start += ln
+    return out
+
+
+def omp_mttkrp_hicoo_reduce(ndims, h, vals, sb_bits, mats, rank, mode, tk, ks_rows, order=None, copies=None):
+    """3-D HiCOO MTTKRP as sptOmpMTTKRPHiCOO_MatrixTiling_Scheduled_Reduce
+    (the kernel rows of `mode`, ks_rows = kschr_rows(...), per-thread output
+    copies)."""
+    N = len(ndims)
+    order = _default_order(N, mode) if order is None else order
+    stride = stride_of(rank)
+    bk, bp = _rows(list(h["binds"]), u32p, np.uint32)
+    ek, ep = _rows(list(h["einds"]), u8p, np.uint8)
+    mkeep, mp = _rows(mats, f32p, np.float32)
+    v = np.ascontiguousarray(vals, np.float32)
+    bptr = np.ascontiguousarray(h["bptr"], np.uint64)
+    kptr = np.ascontiguousarray(h["kptr"], np.uint64)
+    rows_k = ks_rows
+    ks_off = np.zeros(len(rows_k) + 1, np.uint64)
+    ks_off[1:] = np.cumsum([len(r) for r in rows_k])
+    ks_ids = np.ascontiguousarray(np.concatenate(rows_k) if len(rows_k) else np.zeros(0), np.uint32)
+    o, op = _u32(order)
+    out = np.zeros((ndims[mode], stride), np.float32)
+    if copies is None or copies.size < tk * ndims[mode] * stride:
+        copies = np.zeros(tk * ndims[mode] * stride, np.float32)
+    orc().orc_omp_mttkrp_hicoo_reduce(N, bptr.ctypes.data_as(u64p), bp, ep, v.ctypes.data_as(f32p), sb_bits,
+                                      kptr.ctypes.data_as(u64p), len(rows_k), ks_off.ctypes.data_as(u64p),
+                                      ks_ids.ctypes.data_as(u32p), max((len(r) for r in rows_k), default=0), mp,
+                                      stride, rank, op, mode,
+                                      ndims[mode], out.ctypes.data_as(f32p), tk, copies.ctypes.data_as(f32p))
     return out[:, :rank]
 
 

@@ -380,6 +380,49 @@ void orc_mttkrp_hicoo_f32(uint32_t nmodes, uint64_t nb, const uint64_t *bptr, co
     }
 }
 
+/* hicoo/mttkrp_omp.c:1214-1296 (3-D MatrixTiling_Scheduled_Reduce): a dynamic
+ * parallel loop (chunk 1, mttkrp_omp.c:22) over the schedule iterations
+ * i < nkiters; in iteration i, kernel i of every kernel row (kschr[mode][k][i],
+ * kernel rows in order), its blocks in order, the elements of a block in
+ * order, each thread summing into its own output copy; then the copies are
+ * added row by row in thread order.  The kernel rows of `mode` are given
+ * flattened: kernel ids ks_ids[ks_off[k] .. ks_off[k+1]). */
+void orc_omp_mttkrp_hicoo_reduce(uint32_t nmodes, const uint64_t *bptr, const uint32_t *const *binds,
+                                 const uint8_t *const *einds, const float *vals, int sb_bits, const uint64_t *kptr,
+                                 uint32_t nkrows, const uint64_t *ks_off, const uint32_t *ks_ids, uint32_t nkiters,
+                                 const float *const *mats, uint32_t stride, uint32_t R, const uint32_t *mats_order,
+                                 uint32_t mode, uint32_t out_rows, float *out, int tk, float *copies) {
+    if (nmodes != 3) return;
+    memset(out, 0, (size_t)out_rows * stride * sizeof(float));
+    const size_t csz = (size_t)out_rows * stride;
+    memset(copies, 0, (size_t)tk * csz * sizeof(float));
+    const uint32_t m1 = mats_order[1], m2 = mats_order[2];
+#pragma omp parallel for schedule(dynamic, 1) num_threads(tk)
+    for (uint32_t i = 0; i < nkiters; ++i) {
+        float *cp = copies + (size_t)omp_get_thread_num() * csz;
+        for (uint32_t k = 0; k < nkrows; ++k) {
+            if (i >= ks_off[k + 1] - ks_off[k]) continue;
+            const uint32_t kid = ks_ids[ks_off[k] + i];
+            for (uint64_t b = kptr[kid]; b < kptr[kid + 1]; ++b) {
+                float *bo = cp + (size_t)(binds[mode][b] << sb_bits) * stride;
+                const float *b1 = mats[m1] + (size_t)(binds[m1][b] << sb_bits) * stride;
+                const float *b2 = mats[m2] + (size_t)(binds[m2][b] << sb_bits) * stride;
+                for (uint64_t z = bptr[b]; z < bptr[b + 1]; ++z) {
+                    const float entry = vals[z];
+                    float *o = bo + (size_t)einds[mode][z] * stride;
+                    const float *r1 = b1 + (size_t)einds[m1][z] * stride;
+                    const float *r2 = b2 + (size_t)einds[m2][z] * stride;
+                    for (uint32_t r = 0; r < R; ++r) o[r] += entry * r1[r] * r2[r];
+                }
+            }
+        }
+    }
+#pragma omp parallel for schedule(static) num_threads(tk)
+    for (uint32_t i = 0; i < out_rows; ++i)
+        for (int t = 0; t < tk; ++t)
+            for (uint32_t r = 0; r < R; ++r) out[(size_t)i * stride + r] += copies[(size_t)t * csz + (size_t)i * stride + r];
+}
+
 /* -------------------------------------------------------------- CP-ALS --
  * cpd.c:32-137 restated in FP64 with a correct fit:
  *   Grams A^T A (full), per iteration and mode: MTTKRP, solve with the

@@ -37,6 +37,17 @@ def test_hicoo(case):
         for mode in range(len(ndims)):
             out = O.mttkrp_hicoo(ndims, h, g["sorted_vals"], int(g["sb"]), mats, rank, mode)
             assert np.array_equal(out, g["out%d" % mode][:, :rank])
+            if len(ndims) == 3:
+                # the scheduled, privatised OpenMP form: one thread visits each
+                # output row's kernels in the sequential order (bit-exact)
+                rows = O.kschr_rows(h, ndims, int(g["sk"]), mode)
+                for tk in (1, 4):
+                    par = O.omp_mttkrp_hicoo_reduce(ndims, h, g["sorted_vals"], int(g["sb"]), mats, rank, mode,
+                                                    tk, rows)
+                    if tk == 1:
+                        assert np.array_equal(par, g["out%d" % mode][:, :rank])
+                    else:
+                        assert rel_fro(par, g["out%d" % mode][:, :rank]) <= 1e-6
 
 
 @pytest.mark.parametrize("case", ["mttkrp_3d_r16", "mttkrp_3d_r17", "mttkrp_4d_r8"])
