@@ -12,6 +12,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 #include <cuda_runtime_api.h>
 #include "devtensor.h"
 
@@ -19,6 +20,21 @@ sptgb_workspace g_ws = {PTHREAD_MUTEX_INITIALIZER};
 
 void sptgb_lock(void) { pthread_mutex_lock(&g_ws.lock); }
 void sptgb_unlock(void) { pthread_mutex_unlock(&g_ws.lock); }
+
+int sptgb_trace_on(void) {
+    static int on = -1;
+    if (on < 0) {
+        const char *e = getenv("SPTGB_TRACE");
+        on = (e && e[0] && e[0] != '0') ? 1 : 0;
+    }
+    return on;
+}
+
+double sptgb_wall(void) {
+    struct timespec t;
+    clock_gettime(CLOCK_MONOTONIC, &t);
+    return t.tv_sec + 1e-9 * t.tv_nsec;
+}
 
 int sptgb_ws_sync_objects(void) {
     if (!g_ws.hflag) {

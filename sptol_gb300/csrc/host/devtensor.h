@@ -23,6 +23,22 @@ typedef struct {
 } sptgb_workspace;
 extern sptgb_workspace g_ws;
 
+/* SPTGB_TRACE=1 prints the wall time of each phase of a host-buffer call to
+ * stderr (the reference prints its H2D / kernel / D2H times the same way,
+ * src/sptensor/mttkrp_cuda_onekernel.cu:151-155, :381-404); a trace point
+ * synchronises the stream first. */
+int    sptgb_trace_on(void);
+double sptgb_wall(void);
+#define SPTGB_TRACE_POINT(name, stream, t_prev)                                          \
+    do {                                                                                 \
+        if (sptgb_trace_on()) {                                                          \
+            cudaStreamSynchronize(stream);                                               \
+            const double _t = sptgb_wall();                                              \
+            fprintf(stderr, "[sptgb trace] %-10s %8.3f ms\n", name, (_t - (t_prev)) * 1e3); \
+            (t_prev) = _t;                                                               \
+        }                                                                                \
+    } while (0)
+
 void sptgb_lock(void);
 /* Pinned flag words and the two events above, created on first use (lock held). */
 int  sptgb_ws_sync_objects(void);

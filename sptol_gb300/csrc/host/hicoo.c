@@ -311,6 +311,7 @@ static int hicoo_mttkrp(sptSparseTensorHiCOO const *h, sptMatrix *mats[], sptInd
     sptgb_hicoo_args a;
     memset(&a, 0, sizeof a);
     /* bptr, binds, einds, values */
+    double t_prev = sptgb_wall();
     H(sptgb_dbuf_reserve(&g_ws.misc[0], (nb + 1) * 8));
     C(cudaMemcpyAsync(g_ws.misc[0].ptr, h->bptr.data, (nb + 1) * 8, cudaMemcpyHostToDevice, s));
     H(sptgb_dbuf_reserve(&g_ws.misc[1], (size_t)N * (nb * 4 + n) + 64));
@@ -332,6 +333,7 @@ static int hicoo_mttkrp(sptSparseTensorHiCOO const *h, sptMatrix *mats[], sptInd
         a.fac[pm] = (const float *)g_ws.fac[pm].ptr;
     }
     H(sptgb_dbuf_reserve(&g_ws.out, (size_t)(tmpI ? tmpI : 1) * stride * 4));
+    SPTGB_TRACE_POINT("h2d", s, t_prev);
     a.bptr = (const uint64_t *)g_ws.misc[0].ptr;
     a.vals = (const float *)g_ws.vals.ptr;
     a.out = (float *)g_ws.out.ptr;
@@ -358,6 +360,7 @@ static int hicoo_mttkrp(sptSparseTensorHiCOO const *h, sptMatrix *mats[], sptInd
             goto out;
         }
     }
+    SPTGB_TRACE_POINT("bptr check", s, t_prev);
     /* orders 3 and 4: output-window schedule of this mode, then the window kernel */
     if ((N == 3 || N == 4) && nb && n < 0xffffffffull && ((size_t)1 << h->sb_bits) * stride * 4 <= 200 * 1024) {
         sptgb_hicoo_sched_scratch w;
@@ -389,15 +392,18 @@ static int hicoo_mttkrp(sptSparseTensorHiCOO const *h, sptMatrix *mats[], sptInd
         a.heavy = wst + nb + 1;
         a.nheavy = nheavy;
     }
+    SPTGB_TRACE_POINT("schedule", s, t_prev);
     C(cudaMemsetAsync(a.err, 0, sizeof(unsigned int), s));
     if (g_hicoo_timing) C(cudaEventRecord(g_hicoo_ev[0], s));
     C(sptgb_mttkrp_hicoo(&a, s));
     if (g_hicoo_timing) C(cudaEventRecord(g_hicoo_ev[1], s));
+    SPTGB_TRACE_POINT("kernel", s, t_prev);
     unsigned int herr = 0;
     C(cudaMemcpyAsync(&herr, a.err, sizeof herr, cudaMemcpyDeviceToHost, s));
     if (tmpI) C(cudaMemcpyAsync(mats[N]->values, g_ws.out.ptr, (size_t)tmpI * stride * 4, cudaMemcpyDeviceToHost, s));
     C(cudaStreamSynchronize(s));
     if (g_hicoo_timing) C(cudaEventElapsedTime(&g_hicoo_ms, g_hicoo_ev[0], g_hicoo_ev[1]));
+    SPTGB_TRACE_POINT("d2h out", s, t_prev);
     if (herr) {
         spt_ComplainError(module, SPTERR_VALUE_ERROR, __FILE__, __LINE__,
                           "a coordinate is not smaller than its mode size");

@@ -25,34 +25,9 @@
 #include <stdlib.h>
 #include <string.h>
 #include <cuda_runtime_api.h>
-#include <time.h>
 #include "devtensor.h"
 
-/* SPTGB_TRACE=1 prints the wall time of each phase of a host-buffer call to
- * stderr (the reference prints its H2D / kernel / D2H times the same way,
- * src/sptensor/mttkrp_cuda_onekernel.cu:151-155, :381-404). */
-static int trace_on(void) {
-    static int on = -1;
-    if (on < 0) {
-        const char *e = getenv("SPTGB_TRACE");
-        on = (e && e[0] && e[0] != '0') ? 1 : 0;
-    }
-    return on;
-}
-static double wall(void) {
-    struct timespec t;
-    clock_gettime(CLOCK_MONOTONIC, &t);
-    return t.tv_sec + 1e-9 * t.tv_nsec;
-}
-#define TRACE(name)                                                              \
-    do {                                                                         \
-        if (trace_on()) {                                                        \
-            cudaStreamSynchronize(s);                                            \
-            const double _t = wall();                                            \
-            fprintf(stderr, "[sptgb trace] %-10s %8.3f ms\n", name, (_t - t_prev) * 1e3); \
-            t_prev = _t;                                                         \
-        }                                                                        \
-    } while (0)
+#define TRACE(name) SPTGB_TRACE_POINT(name, s, t_prev)
 
 static int check_mats(sptIndex nmodes, const sptIndex *ndims, sptMatrix *mats[], sptIndex mode, const char *module) {
     if (nmodes < 2 || nmodes > SPTGB_MAX_MODES || mode >= nmodes) {
@@ -106,7 +81,7 @@ static int mttkrp_host_locked(sptSparseTensor const *X, sptMatrix *mats[], sptIn
     const sptIndex R = mats[mode]->ncols;
     const sptIndex tmpI = mats[mode]->nrows;
     sptMatrix *M = mats[N];
-    double t_prev = wall();
+    double t_prev = sptgb_wall();
 
     int need[SPTGB_MAX_MODES] = {0};
     need[mode] = 1;
