@@ -397,13 +397,30 @@ __device__ __forceinline__ void solve_rows_body(const float *__restrict__ M, flo
     float *StH = smf;                       // [RMAX][LDK]: S^T hi, k-major per column
     float *StN = StH + RMAX * LDK;          // -hi
     float *StL = StN + RMAX * LDK;          // lo
-    float *Mt = StL + RMAX * LDK;           // [TR][LDK]
-    float *XT = Mt + TR * LDK;              // [RMAX][LDR]: tile of X, transposed
+    float *Mt2 = StL + RMAX * LDK;          // [2][TR][LDK]: row tiles of M, double-buffered
+    float *XT = Mt2 + 2 * TR * LDK;         // [RMAX][LDR]: tile of X, transposed
     float *XN = XT + RMAX * LDR;            // -XT
     __shared__ unsigned char pp_s[PMAX], qq_s[PMAX];
     const int P = rank * (rank + 1) / 2;
     const int RR = rank * rank;
     const int rank2 = (rank + 1) & ~1;
+    // TR x rank2 floats of M from row t0 into dst as 8-byte cp.async chunks,
+    // one commit group; rows past nrows and columns past rank read as zero
+    // (source size 0 or 4 of the 8 bytes)
+    auto load_tile = [&](float *dst, uint64_t t0) {
+        const int half = rank2 / 2;
+        for (int e = threadIdx.x; e < TR * half; e += DT) {
+            const int r = e / half, c = 2 * (e % half);
+            const uint64_t row = t0 + r;
+            const unsigned bytes = row < nrows ? (c + 1 < rank ? 8u : (c < rank ? 4u : 0u)) : 0u;
+            const float *src = bytes ? M + row * stride + c : M;
+            const unsigned dst_s = (unsigned)__cvta_generic_to_shared(dst + r * LDK + c);
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(dst_s), "l"(src), "r"(bytes) : "memory");
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    int cur = 0;
+    if ((uint64_t)bid * TR < nrows) load_tile(Mt2, (uint64_t)bid * TR);
     const float *Sf = reinterpret_cast<const float *>(S);
     for (int e = threadIdx.x; e < rank * rank2; e += DT) {
         const int c = e / rank2, k = e % rank2;   // S[k][c]
@@ -427,12 +444,16 @@ __device__ __forceinline__ void solve_rows_body(const float *__restrict__ M, flo
     const int c0 = threadIdx.x % rank, r0 = threadIdx.x / rank, rstep = DT / rank;
     const int nout = (TR * rank + DT - 1) / DT;   // 1, 2, 4 or 8 when fixed_col
     for (uint64_t t0 = (uint64_t)bid * TR; t0 < nrows; t0 += (uint64_t)nbk * TR) {
-        __syncthreads();
-        for (int e = threadIdx.x; e < TR * rank2; e += DT) {
-            const int r = e / rank2, c = e % rank2;
-            const uint64_t row = t0 + r;
-            Mt[r * LDK + c] = (row < nrows && c < rank) ? M[row * stride + c] : 0.f;
+        // the next tile streams into the other buffer while this one is used;
+        // that buffer was last read before the previous iteration's barrier
+        const float *Mt = Mt2 + cur * TR * LDK;
+        if (t0 + (uint64_t)nbk * TR < nrows) {
+            load_tile(Mt2 + (cur ^ 1) * TR * LDK, t0 + (uint64_t)nbk * TR);
+            asm volatile("cp.async.wait_group 1;" ::: "memory");
+        } else {
+            asm volatile("cp.async.wait_group 0;" ::: "memory");
         }
+        cur ^= 1;
         __syncthreads();
         if (fixed_col) {
             if (r0 < TR) {
@@ -684,7 +705,7 @@ __host__ __device__ inline int nblocks_for_rows(uint64_t nrows) {
     return (int)b;
 }
 
-constexpr size_t SOLVE_SMEM = (size_t)(3 * RMAX * LDK + TR * LDK + 2 * RMAX * LDR) * sizeof(float);
+constexpr size_t SOLVE_SMEM = (size_t)(3 * RMAX * LDK + 2 * TR * LDK + 2 * RMAX * LDR) * sizeof(float);
 constexpr size_t PREP_SMEM = (size_t)(2 * RMAX * (RMAX + 1)) * sizeof(double);
 
 
