@@ -84,6 +84,7 @@ struct sptgbServer {
     uint32_t ul[4];
     int tuned;
     cudaStream_t cs;
+    cudaStream_t as;             /* admission: uploads, checks, sorts of new slots, overlapping the step on cs */
     cudaGraphExec_t gexec;
     int have_graph;
     int changed;
@@ -222,15 +223,15 @@ static void list_add(sptgbServer *s, int l, uint32_t id, uint64_t items) {
 }
 
 /* Uploads lists [l0, l1). */
-static int lists_upload(sptgbServer *s, int l0, int l1) {
+static int lists_upload(sptgbServer *s, int l0, int l1, cudaStream_t st) {
     const char *module = "GPU server lists";
-    SPTGB_CUDA(cudaMemcpyAsync(s->d_counts + l0, s->h_counts + l0, (size_t)(l1 - l0) * 4, cudaMemcpyHostToDevice, s->cs),
+    SPTGB_CUDA(cudaMemcpyAsync(s->d_counts + l0, s->h_counts + l0, (size_t)(l1 - l0) * 4, cudaMemcpyHostToDevice, st),
                module);
     SPTGB_CUDA(cudaMemcpyAsync(s->d_ids + (size_t)l0 * s->cap, s->h_ids + (size_t)l0 * s->cap,
-                               (size_t)(l1 - l0) * s->cap * 4, cudaMemcpyHostToDevice, s->cs),
+                               (size_t)(l1 - l0) * s->cap * 4, cudaMemcpyHostToDevice, st),
                module);
     SPTGB_CUDA(cudaMemcpyAsync(s->d_pre + (size_t)l0 * (s->cap + 1), s->h_pre + (size_t)l0 * (s->cap + 1),
-                               (size_t)(l1 - l0) * (s->cap + 1) * 8, cudaMemcpyHostToDevice, s->cs),
+                               (size_t)(l1 - l0) * (s->cap + 1) * 8, cudaMemcpyHostToDevice, st),
                module);
     return 0;
 }
@@ -309,7 +310,7 @@ static int sort_group_mode(sptgbServer *s, const sptgb_adm_group *g, int mode, i
     uint32_t *keys[2] = {(uint32_t *)s->keys[0].ptr, (uint32_t *)s->keys[1].ptr};
     uint32_t *perm[2] = {(uint32_t *)s->perm[0].ptr, (uint32_t *)s->perm[1].ptr};
     int cur = 0;
-    SPTGB_CUDA(sptgb_iota_u32(perm[0], n, 0, s->cs), module);
+    SPTGB_CUDA(sptgb_iota_u32(perm[0], n, 0, s->as), module);
     /* (job, row) in one key when it fits in 32 bits, else row then job */
     int kinds[2], bits[2], np = 0;
     if (jbits + rowbits <= 32) {
@@ -323,11 +324,11 @@ static int sort_group_mode(sptgbServer *s, const sptgb_adm_group *g, int mode, i
     }
     for (int p = 0; p < np; ++p) {
         if (bits[p] == 0) continue;
-        SPTGB_CUDA(sptgb_adm_keys(g, mode, rowbits, kinds[p], p ? perm[cur] : NULL, keys[0], s->cs), module);
+        SPTGB_CUDA(sptgb_adm_keys(g, mode, rowbits, kinds[p], p ? perm[cur] : NULL, keys[0], s->as), module);
         uint32_t *kk[2] = {keys[0], keys[1]};
         uint32_t *vv[2] = {perm[cur], perm[cur ^ 1]};
         int which = 0;
-        SPTGB_CUDA(sptgb_radix_sort_u32(kk, vv, n, bits[p], s->rtmp.ptr, &which, s->cs), module);
+        SPTGB_CUDA(sptgb_radix_sort_u32(kk, vv, n, bits[p], s->rtmp.ptr, &which, s->as), module);
         if (which) cur ^= 1;
     }
     *perm_out = perm[cur];
@@ -360,7 +361,7 @@ static void fail_job(sptgbServer *s, job_t *j) {
 /* Admits the group s->grp[0..G) (slots and arena space already reserved). */
 static int admit_group(sptgbServer *s, uint32_t G) {
     const char *module = "GPU server admit";
-    const cudaStream_t cs = s->cs;
+    const cudaStream_t cs = s->as;   /* the step graph may be running on s->cs */
     uint64_t total = 0;
     uint32_t lo = s->cap, hi = 0;
     int maxN = 0, rowbits[4] = {0, 0, 0, 0};
@@ -451,7 +452,7 @@ static int admit_group(sptgbServer *s, uint32_t G) {
             list_add(s, NL_GONE + (int)m, a->slot, 1);
         }
     }
-    SPTGB_CHECK(lists_upload(s, NL_STEP, NL_ADM_END), module);
+    SPTGB_CHECK(lists_upload(s, NL_STEP, NL_ADM_END, cs), module);
     const sptgb_wlist sq = wl(s, NL_SQ), sqone = wl(s, NL_SQONE);
     SPTGB_CUDA(sptgb_adm_normsq(s->ds, &g, &sq, &sqone, cs), module);
     for (uint32_t q = 0; q < G; ++q) {
@@ -517,7 +518,7 @@ static int retire(sptgbServer *s, uint32_t R) {
         }
         if ((int)d->nmodes > maxN) maxN = (int)d->nmodes;
     }
-    SPTGB_CHECK(lists_upload(s, NL_RDN, NLISTS), module);
+    SPTGB_CHECK(lists_upload(s, NL_RDN, NLISTS, s->cs), module);
     for (int m = 0; m < maxN; ++m) {
         const sptgb_wlist dn = wl(s, NL_RDN + m), one = wl(s, NL_RONE + m);
         SPTGB_CUDA(sptgb_batch_final_lambda(s->ds, &dn, &one, m, s->cs), module);
@@ -568,7 +569,7 @@ static int autotune(sptgbServer *s) {
         for (int c = 0; c < 4; ++c) {
             s->ul[g] = cand[c];
             step_lists_build(s);
-            SPTGB_CHECK(lists_upload(s, 0, NL_STEP), module);
+            SPTGB_CHECK(lists_upload(s, 0, NL_STEP, s->cs), module);
             const sptgb_wlist w = wl(s, NL_MT + g);
             float ms = 0.f, tot = 0.f;
             for (int rep = 0; rep < 3; ++rep) {
@@ -636,6 +637,7 @@ int sptgbServerCreate(sptgbServer **out, size_t hbm_budget_bytes, uint32_t max_s
     if (e == cudaSuccess) e = cudaMalloc((void **)&s->d_ids, (size_t)NLISTS * s->cap * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMalloc((void **)&s->d_pre, (size_t)NLISTS * (s->cap + 1) * sizeof(uint64_t));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->cs, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->as, cudaStreamNonBlocking);
     if (e != cudaSuccess) r = sptgb_cuda_fail(e, "GPU server create", __FILE__, __LINE__);
     const uint32_t gcap = s->cap < SERVE_GROUP_JOBS ? s->cap : SERVE_GROUP_JOBS;
     s->hs = (sptgb_slot *)calloc(s->cap, sizeof(sptgb_slot));
@@ -720,8 +722,38 @@ int sptgbServerSubmit(sptgbServer *s, const sptSparseTensor *X, sptIndex rank, s
 int sptgbServerStep(sptgbServer *s, uint32_t *active, uint32_t *queued) {
     const char *module = "GPU server step";
     SPTGB_CHECK(sptgb_ctx(), module);
-    double t0 = s->trace ? now_s() : 0.0;
-    /* 1. admission group: queued jobs that fit, in submission order */
+    double t0 = 0.0;
+    /* 1. one ALS iteration of every job admitted by an earlier call, launched
+     *    first: this call's admission (its own stream, new slots only) runs on
+     *    the host and the copy engines while the graph runs */
+    uint32_t R = 0;
+    if (s->nactive > 0) {
+        if (!s->tuned) {
+            SPTGB_CHECK(autotune(s), module);
+            s->changed = 1;
+        }
+        if (s->changed) {
+            step_lists_build(s);
+            SPTGB_CHECK(lists_upload(s, 0, NL_STEP, s->cs), module);
+            s->changed = 0;
+        }
+        if (!s->have_graph) SPTGB_CHECK(capture(s), module);
+        if (s->trace) t0 = now_s();
+        SPTGB_CUDA(cudaGraphLaunch(s->gexec, s->cs), module);
+        if (s->trace) {
+            SPTGB_CUDA(cudaStreamSynchronize(s->cs), module);
+            s->t_step += now_s() - t0;
+            ++s->n_steps;
+        }
+        /* the slots in this step that reach their iteration count retire
+         * after it (slots admitted below start at the next step) */
+        for (uint32_t i = 0; i < s->cap; ++i) {
+            if (s->slot_job[i] < 0) continue;
+            if (++s->slot_iters[i] >= s->jobs[s->slot_job[i]].niters) s->ret[R++] = i;
+        }
+    }
+    /* 2. admission group: queued jobs that fit, in submission order */
+    if (s->trace) t0 = now_s();
     const uint32_t gcap = s->cap < SERVE_GROUP_JOBS ? s->cap : SERVE_GROUP_JOBS;
     uint32_t G = 0;
     uint64_t gnnz = 0, keep = 0;
@@ -759,43 +791,17 @@ int sptgbServerStep(sptgbServer *s, uint32_t *active, uint32_t *queued) {
         if (r) {
             for (uint32_t q = 0; q < G; ++q)
                 if (s->jobs[s->grp[q]].state == JOB_QUEUED) fail_job(s, &s->jobs[s->grp[q]]);
+            cudaStreamSynchronize(s->cs);   /* nothing of this call outlives it on error */
             return r;
         }
         /* jobs with no iterations finish at once */
-        uint32_t R = 0;
         for (uint32_t q = 0; q < G; ++q) {
             const job_t *j = &s->jobs[s->grp[q]];
             if (j->state == JOB_ACTIVE && j->niters == 0) s->ret[R++] = (uint32_t)j->slot;
         }
-        SPTGB_CHECK(retire(s, R), module);
     }
-    /* 2. one ALS iteration of every admitted job */
-    if (s->nactive > 0) {
-        if (!s->tuned) {
-            SPTGB_CHECK(autotune(s), module);
-            s->changed = 1;
-        }
-        if (s->changed) {
-            step_lists_build(s);
-            SPTGB_CHECK(lists_upload(s, 0, NL_STEP), module);
-            s->changed = 0;
-        }
-        if (!s->have_graph) SPTGB_CHECK(capture(s), module);
-        if (s->trace) t0 = now_s();
-        SPTGB_CUDA(cudaGraphLaunch(s->gexec, s->cs), module);
-        if (s->trace) {
-            SPTGB_CUDA(cudaStreamSynchronize(s->cs), module);
-            s->t_step += now_s() - t0;
-            ++s->n_steps;
-        }
-        /* 3. retirement */
-        uint32_t R = 0;
-        for (uint32_t i = 0; i < s->cap; ++i) {
-            if (s->slot_job[i] < 0) continue;
-            if (++s->slot_iters[i] >= s->jobs[s->slot_job[i]].niters) s->ret[R++] = i;
-        }
-        SPTGB_CHECK(retire(s, R), module);
-    }
+    /* 3. retirement (after the step: retire() runs on the step's stream) */
+    SPTGB_CHECK(retire(s, R), module);
     if (active) *active = s->nactive;
     if (queued) *queued = (uint32_t)s->nqueue;
     return 0;
@@ -855,6 +861,7 @@ void sptgbServerFree(sptgbServer *s) {
     sptgb_dbuf_release(&s->d_goffs);
     sptgb_dbuf_release(&s->d_gerr);
     if (s->cs) cudaStreamDestroy(s->cs);
+    if (s->as) cudaStreamDestroy(s->as);
     free(s->hs);
     free(s->slot_job);
     free(s->slot_off);
