@@ -8,6 +8,7 @@ import tempfile
 
 import pytest
 
+import oracle as O
 import sptol_gb300 as S
 from conftest import ROOT
 
@@ -79,9 +80,9 @@ def test_ctypes_mirror_matches_header():
     assert int(ours["sptSparseTensorHiCOO.bptr"]) == S.HiCOOS.bptr.offset
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/include"), reason="reference headers not present")
+@pytest.mark.skipif(not os.path.isdir(os.path.join(O.REF_SRC, "include")), reason="reference headers not present")
 def test_struct_layouts_equal_reference():
     ours = layout(os.path.join(ROOT, "include"))
-    ref = layout("/root/reference/include", ["-DPARTI_INDEX_TYPEWIDTH=32", "-DPARTI_VALUE_TYPEWIDTH=32",
+    ref = layout(os.path.join(O.REF_SRC, "include"), ["-DPARTI_INDEX_TYPEWIDTH=32", "-DPARTI_VALUE_TYPEWIDTH=32",
                                              "-DPARTI_ELEMENT_INDEX_TYPEWIDTH=8", "-DPARTI_USE_OPENMP", "-fopenmp"])
     assert ours == ref

@@ -2,7 +2,7 @@
 own outputs (tests/golden) and the oracle.
 
 Tolerance: relative Frobenius error <= 1e-5 against the reference's
-sequential FP32 sptMTTKRP (the spec criterion); against the FP64 oracle
+sequential FP32 sptMTTKRP (the required tolerance); against the FP64 oracle
 where the reference's own FP32 summation error would dominate.
 """
 import numpy as np
