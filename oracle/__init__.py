@@ -141,6 +141,15 @@ def _rows(arrs, ptype, dtype):
     return arrs, p
 
 
+def _check_mats(mats, ndims, stride):
+    """The C routines read ndims[m] rows of `stride` floats from each factor."""
+    for m, a in enumerate(mats):
+        a = np.asarray(a)
+        if a.ndim != 2 or a.shape[1] < stride or a.shape[0] < ndims[m]:
+            raise ValueError("factor %d must have ndims[%d] rows of at least %d (the padded stride) columns"
+                             % (m, m, stride))
+
+
 def _default_order(N, mode):
     return [mode] + [(mode + i) % N for i in range(1, N)]
 
@@ -208,6 +217,7 @@ def mttkrp(ndims, inds, vals, mats, rank, mode, order=None, precision="f32", tk=
     N, n = inds.shape
     order = _default_order(N, mode) if order is None else order
     stride = stride_of(rank)
+    _check_mats(mats, ndims, stride)
     keep, ip = _rows(list(inds), u32p, np.uint32)
     mkeep, mp = _rows(mats, f32p, np.float32)
     v = np.ascontiguousarray(vals, np.float32)
@@ -259,6 +269,7 @@ def omp_mttkrp_hicoo_reduce(ndims, h, vals, sb_bits, mats, rank, mode, tk, ks_ro
     stride = stride_of(rank)
     bk, bp = _rows(list(h["binds"]), u32p, np.uint32)
     ek, ep = _rows(list(h["einds"]), u8p, np.uint8)
+    _check_mats(mats, ndims, stride)
     mkeep, mp = _rows(mats, f32p, np.float32)
     v = np.ascontiguousarray(vals, np.float32)
     bptr = np.ascontiguousarray(h["bptr"], np.uint64)
@@ -285,6 +296,7 @@ def mttkrp_hicoo(ndims, h, vals, sb_bits, mats, rank, mode, order=None):
     stride = stride_of(rank)
     bk, bp = _rows(list(h["binds"]), u32p, np.uint32)
     ek, ep = _rows(list(h["einds"]), u8p, np.uint8)
+    _check_mats(mats, ndims, stride)
     mkeep, mp = _rows(mats, f32p, np.float32)
     v = np.ascontiguousarray(vals, np.float32)
     bptr = np.ascontiguousarray(h["bptr"], np.uint64)

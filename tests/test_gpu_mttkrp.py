@@ -240,8 +240,8 @@ def test_orders_2_5_6_8_against_fp64(ndims, entry):
         assert rel_fro(out, ref) <= TOL, (ndims, mode)
 
 
-@pytest.mark.parametrize("shuffled", [False, True])
-def test_chunked_result_copy_with_a_row_across_chunks(shuffled):
+@pytest.mark.parametrize("shuffled,rank", [(False, 16), (True, 16), (True, 17), (False, 64)])
+def test_chunked_result_copy_with_a_row_across_chunks(shuffled, rank):
     """Order 3, >= 4M nonzeros through the host-buffer entry: the kernel runs
     in unit ranges and finished rows are copied back while later ranges run.
     One row holds ~30% of the nonzeros, so it crosses range boundaries;
@@ -257,11 +257,13 @@ def test_chunked_result_copy_with_a_row_across_chunks(shuffled):
         order = rng.permutation(n)
     inds = np.ascontiguousarray(inds[:, order])
     vals = rng.uniform(-1, 1, n).astype(np.float32)
-    rank = 16
-    facs = [rng.uniform(-1, 1, (d, rank)).astype(np.float32) for d in ndims]
     t = S.Tensor.from_arrays(ndims, inds, vals)
-    mats = [S.Matrix.from_array(f) for f in facs] + [S.Matrix(max(ndims), rank)]
+    mats = [S.Matrix.from_array(rng.uniform(-1, 1, (d, rank)).astype(np.float32)) for d in ndims]
+    mats.append(S.Matrix(max(ndims), rank))
+    facs = [m.array()[: ndims[k]].copy() for k, m in enumerate(mats[:3])]   # stride-padded rows
     for mode in range(3):
         out = S.mttkrp(t, mats, mode, entry="sptCudaMTTKRP")
         ref = O.mttkrp(ndims, inds, vals, facs, rank, mode, precision="f64_omp")
         assert rel_fro(out, ref) <= TOL, mode
+        # padding columns of the output stay zero
+        assert not mats[3].array()[: ndims[mode], rank:].any()
