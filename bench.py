@@ -94,6 +94,16 @@ def spec_for(count, seed=SEED):
     return s
 
 
+def workload_config(nnz, world):
+    """The workload both arms report: the 100M-nonzero power-law tensor at
+    rank 32 (the reference arm times a bounded sample of it, described in its
+    cpu_baseline)."""
+    return {"workload": "mttkrp_powerlaw_coo_4Mx2Mx25K_100Mnnz_rank32", "dims": DIMS, "nnz": nnz,
+            "zipf": ZIPF, "values": "lognormal(0,1)", "rank": RANK, "modes_per_step": 3,
+            "l2": "inputs larger than L2 (1.6 GB nonzero stream per launch)",
+            "parallelism": "replicas" if world > 1 else "single"}
+
+
 def algo_bytes(ndims, nnz, rank):
     N = len(ndims)
     return nnz * (4 * N + 4) + sum(d * rank * 4 for d in ndims)
@@ -535,8 +545,7 @@ def run_reference(args, world, rank):
         "metric": METRIC, "value": round(gbs, 3), "unit": "GB/s", "n_gpus": args.gpus, "steps": steps,
         "warmup": warm, "ms_per_step": secs * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
-        "config": {"workload": "mttkrp_powerlaw_coo_4Mx2Mx25K_rank32_sample", "nnz": t.nnz,
-                   "dims": DIMS, "zipf": ZIPF, "values": "lognormal(0,1)", "rank": RANK},
+        "config": workload_config(args.nnz, args.gpus),
         "cpu_baseline": {"value": round(gbs, 3), "unit": "GB/s", "cores": threads, "kind": kind,
                          "sample": "%d-nnz tensor of the workload's shape and distributions, 3 modes per step, "
                                    "sptOmpMTTKRP_Reduce, %d threads" % (t.nnz, threads)},
@@ -687,10 +696,7 @@ def run_ours(args, world, rank, local):
             "metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": world, "steps": K,
             "warmup": args.warmup, "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "mttkrp_powerlaw_coo_4Mx2Mx25K_100Mnnz_rank32", "dims": ndims, "nnz": nnz,
-                       "zipf": ZIPF, "values": "lognormal(0,1)", "rank": RANK, "modes_per_step": 3,
-                       "l2": "inputs larger than L2 (1.6 GB nonzero stream per launch)",
-                       "parallelism": "replicas" if world > 1 else "single"},
+            "config": workload_config(nnz, world),
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": peak_kind,
                          "kernel": "k_mttkrp_rec (order-3 record kernel) after the output memset, one launch per mode",
