@@ -144,6 +144,19 @@ typedef struct {
 
 typedef struct { sptIndex key; sptIndex value; } sptKeyValuePair;
 
+/* OpenMP lock pool (structs.h:228-238, locks.c:21-55): `locks` holds
+ * nlocks * padsize omp_lock_t, lock i at (i % nlocks) * padsize.  Callers of
+ * sptOmpMTTKRP_Lock create one; the library itself takes no lock in it. */
+typedef struct {
+    bool initialized;
+    sptIndex nlocks;
+    sptIndex padsize;
+    void *locks;
+} sptMutexPool;
+sptMutexPool *sptMutexAlloc(void);
+sptMutexPool *SptMutexAllocCustom(sptIndex const num_locks, sptIndex const pad_size);
+void sptMutexFree(sptMutexPool *pool);
+
 /* Semi-sparse tensor (structs.h:167-175): mode `mode` dense, the others
  * sparse; nnz dense fibers of `stride` values (ndims[mode] rounded up to 8),
  * inds[m] the fiber coordinates for m != mode (inds[mode] unused). */
@@ -268,6 +281,9 @@ int sptOmpMTTKRP(sptSparseTensor const *const X, sptMatrix *mats[], sptIndex con
                  sptIndex const mode, const int tk);
 int sptOmpMTTKRP_Reduce(sptSparseTensor const *const X, sptMatrix *mats[], sptMatrix *copy_mats[],
                         sptIndex const mats_order[], sptIndex const mode, const int tk);
+/* mttkrp_omp.c:255-395; the lock pool is not used (the product runs on the GPU). */
+int sptOmpMTTKRP_Lock(sptSparseTensor const *const X, sptMatrix *mats[], sptIndex const mats_order[],
+                      sptIndex const mode, const int tk, sptMutexPool *lock_pool);
 int sptCudaMTTKRP(sptSparseTensor const *const X, sptMatrix *mats[], sptIndex *const mats_order,
                   sptIndex const mode, sptIndex const impl_num);
 int sptCudaMTTKRPOneKernel(sptSparseTensor const *const X, sptMatrix **const mats, sptIndex *const mats_order,
@@ -276,6 +292,19 @@ int sptMTTKRPHiCOO(sptSparseTensorHiCOO const *const hitsr, sptMatrix *mats[], s
                    sptIndex const mode);
 int sptOmpMTTKRPHiCOO(sptSparseTensorHiCOO const *const hitsr, sptMatrix *mats[], sptIndex const mats_order[],
                       sptIndex const mode, const int nt);
+/* The rank-matrix forms (hicoo/mttkrp.c:158-245, hicoo/mttkrp_omp.c:158-212, :555-680, :1214-1351):
+ * the same product with sptRankMatrix factors and output; thread counts, the
+ * reduction copies and `balanced` are not used. */
+int sptMTTKRPHiCOO_MatrixTiling(sptSparseTensorHiCOO const *const hitsr, sptRankMatrix *mats[],
+                                sptIndex const mats_order[], sptIndex const mode);
+int sptOmpMTTKRPHiCOO_MatrixTiling(sptSparseTensorHiCOO const *const hitsr, sptRankMatrix *mats[],
+                                   sptIndex const mats_order[], sptIndex const mode, const int nt);
+int sptOmpMTTKRPHiCOO_MatrixTiling_Scheduled(sptSparseTensorHiCOO const *const hitsr, sptRankMatrix *mats[],
+                                             sptIndex const mats_order[], sptIndex const mode, const int tk,
+                                             int balanced);
+int sptOmpMTTKRPHiCOO_MatrixTiling_Scheduled_Reduce(sptSparseTensorHiCOO const *const hitsr, sptRankMatrix *mats[],
+                                                    sptRankMatrix *copy_mats[], sptIndex const mats_order[],
+                                                    sptIndex const mode, const int tk, int balanced);
 
 /* Semi-sparse tensors and sparse tensor times matrix (ssptensors.h:26-31,
  * sptensors.h:136-139): Y = X x_mode U, one dense fiber of U->ncols values per

@@ -126,6 +126,18 @@ def _declare(L):
         "sptFreeMatrix": (None, [M]),
         "sptMTTKRP": (C.c_int, [T, MM, u32p, C.c_uint32]),
         "sptOmpMTTKRP": (C.c_int, [T, MM, u32p, C.c_uint32, C.c_int]),
+        "sptOmpMTTKRP_Lock": (C.c_int, [T, MM, u32p, C.c_uint32, C.c_int, C.c_void_p]),
+        "sptMutexAlloc": (C.c_void_p, []),
+        "SptMutexAllocCustom": (C.c_void_p, [C.c_uint32, C.c_uint32]),
+        "sptMutexFree": (None, [C.c_void_p]),
+        "sptMTTKRPHiCOO_MatrixTiling": (C.c_int, [H, C.POINTER(C.POINTER(RankMatrixS)), u32p, C.c_uint32]),
+        "sptOmpMTTKRPHiCOO_MatrixTiling": (C.c_int, [H, C.POINTER(C.POINTER(RankMatrixS)), u32p, C.c_uint32,
+                                                      C.c_int]),
+        "sptOmpMTTKRPHiCOO_MatrixTiling_Scheduled": (C.c_int, [H, C.POINTER(C.POINTER(RankMatrixS)), u32p,
+                                                                C.c_uint32, C.c_int, C.c_int]),
+        "sptOmpMTTKRPHiCOO_MatrixTiling_Scheduled_Reduce": (C.c_int, [H, C.POINTER(C.POINTER(RankMatrixS)),
+                                                                       C.POINTER(C.POINTER(RankMatrixS)), u32p,
+                                                                       C.c_uint32, C.c_int, C.c_int]),
         "sptCudaMTTKRP": (C.c_int, [T, MM, u32p, C.c_uint32, C.c_uint32]),
         "sptSparseTensorSortIndex": (None, [T, C.c_int, C.c_int]),
         "sptSparseTensorSortIndexCustomOrder": (None, [T, u32p, C.c_int, C.c_int]),
@@ -384,6 +396,12 @@ def mttkrp(tensor, mats, mode, mats_order=None, entry="sptMTTKRP", copy=True):
         r = L.sptCudaMTTKRP(tensor.ptr(), arr, op, mode, 15)
     elif entry == "sptOmpMTTKRP":
         r = L.sptOmpMTTKRP(tensor.ptr(), arr, op, mode, 1)
+    elif entry == "sptOmpMTTKRP_Lock":
+        pool = L.sptMutexAlloc()
+        try:
+            r = L.sptOmpMTTKRP_Lock(tensor.ptr(), arr, op, mode, 4, pool)
+        finally:
+            L.sptMutexFree(pool)
     else:
         raise ValueError(entry)
     _check(r, entry)

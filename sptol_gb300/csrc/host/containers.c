@@ -12,6 +12,7 @@
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
+#include <omp.h>
 #include <string.h>
 #include "../sptgb_internal.h"
 #include "../../../include/sptgb.h"
@@ -494,4 +495,32 @@ void sptFreeKruskalTensor(sptKruskalTensor *k) {
     }
     k->factors = NULL;
     k->nmodes = 0;
+}
+
+/* ------------------------------------------------------ OpenMP lock pool -- */
+/* locks.c:21-55: nlocks * padsize locks, lock i initialised at (i % nlocks) * padsize. */
+sptMutexPool *SptMutexAllocCustom(sptIndex const num_locks, sptIndex const pad_size) {
+    sptMutexPool *pool = (sptMutexPool *)malloc(sizeof *pool);
+    if (!pool) return NULL;
+    pool->nlocks = num_locks;
+    pool->padsize = pad_size;
+    omp_lock_t *locks = (omp_lock_t *)malloc((size_t)num_locks * pad_size * sizeof(omp_lock_t));
+    if (!locks && num_locks) {
+        free(pool);
+        return NULL;
+    }
+    for (sptIndex l = 0; l < num_locks; ++l) omp_init_lock(locks + (size_t)l * pad_size);
+    pool->locks = locks;
+    pool->initialized = true;
+    return pool;
+}
+
+sptMutexPool *sptMutexAlloc(void) { return SptMutexAllocCustom(1024, 16); }
+
+void sptMutexFree(sptMutexPool *pool) {
+    if (!pool) return;
+    omp_lock_t *locks = (omp_lock_t *)pool->locks;
+    for (sptIndex l = 0; l < pool->nlocks; ++l) omp_destroy_lock(locks + (size_t)l * pool->padsize);
+    free(locks);
+    free(pool);
 }

@@ -425,6 +425,56 @@ int sptOmpMTTKRPHiCOO(sptSparseTensorHiCOO const *const hitsr, sptMatrix *mats[]
     return hicoo_mttkrp(hitsr, mats, mats_order, mode, "GPU HiCOO SpTns MTTKRP");
 }
 
+/* Rank-matrix factors and output, viewed as sptMatrix over the same rows. */
+static int hicoo_mttkrp_rank(sptSparseTensorHiCOO const *h, sptRankMatrix *mats[], sptIndex const *mats_order,
+                             sptIndex mode) {
+    const char *module = "GPU HiCOO SpTns MTTKRP";
+    const sptIndex N = h->nmodes;
+    if (N < 2 || N > SPTGB_MAX_MODES) {
+        spt_ComplainError(module, SPTERR_VALUE_ERROR, __FILE__, __LINE__, "unsupported order");
+        return SPTERR_VALUE_ERROR;
+    }
+    sptMatrix view[SPTGB_MAX_MODES + 1];
+    sptMatrix *pv[SPTGB_MAX_MODES + 1];
+    for (sptIndex i = 0; i <= N; ++i) {
+        view[i].nrows = mats[i]->nrows;
+        view[i].ncols = mats[i]->ncols;
+        view[i].cap = mats[i]->cap;
+        view[i].stride = mats[i]->stride;
+        view[i].values = mats[i]->values;
+        pv[i] = &view[i];
+    }
+    return hicoo_mttkrp(h, pv, mats_order, mode, module);
+}
+
+int sptMTTKRPHiCOO_MatrixTiling(sptSparseTensorHiCOO const *const hitsr, sptRankMatrix *mats[],
+                                sptIndex const mats_order[], sptIndex const mode) {
+    return hicoo_mttkrp_rank(hitsr, mats, mats_order, mode);
+}
+
+int sptOmpMTTKRPHiCOO_MatrixTiling(sptSparseTensorHiCOO const *const hitsr, sptRankMatrix *mats[],
+                                   sptIndex const mats_order[], sptIndex const mode, const int nt) {
+    (void)nt;
+    return hicoo_mttkrp_rank(hitsr, mats, mats_order, mode);
+}
+
+int sptOmpMTTKRPHiCOO_MatrixTiling_Scheduled(sptSparseTensorHiCOO const *const hitsr, sptRankMatrix *mats[],
+                                             sptIndex const mats_order[], sptIndex const mode, const int tk,
+                                             int balanced) {
+    (void)tk;
+    (void)balanced;
+    return hicoo_mttkrp_rank(hitsr, mats, mats_order, mode);
+}
+
+int sptOmpMTTKRPHiCOO_MatrixTiling_Scheduled_Reduce(sptSparseTensorHiCOO const *const hitsr, sptRankMatrix *mats[],
+                                                    sptRankMatrix *copy_mats[], sptIndex const mats_order[],
+                                                    sptIndex const mode, const int tk, int balanced) {
+    (void)copy_mats;
+    (void)tk;
+    (void)balanced;
+    return hicoo_mttkrp_rank(hitsr, mats, mats_order, mode);
+}
+
 /* ------------------------------------------------ resident HiCOO tensor -- */
 static int hicoo_window_ok(const sptgbHicoo *t, sptIndex stride) {
     return (t->nmodes == 3 || t->nmodes == 4) && t->nb && t->nnz < 0xffffffffull &&

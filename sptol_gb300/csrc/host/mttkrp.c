@@ -344,6 +344,13 @@ int sptOmpMTTKRP_Reduce(sptSparseTensor const *const X, sptMatrix *mats[], sptMa
     return mttkrp_host(X, mats, mats_order, mode, "GPU SpTns MTTKRP");
 }
 
+int sptOmpMTTKRP_Lock(sptSparseTensor const *const X, sptMatrix *mats[], sptIndex const mats_order[],
+                      sptIndex const mode, const int tk, sptMutexPool *lock_pool) {
+    (void)tk;
+    (void)lock_pool;
+    return mttkrp_host(X, mats, mats_order, mode, "GPU SpTns MTTKRP");
+}
+
 int sptCudaMTTKRP(sptSparseTensor const *const X, sptMatrix *mats[], sptIndex *const mats_order, sptIndex const mode,
                   sptIndex const impl_num) {
     (void)impl_num;

@@ -55,6 +55,7 @@ int main(void) {
   P(sptRankKruskalTensor) O(sptRankKruskalTensor, rank) O(sptRankKruskalTensor, lambda)
   O(sptRankKruskalTensor, fit) O(sptRankKruskalTensor, factors)
   O(sptRankMatrix, ncols) O(sptRankMatrix, cap) O(sptRankMatrix, stride) O(sptRankMatrix, values)
+  P(sptMutexPool) O(sptMutexPool, nlocks) O(sptMutexPool, padsize) O(sptMutexPool, locks)
   return 0;
 }
 """
@@ -86,3 +87,19 @@ def test_struct_layouts_equal_reference():
     ref = layout(os.path.join(O.REF_SRC, "include"), ["-DPARTI_INDEX_TYPEWIDTH=32", "-DPARTI_VALUE_TYPEWIDTH=32",
                                              "-DPARTI_ELEMENT_INDEX_TYPEWIDTH=8", "-DPARTI_USE_OPENMP", "-fopenmp"])
     assert ours == ref
+
+
+def test_mutex_pool_alloc_and_free():
+    """sptMutexAlloc / SptMutexAllocCustom / sptMutexFree (locks.c:21-55) need no GPU."""
+    L = S.lib()
+
+    class Pool(C.Structure):
+        _fields_ = [("initialized", C.c_bool), ("nlocks", C.c_uint32), ("padsize", C.c_uint32),
+                    ("locks", C.c_void_p)]
+    for alloc in (lambda: L.sptMutexAlloc(), lambda: L.SptMutexAllocCustom(7, 3)):
+        p = alloc()
+        assert p
+        pool = Pool.from_address(p)
+        assert pool.initialized and pool.locks
+        assert (pool.nlocks, pool.padsize) in ((1024, 16), (7, 3))
+        L.sptMutexFree(p)

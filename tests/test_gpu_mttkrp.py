@@ -25,7 +25,7 @@ def _with_out(mats, ndims, rank):
 
 
 @pytest.mark.parametrize("case", ["mttkrp_3d_r16", "mttkrp_3d_r17", "mttkrp_4d_r8"])
-@pytest.mark.parametrize("entry", ["sptMTTKRP", "sptCudaMTTKRP"])
+@pytest.mark.parametrize("entry", ["sptMTTKRP", "sptCudaMTTKRP", "sptOmpMTTKRP_Lock"])
 def test_golden_all_modes(case, entry):
     g = golden(case)
     ndims = [int(x) for x in g["ndims"]]

@@ -278,3 +278,48 @@ def test_inconsistent_block_pointers_are_rejected_then_a_valid_call():
         ref = O.mttkrp(ndims, i2, v2, facs, rank, mode, precision="f64")
         assert rel_fro(mats[3].array()[: ndims[mode], :rank], ref) <= 1e-5
     del keep
+
+
+@pytest.mark.parametrize("order", [3, 4])
+def test_rank_matrix_hicoo_entry_points(order):
+    """sptMTTKRPHiCOO_MatrixTiling and the OpenMP-named Scheduled / Reduce
+    forms take sptRankMatrix factors and output; every mode against FP64."""
+    if order == 3:
+        t = _skewed3(60_000, 31)
+    else:
+        spec = S.GenSpec()
+        spec.seed = 32
+        spec.nmodes = 4
+        for m, d in enumerate([3000, 700, 2000, 90]):
+            spec.ndims[m] = d
+        spec.count = 60_000
+        spec.value_dist = S.VAL_UPM1
+        t = S.Tensor.generate(spec)
+    ndims = t.ndims
+    N = len(ndims)
+    h = S.HiCOO(t, 7, 12)
+    i2, v2 = t.arrays()
+    rank = 24
+    rng = np.random.default_rng(33)
+    facs = [rng.uniform(-1, 1, (d, rank)).astype(np.float32) for d in ndims]
+    rmats = [S.RankMatrix.from_array(f) for f in facs] + [S.RankMatrix(max(ndims), rank)]
+    copies = [S.RankMatrix(max(ndims), rank) for _ in range(2)]
+    arr = (C.POINTER(S.RankMatrixS) * (N + 1))(*[C.pointer(m.s) for m in rmats])
+    carr = (C.POINTER(S.RankMatrixS) * 2)(*[C.pointer(m.s) for m in copies])
+    L = S.lib()
+    pad = [np.pad(f, ((0, 0), (0, rmats[0].s.stride - rank))) for f in facs]
+    for mode in range(N):
+        order_, op = S._u32([mode] + [(mode + i) % N for i in range(1, N)])
+        rmats[N].s.nrows = ndims[mode]
+        ref = O.mttkrp(ndims, i2, v2, pad, rank, mode, precision="f64")
+        for name, call in (
+                ("MatrixTiling", lambda: L.sptMTTKRPHiCOO_MatrixTiling(h.ptr(), arr, op, mode)),
+                ("Omp", lambda: L.sptOmpMTTKRPHiCOO_MatrixTiling(h.ptr(), arr, op, mode, 4)),
+                ("Scheduled", lambda: L.sptOmpMTTKRPHiCOO_MatrixTiling_Scheduled(h.ptr(), arr, op, mode, 4, 0)),
+                ("Reduce", lambda: L.sptOmpMTTKRPHiCOO_MatrixTiling_Scheduled_Reduce(h.ptr(), arr, carr, op, mode,
+                                                                                    2, 0))):
+            rmats[N].array()[:] = 7.0
+            assert call() == 0, name
+            out = rmats[N].array()[: ndims[mode], :rank]
+            assert rel_fro(out, ref) <= 1e-5, (name, mode)
+            assert not rmats[N].array()[: ndims[mode], rank:].any(), name
