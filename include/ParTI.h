@@ -326,10 +326,32 @@ int  sptCudaSparseTensorMulMatrixOneKernel(sptSemiSparseTensor *Y, sptSparseTens
  * indices (start_index based) and the value; parsed on the GPU, result equal
  * to the reference's (zero values removed as collect.c:29-49 does). */
 int sptLoadSparseTensor(sptSparseTensor *tsr, sptIndex start_index, FILE *fp);
+/* Text output in the reference's formats (sptensor/dump.c:29-52,
+ * matrix/dump.c:34-50, ktensor/dump.c:24-51; NULL factor pointers skipped). */
+int sptDumpSparseTensor(const sptSparseTensor *tsr, sptIndex start_index, FILE *fp);
+int sptDumpMatrix(sptMatrix *mtx, FILE *fp);
 
 /* ------------------------------------------------------ Kruskal / CP-ALS -- */
 int  sptNewKruskalTensor(sptKruskalTensor *ktsr, sptIndex nmodes, const sptIndex ndims[], sptIndex rank);
 void sptFreeKruskalTensor(sptKruskalTensor *ktsr);
+int  sptDumpKruskalTensor(sptKruskalTensor *ktsr, FILE *fp);
+
+/* The dense ALS pieces on caller matrices (ranks up to 64), on the GPU:
+ * Hadamard of the other Grams' upper triangles into mats[nmodes]
+ * (matrix.c:341-386, FP32 in the same order); the normal equations X G = rhs
+ * for every row of rhs, G that Hadamard (matrix_solver.c:32-83; FP64
+ * Cholesky, LU when G is not positive definite); column 2-norm and max-norm
+ * normalisation (matrix.c:390-554), GetFinalLambda (matrix.c:557-573); the
+ * fit and its parts (ktensor.c:102-257, the same triangles and formulas). */
+int    sptMatrixDotMulSeqTriangle(sptIndex const mode, sptIndex const nmodes, sptMatrix **mats);
+int    sptMatrixSolveNormals(sptIndex const mode, sptIndex const nmodes, sptMatrix **aTa, sptMatrix *rhs);
+int    sptMatrix2Norm(sptMatrix *const A, sptValue *const lambda);
+int    sptMatrixMaxNorm(sptMatrix *const A, sptValue *const lambda);
+void   GetFinalLambda(sptIndex const rank, sptIndex const nmodes, sptMatrix **mats, sptValue *const lambda);
+double sptKruskalTensorFit(sptSparseTensor const *const spten, sptValue const *const lambda, sptMatrix **mats,
+                           sptMatrix **ata);
+double sptKruskalTensorFrobeniusNormSquared(sptIndex const nmodes, sptValue const *const lambda, sptMatrix **ata);
+double sptSparseKruskalTensorInnerProduct(sptIndex const nmodes, sptValue const *const lambda, sptMatrix **mats);
 
 /* One CP-ALS run from caller-initialised factors mats[0..nmodes-1] (and a
  * scratch mats[nmodes] with max_dim rows); returns the last fit

@@ -128,6 +128,16 @@ def _declare(L):
         "sptOmpMTTKRP": (C.c_int, [T, MM, u32p, C.c_uint32, C.c_int]),
         "sptOmpMTTKRP_Lock": (C.c_int, [T, MM, u32p, C.c_uint32, C.c_int, C.c_void_p]),
         "sptMutexAlloc": (C.c_void_p, []),
+        "sptMatrixDotMulSeqTriangle": (C.c_int, [C.c_uint32, C.c_uint32, MM]),
+        "sptMatrixSolveNormals": (C.c_int, [C.c_uint32, C.c_uint32, MM, M]),
+        "sptMatrix2Norm": (C.c_int, [M, f32p]),
+        "sptMatrixMaxNorm": (C.c_int, [M, f32p]),
+        "GetFinalLambda": (None, [C.c_uint32, C.c_uint32, MM, f32p]),
+        "sptKruskalTensorFit": (C.c_double, [T, f32p, MM, MM]),
+        "sptKruskalTensorFrobeniusNormSquared": (C.c_double, [C.c_uint32, f32p, MM]),
+        "sptSparseKruskalTensorInnerProduct": (C.c_double, [C.c_uint32, f32p, MM]),
+        "sptDumpSparseTensor": (C.c_int, [T, C.c_uint32, C.c_void_p]),
+        "sptDumpMatrix": (C.c_int, [M, C.c_void_p]),
         "SptMutexAllocCustom": (C.c_void_p, [C.c_uint32, C.c_uint32]),
         "sptMutexFree": (None, [C.c_void_p]),
         "sptMTTKRPHiCOO_MatrixTiling": (C.c_int, [H, C.POINTER(C.POINTER(RankMatrixS)), u32p, C.c_uint32]),

@@ -158,3 +158,167 @@ extern "C" cudaError_t sptgb_f32_to_bf16(const float *in, uint16_t *out, uint64_
     sptgb_count_launch(1);
     return cudaGetLastError();
 }
+
+// --------------------------------------------------------------------------
+// The reference's dense helpers on caller matrices (FP32, `stride` floats per
+// row): sptMatrixDotMulSeqTriangle, sptMatrixMaxNorm,
+// sptKruskalTensorFrobeniusNormSquared, sptSparseKruskalTensorInnerProduct.
+namespace {
+
+struct F32Ptrs { const float *p[SPTGB_MAX_MODES]; };
+
+// matrix.c:341-386: the upper triangle (j >= i) of every mats[(mode+m) % N],
+// m = 1..N-1, multiplied in FP32 in that order, then mirrored.
+__global__ void k_hadamard_upper(F32Ptrs mats, int nmodes, int mode, int rank, int stride, float *__restrict__ out) {
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < rank * rank; e += gridDim.x * blockDim.x) {
+        const int i = e / rank, j = e % rank;
+        if (j < i) continue;
+        float v = 1.f;
+        for (int m = 1; m < nmodes; ++m) v = __fmul_rn(v, mats.p[(mode + m) % nmodes][i * stride + j]);
+        out[i * stride + j] = v;
+        out[j * stride + i] = v;
+    }
+}
+
+// FP64 R x R copies of the caller's Grams from their upper triangles (the
+// triangle the reference's solve reads), for the FP64 factorisation.
+__global__ void k_grams_upper_f64(F32Ptrs mats, int nmodes, int rank, int stride, double *__restrict__ out) {
+    const int RR = rank * rank;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nmodes * RR; e += gridDim.x * blockDim.x) {
+        const int m = e / RR, i = (e % RR) / rank, j = e % rank;
+        const int a = i < j ? i : j, b = i < j ? j : i;
+        out[e] = (double)mats.p[m][a * stride + b];
+    }
+}
+
+// ktensor.c:126-168, one thread: tmp = 1 over rank x stride, entries
+// (row j, column i), j >= i, multiplied over every mode in FP32; then the
+// lambda-weighted sum over those entries in the reference's order (i outer,
+// j inner; FP32 terms added to an FP64 sum), absolute value.
+__global__ void k_kruskal_normsq(F32Ptrs ata, int nmodes, int rank, int stride, const float *__restrict__ lambda,
+                                 float *__restrict__ tmp, double *__restrict__ out) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    for (int x = 0; x < rank * stride; ++x) tmp[x] = 1.f;
+    for (int m = 0; m < nmodes; ++m)
+        for (int i = 0; i < rank; ++i)
+            for (int j = i; j < rank; ++j) tmp[j * stride + i] = __fmul_rn(tmp[j * stride + i], ata.p[m][j * stride + i]);
+    double norm = 0.0;
+    for (int i = 0; i < rank; ++i) {
+        norm += (double)__fmul_rn(__fmul_rn(tmp[i + i * stride], lambda[i]), lambda[i]);
+        for (int j = i + 1; j < rank; ++j)
+            norm += (double)__fmul_rn(__fmul_rn(__fmul_rn(tmp[i + j * stride], lambda[i]), lambda[j]), 2.f);
+    }
+    *out = fabs(norm);
+}
+
+// Per-block column maxima (signed, starting at 0 as matrix.c:484-486).
+__global__ void k_colmax_partial(const float *__restrict__ A, uint32_t nrows, int rank, int stride,
+                                 float *__restrict__ part) {
+    for (int j = threadIdx.x; j < rank; j += blockDim.x) {
+        float mx = 0.f;
+        for (uint64_t i = blockIdx.x; i < nrows; i += gridDim.x) {
+            const float v = A[i * stride + j];
+            if (v > mx) mx = v;
+        }
+        part[(uint64_t)blockIdx.x * rank + j] = mx;
+    }
+}
+
+// lambda[j] = max over blocks, clamped to >= 1 (matrix.c:541-547).
+__global__ void k_colmax_final(const float *__restrict__ part, int nb, int rank, float *__restrict__ lambda) {
+    for (int j = threadIdx.x; j < rank; j += blockDim.x) {
+        float mx = 0.f;
+        for (int b = 0; b < nb; ++b)
+            if (part[(uint64_t)b * rank + j] > mx) mx = part[(uint64_t)b * rank + j];
+        lambda[j] = mx < 1.f ? 1.f : mx;
+    }
+}
+
+// Per-block sum over rows of the FP32 products A[i][r] * B[i][r] in FP64
+// (ktensor.c:203-236).
+__global__ void k_rowdot_partial(const float *__restrict__ A, const float *__restrict__ B, uint32_t nrows, int rank,
+                                 int stride, double *__restrict__ part) {
+    for (int r = threadIdx.x; r < rank; r += blockDim.x) {
+        double acc = 0.0;
+        for (uint64_t i = blockIdx.x; i < nrows; i += gridDim.x)
+            acc += (double)__fmul_rn(A[i * stride + r], B[i * stride + r]);
+        part[(uint64_t)blockIdx.x * rank + r] = acc;
+    }
+}
+
+// inner = sum_r (sum over blocks) * lambda[r] (ktensor.c:238-241).
+__global__ void k_rowdot_final(const double *__restrict__ part, int nb, int rank, const float *__restrict__ lambda,
+                               double *__restrict__ out) {
+    if (threadIdx.x != 0) return;
+    double inner = 0.0;
+    for (int r = 0; r < rank; ++r) {
+        double acc = 0.0;
+        for (int b = 0; b < nb; ++b) acc += part[(uint64_t)b * rank + r];
+        inner += acc * (double)lambda[r];
+    }
+    *out = inner;
+}
+
+int rows_blocks(uint32_t nrows) {
+    uint32_t nb = nrows < (uint32_t)NBLK ? nrows : (uint32_t)NBLK;
+    return nb ? (int)nb : 1;
+}
+
+}  // namespace
+
+extern "C" cudaError_t sptgb_hadamard_upper(const float *const *mats, int nmodes, int mode, int rank, int stride,
+                                            float *out, cudaStream_t s) {
+    if (nmodes < 1 || nmodes > SPTGB_MAX_MODES || rank < 1) return cudaErrorInvalidValue;
+    F32Ptrs p;
+    for (int m = 0; m < SPTGB_MAX_MODES; ++m) p.p[m] = m < nmodes ? mats[m] : nullptr;
+    k_hadamard_upper<<<(rank * rank + 255) / 256, 256, 0, s>>>(p, nmodes, mode, rank, stride, out);
+    sptgb_count_launch(1);
+    return cudaGetLastError();
+}
+
+extern "C" cudaError_t sptgb_grams_upper_f64(const float *const *mats, int nmodes, int rank, int stride, double *out,
+                                             cudaStream_t s) {
+    if (nmodes < 1 || nmodes > SPTGB_MAX_MODES || rank < 1) return cudaErrorInvalidValue;
+    F32Ptrs p;
+    for (int m = 0; m < SPTGB_MAX_MODES; ++m) p.p[m] = m < nmodes ? mats[m] : nullptr;
+    k_grams_upper_f64<<<(nmodes * rank * rank + 255) / 256, 256, 0, s>>>(p, nmodes, rank, stride, out);
+    sptgb_count_launch(1);
+    return cudaGetLastError();
+}
+
+extern "C" cudaError_t sptgb_kruskal_normsq(const float *const *ata, int nmodes, int rank, int stride,
+                                            const float *lambda, float *tmp, double *out, cudaStream_t s) {
+    if (nmodes < 1 || nmodes > SPTGB_MAX_MODES || rank < 1) return cudaErrorInvalidValue;
+    F32Ptrs p;
+    for (int m = 0; m < SPTGB_MAX_MODES; ++m) p.p[m] = m < nmodes ? ata[m] : nullptr;
+    k_kruskal_normsq<<<1, 32, 0, s>>>(p, nmodes, rank, stride, lambda, tmp, out);
+    sptgb_count_launch(1);
+    return cudaGetLastError();
+}
+
+// ws: at least rows_blocks(nrows) * rank floats.
+extern "C" cudaError_t sptgb_colmax_scale(float *A, uint32_t nrows, int rank, int stride, float *lambda, float *ws,
+                                          cudaStream_t s) {
+    if (rank < 1) return cudaErrorInvalidValue;
+    const int nb = rows_blocks(nrows);
+    k_colmax_partial<<<nb, 64, 0, s>>>(A, nrows, rank, stride, ws);
+    k_colmax_final<<<1, 64, 0, s>>>(ws, nb, rank, lambda);
+    uint64_t total = (uint64_t)nrows * (stride / 4);
+    uint64_t g = (total + 255) / 256;
+    if (g > 152 * 16) g = 152 * 16;
+    if (g < 1) g = 1;
+    k_scale_cols<<<(unsigned)g, 256, 0, s>>>(A, nrows, rank, stride, lambda);
+    sptgb_count_launch(3);
+    return cudaGetLastError();
+}
+
+// ws: at least rows_blocks(nrows) * rank doubles.
+extern "C" cudaError_t sptgb_rowdot(const float *A, const float *B, uint32_t nrows, int rank, int stride,
+                                    const float *lambda, double *out, double *ws, cudaStream_t s) {
+    if (rank < 1) return cudaErrorInvalidValue;
+    const int nb = rows_blocks(nrows);
+    k_rowdot_partial<<<nb, 64, 0, s>>>(A, B, nrows, rank, stride, ws);
+    k_rowdot_final<<<1, 32, 0, s>>>(ws, nb, rank, lambda, out);
+    sptgb_count_launch(2);
+    return cudaGetLastError();
+}

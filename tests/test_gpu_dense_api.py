@@ -1,0 +1,123 @@
+"""The reference's dense ALS helpers on caller matrices, on the GPU:
+sptMatrixDotMulSeqTriangle (bit-exact FP32, same product order),
+sptMatrixSolveNormals, sptMatrix2Norm / sptMatrixMaxNorm / GetFinalLambda and
+the fit and its parts, against numpy restatements of matrix.c / ktensor.c."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import sptol_gb300 as S
+from conftest import rel_fro
+
+pytestmark = pytest.mark.gpu
+
+
+def _arr(mats):
+    return (C.POINTER(S.MatrixS) * len(mats))(*[C.pointer(m.s) for m in mats])
+
+
+def _grams(rng, N, rank, upper_only=True):
+    gs = []
+    for _ in range(N):
+        a = rng.uniform(0, 1, (rng.integers(rank + 5, 4 * rank + 5), rank)).astype(np.float32)
+        g = (a.T.astype(np.float64) @ a).astype(np.float32)
+        if upper_only:
+            g[np.tril_indices(rank, -1)] = np.float32(7e3)   # never read
+        gs.append(g)
+    return gs
+
+
+@pytest.mark.parametrize("N,rank,mode", [(3, 16, 0), (3, 24, 2), (4, 64, 1)])
+def test_dot_mul_seq_triangle_bitexact(N, rank, mode):
+    rng = np.random.default_rng(N * 100 + rank)
+    gs = _grams(rng, N, rank)
+    mats = [S.Matrix.from_array(g) for g in gs] + [S.Matrix(rank, rank)]
+    assert S.lib().sptMatrixDotMulSeqTriangle(mode, N, _arr(mats)) == 0
+    exp = np.ones((rank, rank), np.float32)
+    for m in range(1, N):
+        pm = (mode + m) % N
+        for i in range(rank):
+            exp[i, i:] = exp[i, i:] * gs[pm][i, i:]
+    exp = np.triu(exp) + np.triu(exp, 1).T
+    assert np.array_equal(mats[N].array()[:rank, :rank], exp)
+
+
+@pytest.mark.parametrize("N,rank,mode", [(3, 16, 1), (4, 32, 3)])
+def test_solve_normals(N, rank, mode):
+    rng = np.random.default_rng(7 + rank)
+    gs = _grams(rng, N, rank)
+    mats = [S.Matrix.from_array(g) for g in gs] + [S.Matrix(rank, rank)]
+    rhs_a = rng.uniform(-1, 1, (500, rank)).astype(np.float32)
+    rhs = S.Matrix.from_array(rhs_a)
+    assert S.lib().sptMatrixSolveNormals(mode, N, _arr(mats), C.byref(rhs.s)) == 0
+    up = [np.triu(g.astype(np.float64)) for g in gs]
+    full = [u + np.triu(u, 1).T for u in up]
+    H = np.ones((rank, rank))
+    for m in range(1, N):
+        H *= full[(mode + m) % N]
+    X = np.linalg.solve(H, rhs_a.astype(np.float64).T).T
+    assert rel_fro(rhs.array()[:500, :rank], X) <= 1e-5
+    # aTa[N] holds the Hadamard, as sptMatrixDotMulSeqTriangle leaves it
+    assert rel_fro(mats[N].array()[:rank, :rank], H) <= 1e-6
+
+
+def test_norms_and_final_lambda():
+    rng = np.random.default_rng(3)
+    rank = 20
+    a = rng.uniform(-2, 3, (3000, rank)).astype(np.float32)
+    L = S.lib()
+    m = S.Matrix.from_array(a)
+    lam = np.zeros(rank, np.float32)
+    assert L.sptMatrix2Norm(C.byref(m.s), lam.ctypes.data_as(S.f32p)) == 0
+    n2 = np.sqrt((a.astype(np.float64) ** 2).sum(0))
+    assert np.allclose(lam, n2, rtol=1e-6)
+    assert np.allclose(m.array()[:3000, :rank], a / n2, rtol=1e-6)
+    m = S.Matrix.from_array(a)
+    assert L.sptMatrixMaxNorm(C.byref(m.s), lam.ctypes.data_as(S.f32p)) == 0
+    mx = np.maximum(np.maximum(a.max(0), 0), 1)
+    assert np.array_equal(lam, mx.astype(np.float32))
+    assert np.allclose(m.array()[:3000, :rank], a / mx, rtol=1e-6)
+    # GetFinalLambda: lambda *= the 2-norms of every factor
+    fs = [rng.uniform(0, 1, (n, rank)).astype(np.float32) for n in (700, 500, 90)]
+    ms = [S.Matrix.from_array(f) for f in fs]
+    lam = rng.uniform(1, 2, rank).astype(np.float32)
+    exp = lam.astype(np.float64).copy()
+    for f in fs:
+        exp *= np.sqrt((f.astype(np.float64) ** 2).sum(0))
+    L.GetFinalLambda(rank, 3, _arr(ms), lam.ctypes.data_as(S.f32p))
+    assert np.allclose(lam, exp, rtol=1e-5)
+
+
+def test_fit_and_parts():
+    rng = np.random.default_rng(5)
+    ndims = [60, 50, 40]
+    rank = 8
+    inds = np.stack([rng.integers(0, d, 3000) for d in ndims]).astype(np.uint32)
+    vals = rng.uniform(0, 1, 3000).astype(np.float32)
+    t = S.Tensor.from_arrays(ndims, inds, vals)
+    facs = [rng.uniform(0, 1, (d, rank)).astype(np.float32) for d in ndims]
+    lam = rng.uniform(0.5, 2, rank).astype(np.float32)
+    mats = [S.Matrix.from_array(f) for f in facs] + [S.Matrix(max(ndims), rank)]
+    # mats[N]: the last mode's MTTKRP output
+    out = S.mttkrp(t, mats, 2)
+    grams = [f.astype(np.float64).T @ f for f in facs]
+    ata = [S.Matrix.from_array(g.astype(np.float32)) for g in grams] + [S.Matrix(rank, rank)]
+    L = S.lib()
+    lp = lam.ctypes.data_as(S.f32p)
+    # ||K||^2 from the (row j, column i), j >= i, entries, as ktensor.c:126-168
+    tmp = np.ones((rank, rank), np.float64)
+    for g in grams:
+        tmp *= g.astype(np.float32)
+    nk = sum(tmp[i, i] * lam[i] * lam[i] for i in range(rank)) + \
+        2 * sum(tmp[j, i] * lam[i] * lam[j] for i in range(rank) for j in range(i + 1, rank))
+    got = L.sptKruskalTensorFrobeniusNormSquared(3, lp, _arr(ata))
+    assert abs(got - nk) <= 1e-5 * abs(nk)
+    inner = float((facs[2].astype(np.float64) * out.astype(np.float64)).sum(0) @ lam)
+    got_inner = L.sptSparseKruskalTensorInnerProduct(3, lp, _arr(mats))
+    assert abs(got_inner - inner) <= 1e-5 * abs(inner)
+    nx = float((vals.astype(np.float64) ** 2).sum())
+    res = nx + nk - 2 * inner
+    exp_fit = 1 - (np.sqrt(res) if res > 0 else res) / np.sqrt(nx)
+    fit = L.sptKruskalTensorFit(t.ptr(), lp, _arr(mats), _arr(ata))
+    assert abs(fit - exp_fit) <= 1e-5
