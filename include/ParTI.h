@@ -330,6 +330,16 @@ int sptLoadSparseTensor(sptSparseTensor *tsr, sptIndex start_index, FILE *fp);
  * matrix/dump.c:34-50, ktensor/dump.c:24-51; NULL factor pointers skipped). */
 int sptDumpSparseTensor(const sptSparseTensor *tsr, sptIndex start_index, FILE *fp);
 int sptDumpMatrix(sptMatrix *mtx, FILE *fp);
+/* vector/dump.c:32-176 ("<type> length: n", entries tab-separated) and
+ * sptensor/hicoo/dump.c:28-72 (every HiCOO array in that layout). */
+int sptDumpElementIndexVector(sptElementIndexVector *vec, FILE *fp);
+int sptDumpIndexVector(sptIndexVector *vec, FILE *fp);
+int sptDumpBlockIndexVector(sptBlockIndexVector *vec, FILE *fp);
+int sptDumpNnzIndexVector(sptNnzIndexVector *vec, FILE *fp);
+int sptDumpValueIndexVector(sptValueVector *vec, FILE *fp);
+int sptDumpIndexArray(sptIndex *array, sptNnzIndex const n, FILE *fp);
+int sptDumpNnzIndexArray(sptNnzIndex *array, sptNnzIndex const n, FILE *fp);
+int sptDumpSparseTensorHiCOO(sptSparseTensorHiCOO *const hitsr, FILE *fp);
 
 /* ------------------------------------------------------ Kruskal / CP-ALS -- */
 int  sptNewKruskalTensor(sptKruskalTensor *ktsr, sptIndex nmodes, const sptIndex ndims[], sptIndex rank);
@@ -373,6 +383,26 @@ void sptFreeRankMatrix(sptRankMatrix *mtx);
 int  sptNewRankKruskalTensor(sptRankKruskalTensor *ktsr, sptIndex nmodes, const sptIndex ndims[],
                              sptElementIndex rank);
 void sptFreeRankKruskalTensor(sptRankKruskalTensor *ktsr);
+int  sptDumpRankMatrix(sptRankMatrix *mtx, FILE *fp);
+int  sptDumpRankKruskalTensor(sptRankKruskalTensor *ktsr, FILE *fp);
+
+/* The dense ALS helpers on rank matrices (rankmatrix.c:137-378,
+ * rankmatrix_solver.c:32-84, rankktensor.c:101-257): the same results as
+ * the sptMatrix forms above; sptKruskalTensorFitHiCOO is sptKruskalTensorFit
+ * with the HiCOO tensor's norm. */
+int    sptRankMatrixDotMulSeqTriangle(sptIndex const mode, sptIndex const nmodes, sptRankMatrix **mats);
+int    sptRankMatrixSolveNormals(sptIndex const mode, sptIndex const nmodes, sptRankMatrix **aTa,
+                                 sptRankMatrix *rhs);
+int    sptRankMatrix2Norm(sptRankMatrix *const A, sptValue *const lambda);
+int    sptRankMatrixMaxNorm(sptRankMatrix *const A, sptValue *const lambda);
+void   GetRankFinalLambda(sptElementIndex const rank, sptIndex const nmodes, sptRankMatrix **mats,
+                          sptValue *const lambda);
+double sptKruskalTensorFitHiCOO(sptSparseTensorHiCOO const *const hitsr, sptValue const *const lambda,
+                                sptRankMatrix **mats, sptRankMatrix **ata);
+double sptKruskalTensorFrobeniusNormSquaredRank(sptIndex const nmodes, sptValue const *const lambda,
+                                                sptRankMatrix **ata);
+double sptSparseKruskalTensorInnerProductRank(sptIndex const nmodes, sptValue const *const lambda,
+                                              sptRankMatrix **mats);
 
 /* CP-ALS over a HiCOO tensor (cpds.h:46-59, src/sptensor/hicoo/cpd.c:149-195):
  * the same loop with the HiCOO MTTKRP; factors are rank matrices.  The

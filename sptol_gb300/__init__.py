@@ -114,6 +114,8 @@ def _declare(L):
     M = C.POINTER(MatrixS)
     MM = C.POINTER(M)
     H = C.POINTER(HiCOOS)
+    RM = C.POINTER(RankMatrixS)
+    RMM = C.POINTER(RM)
     sig = {
         "sptGetLastError": (C.c_int, [C.POINTER(C.c_char_p), C.POINTER(C.c_char_p), C.POINTER(C.c_uint),
                                       C.POINTER(C.c_char_p)]),
@@ -138,6 +140,20 @@ def _declare(L):
         "sptSparseKruskalTensorInnerProduct": (C.c_double, [C.c_uint32, f32p, MM]),
         "sptDumpSparseTensor": (C.c_int, [T, C.c_uint32, C.c_void_p]),
         "sptDumpMatrix": (C.c_int, [M, C.c_void_p]),
+        "sptDumpSparseTensorHiCOO": (C.c_int, [H, C.c_void_p]),
+        "sptDumpRankMatrix": (C.c_int, [RM, C.c_void_p]),
+        "sptDumpRankKruskalTensor": (C.c_int, [C.POINTER(RankKruskalS), C.c_void_p]),
+        "sptDumpKruskalTensor": (C.c_int, [C.POINTER(KruskalS), C.c_void_p]),
+        "sptDumpIndexArray": (C.c_int, [u32p, C.c_uint64, C.c_void_p]),
+        "sptDumpNnzIndexArray": (C.c_int, [u64p, C.c_uint64, C.c_void_p]),
+        "sptRankMatrixDotMulSeqTriangle": (C.c_int, [C.c_uint32, C.c_uint32, RMM]),
+        "sptRankMatrixSolveNormals": (C.c_int, [C.c_uint32, C.c_uint32, RMM, RM]),
+        "sptRankMatrix2Norm": (C.c_int, [RM, f32p]),
+        "sptRankMatrixMaxNorm": (C.c_int, [RM, f32p]),
+        "GetRankFinalLambda": (None, [C.c_uint8, C.c_uint32, RMM, f32p]),
+        "sptKruskalTensorFitHiCOO": (C.c_double, [H, f32p, RMM, RMM]),
+        "sptKruskalTensorFrobeniusNormSquaredRank": (C.c_double, [C.c_uint32, f32p, RMM]),
+        "sptSparseKruskalTensorInnerProductRank": (C.c_double, [C.c_uint32, f32p, RMM]),
         "SptMutexAllocCustom": (C.c_void_p, [C.c_uint32, C.c_uint32]),
         "sptMutexFree": (None, [C.c_void_p]),
         "sptMTTKRPHiCOO_MatrixTiling": (C.c_int, [H, C.POINTER(C.POINTER(RankMatrixS)), u32p, C.c_uint32]),

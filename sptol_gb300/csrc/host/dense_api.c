@@ -303,3 +303,90 @@ double sptKruskalTensorFit(sptSparseTensor const *const spten, sptValue const *c
     if (residual > 0.0) residual = sqrt(residual);
     return 1 - residual / sqrt(normsq);
 }
+
+/* ---------------------------------------------------- rank-matrix forms -- */
+/* The sptRankMatrix forms of the helpers above (rankmatrix.c:137-378,
+ * rankmatrix_solver.c:32-84, rankktensor.c:101-257) compute the same thing
+ * on matrices whose column count and stride are 8-bit; each runs the
+ * sptMatrix form on views of the caller's matrices. */
+static void rank_views(sptRankMatrix **in, sptIndex n, sptMatrix *view, sptMatrix **pv) {
+    for (sptIndex i = 0; i < n; ++i) {
+        view[i].nrows = in[i]->nrows;
+        view[i].ncols = in[i]->ncols;
+        view[i].cap = in[i]->cap;
+        view[i].stride = in[i]->stride;
+        view[i].values = in[i]->values;
+        pv[i] = &view[i];
+    }
+}
+
+static int bad_order(const char *module, sptIndex nmodes) {
+    if (nmodes >= 1 && nmodes <= SPTGB_MAX_MODES) return 0;
+    spt_ComplainError(module, SPTERR_VALUE_ERROR, __FILE__, __LINE__, "unsupported order");
+    return 1;
+}
+
+int sptRankMatrixDotMulSeqTriangle(sptIndex const mode, sptIndex const nmodes, sptRankMatrix **mats) {
+    if (bad_order("RankMtx DotMulSeqTriangle", nmodes)) return SPTERR_VALUE_ERROR;
+    sptMatrix v[SPTGB_MAX_MODES + 1], *pv[SPTGB_MAX_MODES + 1];
+    rank_views(mats, nmodes + 1, v, pv);
+    return sptMatrixDotMulSeqTriangle(mode, nmodes, pv);
+}
+
+int sptRankMatrixSolveNormals(sptIndex const mode, sptIndex const nmodes, sptRankMatrix **aTa, sptRankMatrix *rhs) {
+    if (bad_order("RankMtx SolveNormals", nmodes)) return SPTERR_VALUE_ERROR;
+    sptMatrix v[SPTGB_MAX_MODES + 2], *pv[SPTGB_MAX_MODES + 2];
+    rank_views(aTa, nmodes + 1, v, pv);
+    rank_views(&rhs, 1, v + nmodes + 1, pv + nmodes + 1);
+    return sptMatrixSolveNormals(mode, nmodes, pv, pv[nmodes + 1]);
+}
+
+int sptRankMatrix2Norm(sptRankMatrix *const A, sptValue *const lambda) {
+    sptMatrix v, *pv;
+    sptRankMatrix *a = A;
+    rank_views(&a, 1, &v, &pv);
+    return col_norm(pv, lambda, 0, 0, "RankMtx 2Norm");
+}
+
+int sptRankMatrixMaxNorm(sptRankMatrix *const A, sptValue *const lambda) {
+    sptMatrix v, *pv;
+    sptRankMatrix *a = A;
+    rank_views(&a, 1, &v, &pv);
+    return col_norm(pv, lambda, 1, 0, "RankMtx MaxNorm");
+}
+
+void GetRankFinalLambda(sptElementIndex const rank, sptIndex const nmodes, sptRankMatrix **mats,
+                        sptValue *const lambda) {
+    if (bad_order("GetRankFinalLambda", nmodes)) return;
+    sptMatrix v[SPTGB_MAX_MODES + 1], *pv[SPTGB_MAX_MODES + 1];
+    rank_views(mats, nmodes, v, pv);
+    GetFinalLambda(rank, nmodes, pv, lambda);
+}
+
+double sptKruskalTensorFrobeniusNormSquaredRank(sptIndex const nmodes, sptValue const *const lambda,
+                                                sptRankMatrix **ata) {
+    if (bad_order("Kruskal NormSquared", nmodes)) return NAN;
+    sptMatrix v[SPTGB_MAX_MODES + 1], *pv[SPTGB_MAX_MODES + 1];
+    rank_views(ata, nmodes + 1, v, pv);
+    return sptKruskalTensorFrobeniusNormSquared(nmodes, lambda, pv);
+}
+
+double sptSparseKruskalTensorInnerProductRank(sptIndex const nmodes, sptValue const *const lambda,
+                                              sptRankMatrix **mats) {
+    if (bad_order("Kruskal InnerProduct", nmodes)) return NAN;
+    sptMatrix v[SPTGB_MAX_MODES + 1], *pv[SPTGB_MAX_MODES + 1];
+    rank_views(mats, nmodes + 1, v, pv);
+    return sptSparseKruskalTensorInnerProduct(nmodes, lambda, pv);
+}
+
+/* rankktensor.c:101-119, the fit of sptKruskalTensorFit over a HiCOO tensor. */
+double sptKruskalTensorFitHiCOO(sptSparseTensorHiCOO const *const hitsr, sptValue const *const lambda,
+                                sptRankMatrix **mats, sptRankMatrix **ata) {
+    const sptIndex nmodes = hitsr->nmodes;
+    const double normsq = sptSparseTensorFrobeniusNormSquaredHiCOO(hitsr);
+    const double norm_mats = sptKruskalTensorFrobeniusNormSquaredRank(nmodes, lambda, ata);
+    const double inner = sptSparseKruskalTensorInnerProductRank(nmodes, lambda, mats);
+    double residual = normsq + norm_mats - 2 * inner;
+    if (residual > 0.0) residual = sqrt(residual);
+    return 1 - residual / sqrt(normsq);
+}

@@ -3,6 +3,7 @@ matrix/dump.c:34-50, ktensor/dump.c:24-51); host only, no GPU."""
 import ctypes as C
 
 import numpy as np
+import pytest
 
 import sptol_gb300 as S
 
@@ -38,3 +39,57 @@ def test_dump_matrix(tmp_path):
     text = _write(tmp_path, lambda fp: S.lib().sptDumpMatrix(C.byref(m.s), fp))
     exp = "2 x 3 matrix\n" + "".join("".join("%.2f\t" % float(v) for v in row) + "\n" for row in a) + "\n"
     assert text == exp
+
+
+def _lines(tag, fmt, xs):
+    return "%s length: %d\n" % (tag, len(xs)) + "".join((fmt % x) + "\t" for x in xs) + "\n"
+
+
+def test_dump_arrays(tmp_path):
+    L = S.lib()
+    a = np.array([7, 0, 4294967295, 12], np.uint32)
+    text = _write(tmp_path, lambda fp: L.sptDumpIndexArray(a.ctypes.data_as(S.u32p), len(a), fp))
+    assert text == _lines("sptIndex array", "%u", a.tolist())
+    b = np.array([1 << 40, 3], np.uint64)
+    text = _write(tmp_path, lambda fp: L.sptDumpNnzIndexArray(b.ctypes.data_as(S.u64p), len(b), fp))
+    assert text == _lines("sptNnzIndex array", "%u", b.tolist())
+    text = _write(tmp_path, lambda fp: L.sptDumpIndexArray(a.ctypes.data_as(S.u32p), 0, fp))
+    assert text == "sptIndex array length: 0\n\n"
+
+
+def test_dump_rank_matrix(tmp_path):
+    a = np.array([[1.0, -2.345, 3.0], [0.004, 5.0, 6.5], [9, 8, 7]], np.float32)
+    m = S.RankMatrix.from_array(a)
+    text = _write(tmp_path, lambda fp: S.lib().sptDumpRankMatrix(C.byref(m.s), fp))
+    exp = "3 x 3 matrix\n" + "".join("".join("%.2f\t" % float(v) for v in row) + "\n" for row in a) + "\n"
+    assert text == exp
+
+
+def _ktensor_text(nmodes, rank, ndims, fit, lam, facs):
+    exp = "nmodes: %d, rank: %d\n" % (nmodes, rank) + " ".join(str(d) for d in ndims) + "\n"
+    exp += "fit: %f\nlambda:\n" % fit + "".join("%f " % float(lam[m]) for m in range(nmodes))
+    exp += "Factor matrices:\n"
+    for f in facs:
+        exp += "%d x %d matrix\n" % f.shape + "".join("".join("%.2f\t" % float(v) for v in row) + "\n"
+                                                  for row in f) + "\n"
+    return exp
+
+
+@pytest.mark.parametrize("rank_form", [False, True])
+def test_dump_kruskal(tmp_path, rank_form):
+    L = S.lib()
+    ndims = np.array([3, 2, 4], np.uint32)
+    rank = 4
+    rng = np.random.default_rng(1)
+    facs = [rng.uniform(-1, 1, (int(d), rank)).astype(np.float32) for d in ndims]
+    lam = np.array([1.25, -0.5, 3.0, 2.0], np.float32)
+    mk = S.RankMatrix if rank_form else S.Matrix
+    mats = [mk.from_array(f) for f in facs]
+    P = type(C.pointer(mats[0].s))
+    arr = (P * 4)(*[C.pointer(m.s) for m in mats])        # factors[nmodes] left NULL
+    K = S.RankKruskalS if rank_form else S.KruskalS
+    k = K(3, rank, ndims.ctypes.data_as(S.u32p), lam.ctypes.data_as(S.f32p), 0.8125, arr)
+    fn = L.sptDumpRankKruskalTensor if rank_form else L.sptDumpKruskalTensor
+    text = _write(tmp_path, lambda fp: fn(C.byref(k), fp))
+    # one lambda entry per mode, as the reference prints
+    assert text == _ktensor_text(3, rank, ndims, 0.8125, lam, facs)

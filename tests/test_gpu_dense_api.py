@@ -121,3 +121,69 @@ def test_fit_and_parts():
     exp_fit = 1 - (np.sqrt(res) if res > 0 else res) / np.sqrt(nx)
     fit = L.sptKruskalTensorFit(t.ptr(), lp, _arr(mats), _arr(ata))
     assert abs(fit - exp_fit) <= 1e-5
+
+
+def _rarr(mats):
+    return (C.POINTER(S.RankMatrixS) * len(mats))(*[C.pointer(m.s) for m in mats])
+
+
+def test_rank_forms_match_matrix_forms():
+    """rankmatrix.c / rankmatrix_solver.c / rankktensor.c: the sptRankMatrix
+    forms give the sptMatrix forms' results bit for bit."""
+    rng = np.random.default_rng(11)
+    N, rank, mode = 3, 16, 1
+    L = S.lib()
+    gs = _grams(rng, N, rank)
+    m = [S.Matrix.from_array(g) for g in gs] + [S.Matrix(rank, rank)]
+    rm = [S.RankMatrix.from_array(g) for g in gs] + [S.RankMatrix(rank, rank)]
+    assert L.sptMatrixDotMulSeqTriangle(mode, N, _arr(m)) == 0
+    assert L.sptRankMatrixDotMulSeqTriangle(mode, N, _rarr(rm)) == 0
+    assert np.array_equal(m[N].array()[:rank, :rank], rm[N].array()[:rank, :rank])
+    rhs_a = rng.uniform(-1, 1, (300, rank)).astype(np.float32)
+    rhs, rrhs = S.Matrix.from_array(rhs_a), S.RankMatrix.from_array(rhs_a)
+    assert L.sptMatrixSolveNormals(mode, N, _arr(m), C.byref(rhs.s)) == 0
+    assert L.sptRankMatrixSolveNormals(mode, N, _rarr(rm), C.byref(rrhs.s)) == 0
+    assert np.array_equal(rhs.array()[:300, :rank], rrhs.array()[:300, :rank])
+    a = rng.uniform(-2, 3, (2000, rank)).astype(np.float32)
+    for f, rf in (("sptMatrix2Norm", "sptRankMatrix2Norm"), ("sptMatrixMaxNorm", "sptRankMatrixMaxNorm")):
+        x, rx = S.Matrix.from_array(a), S.RankMatrix.from_array(a)
+        l1, l2 = np.zeros(rank, np.float32), np.zeros(rank, np.float32)
+        assert getattr(L, f)(C.byref(x.s), l1.ctypes.data_as(S.f32p)) == 0
+        assert getattr(L, rf)(C.byref(rx.s), l2.ctypes.data_as(S.f32p)) == 0
+        assert np.array_equal(l1, l2)
+        assert np.array_equal(x.array()[:2000, :rank], rx.array()[:2000, :rank])
+    fs = [rng.uniform(0, 1, (n, rank)).astype(np.float32) for n in (70, 50, 90)]
+    lam1 = rng.uniform(1, 2, rank).astype(np.float32)
+    lam2 = lam1.copy()
+    L.GetFinalLambda(rank, 3, _arr([S.Matrix.from_array(f) for f in fs]), lam1.ctypes.data_as(S.f32p))
+    L.GetRankFinalLambda(rank, 3, _rarr([S.RankMatrix.from_array(f) for f in fs]), lam2.ctypes.data_as(S.f32p))
+    assert np.array_equal(lam1, lam2)
+
+
+def test_fit_hicoo_matches_coo_fit():
+    """sptKruskalTensorFitHiCOO (rankktensor.c:101-119) against
+    sptKruskalTensorFit on the same tensor and factors."""
+    rng = np.random.default_rng(12)
+    ndims = [300, 200, 150]
+    rank = 8
+    inds = np.stack([rng.integers(0, d, 20000) for d in ndims]).astype(np.uint32)
+    vals = rng.uniform(0, 1, 20000).astype(np.float32)
+    t = S.Tensor.from_arrays(ndims, inds, vals)
+    facs = [rng.uniform(0, 1, (d, rank)).astype(np.float32) for d in ndims]
+    lam = rng.uniform(0.5, 2, rank).astype(np.float32)
+    mats = [S.Matrix.from_array(f) for f in facs] + [S.Matrix(max(ndims), rank)]
+    out = S.mttkrp(t, mats, 2)
+    rmats = [S.RankMatrix.from_array(f) for f in facs] + [S.RankMatrix.from_array(
+        np.vstack([out, np.zeros((max(ndims) - ndims[2], rank), np.float32)]))]
+    grams = [(f.astype(np.float64).T @ f).astype(np.float32) for f in facs]
+    ata = [S.Matrix.from_array(g) for g in grams] + [S.Matrix(rank, rank)]
+    rata = [S.RankMatrix.from_array(g) for g in grams] + [S.RankMatrix(rank, rank)]
+    L = S.lib()
+    lp = lam.ctypes.data_as(S.f32p)
+    fit = L.sptKruskalTensorFit(t.ptr(), lp, _arr(mats), _arr(ata))
+    h = S.HiCOO(t, 4, 6)
+    fit_h = L.sptKruskalTensorFitHiCOO(h.ptr(), lp, _rarr(rmats), _rarr(rata))
+    assert abs(fit - fit_h) <= 1e-9 + 1e-6 * abs(fit)
+    assert L.sptKruskalTensorFrobeniusNormSquaredRank(3, lp, _rarr(rata)) == \
+        L.sptKruskalTensorFrobeniusNormSquared(3, lp, _arr(ata))
+    h.free()

@@ -323,3 +323,37 @@ def test_rank_matrix_hicoo_entry_points(order):
             out = rmats[N].array()[: ndims[mode], :rank]
             assert rel_fro(out, ref) <= 1e-5, (name, mode)
             assert not rmats[N].array()[: ndims[mode], rank:].any(), name
+
+
+def test_dump_hicoo(tmp_path):
+    """sptDumpSparseTensorHiCOO (sptensor/hicoo/dump.c:28-72): every array of
+    the converted tensor, in the reference's text layout."""
+    libc = C.CDLL(None)
+    libc.fopen.restype = C.c_void_p
+    libc.fopen.argtypes = [C.c_char_p, C.c_char_p]
+    libc.fclose.argtypes = [C.c_void_p]
+    rng = np.random.default_rng(21)
+    ndims = [70, 40, 33]
+    inds = np.stack([rng.integers(0, d, 500) for d in ndims]).astype(np.uint32)
+    vals = rng.uniform(0, 1, 500).astype(np.float32)
+    h = S.HiCOO(S.Tensor.from_arrays(ndims, inds, vals), 3, 5)
+    A = h.arrays()
+    path = str(tmp_path / "h.txt")
+    fp = libc.fopen(path.encode(), b"w")
+    rc = S.lib().sptDumpSparseTensorHiCOO(h.ptr(), fp)
+    libc.fclose(fp)
+    assert rc == 0
+
+    def lst(tag, fmt, xs):
+        return "%s length: %d\n" % (tag, len(xs)) + "".join((fmt % x) + "\t" for x in xs) + "\n"
+
+    exp = "3\n70 40 33\nnkiters:\n" + lst("sptIndex array", "%u", A["nkiters"]) + "kschr:\n"
+    for m in range(3):
+        exp += "mode %d\n" % m + "".join(lst("sptIndexVector", "%u", v.tolist()) for v in A["kschr"][m])
+    for name in ("kptr", "cptr", "bptr"):
+        exp += name + ":\n" + lst("sptNnzIndexVector", "%u", A[name].tolist())
+    exp += "binds:\n" + "".join(lst("sptBlockIndexVector", "%u", b.tolist()) for b in A["binds"])
+    exp += "einds:\n" + "".join(lst("sptElementIndexVector", "%u", e.tolist()) for e in A["einds"])
+    exp += "values:\n" + lst("sptValueVector", "%f", [float(v) for v in A["values"]])
+    assert open(path).read() == exp
+    h.free()
