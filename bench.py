@@ -67,7 +67,7 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--nnz", type=int, default=100_000_000)
     p.add_argument("--cpu-sample", type=int, default=10_000_000)
-    p.add_argument("--e2e-steps", type=int, default=3)
+    p.add_argument("--e2e-steps", type=int, default=5)
     p.add_argument("--skip-cpu", action="store_true")
     p.add_argument("--serve-requests", type=int, default=4096)
     p.add_argument("--plain-sample", type=int, default=256)
@@ -92,6 +92,28 @@ def spec_for(count, seed=SEED):
     s.merge_duplicates = 0
     s.value_dist = S.VAL_LOGNORMAL
     return s
+
+
+def host_link_gbs(nbytes=1 << 30, reps=3):
+    """Pageable host-to-device copy rate of this machine (GB/s), the floor of the
+    host-buffer path."""
+    import torch
+    try:
+        a = np.ones(nbytes // 4, np.float32)
+        h = torch.from_numpy(a)
+        d = torch.empty(nbytes // 4, dtype=torch.float32, device="cuda")
+        d.copy_(h)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            d.copy_(h)
+        torch.cuda.synchronize()
+        gbs = reps * nbytes / (time.perf_counter() - t0) / 1e9
+        del d, h, a
+        torch.cuda.empty_cache()
+        return round(gbs, 1)
+    except Exception:
+        return None
 
 
 def workload_config(nnz, world):
@@ -666,13 +688,17 @@ def run_ours(args, world, rank, local):
         h2d += nnz * 16 + sum(ndims[p] * stride * 4 for p in orders[m][1:])
         d2h += ndims[m] * stride * 4
     ke = max(1, args.e2e_steps)
+    link_gbs = host_link_gbs()
     for m in range(3):   # warm-up: grows the library's device buffers outside the timed region
         S.mttkrp(t, mats, m, mats_order=orders[m], entry="sptCudaMTTKRP")
     barrier(world)
+    e_each = []
     e0 = time.perf_counter()
     for _ in range(ke):
+        s0 = time.perf_counter()
         for m in range(3):
             S.mttkrp(t, mats, m, mats_order=orders[m], entry="sptCudaMTTKRP", copy=False)
+        e_each.append(time.perf_counter() - s0)
     e_s = reduce_max((time.perf_counter() - e0) / ke, world)
     e2e = world * bytes_step / e_s / 1e9
 
@@ -702,7 +728,10 @@ def run_ours(args, world, rank, local):
                          "kernel": "k_mttkrp_rec (order-3 record kernel) after the output memset, one launch per mode",
                          "ms_per_launch_by_mode": [round(x, 4) for x in per_mode]},
             "e2e": {"value": round(e2e, 2), "unit": "GB/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "entry": "sptCudaMTTKRP (host buffers)", "ms_per_step": e_s * 1e3},
+                    "entry": "sptCudaMTTKRP (host buffers)", "ms_per_step": e_s * 1e3,
+                    "ms_each_step": [round(x * 1e3, 2) for x in e_each],
+                    "host_link_h2d_gbs": link_gbs,
+                    "link_floor_ms": round((h2d + d2h) / (link_gbs * 1e9) * 1e3, 2) if link_gbs else None},
             "gpu_launches": int(n1 - n0),
             "clocks": clocks.summary(),
             "nnz_per_s": round(world * K * 3 * nnz / (ms_max / 1e3), 1),
