@@ -1,4 +1,4 @@
-/* Host-side helpers shared by the drop-in entry points (csrc/host/*.c). */
+/* Host-side helpers shared by the drop-in entry points (the .c files of csrc/host). */
 #ifndef SPTGB_DEVTENSOR_H
 #define SPTGB_DEVTENSOR_H
 

@@ -1,6 +1,6 @@
 /*
- * Internal interface between the C host layer (csrc/host/*.c) and the CUDA
- * translation units (csrc/cuda/*.cu).  Plain C types only; every launcher
+ * Internal interface between the C host layer (the .c files of csrc/host) and the CUDA
+ * translation units (the .cu files of csrc/cuda).  Plain C types only; every launcher
  * is extern "C", takes device pointers and a stream, and returns a cudaError_t
  * value (0 on success) so that the host layer maps it to
  * SPTERR_CUDA_ERROR + code.
