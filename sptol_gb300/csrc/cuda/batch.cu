@@ -181,13 +181,6 @@ __global__ void k_b_fit_final(const sptgb_slot *__restrict__ slots, sptgb_wlist 
     }
 }
 
-__global__ void k_pack_records4(const uint32_t *__restrict__ rows, const uint32_t *__restrict__ ia,
-                                const uint32_t *__restrict__ ib, const uint32_t *__restrict__ ic,
-                                uint4 *__restrict__ rec, uint64_t n) {
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
-        rec[i] = make_uint4(rows[i], ia[i], ib[i], ic[i]);
-}
-
 // ------------------------------------------------------------ admission --
 // Last job j with offs[j] <= i.
 __device__ __forceinline__ uint32_t job_of(const uint64_t *offs, uint32_t njobs, uint64_t i) {
@@ -404,16 +397,6 @@ extern "C" cudaError_t sptgb_batch_step(const sptgb_slot *slots, const sptgb_ste
     k_b_fit_partial<<<n * 4, DT, 0, s>>>(slots, L->fit);
     k_b_fit_final<<<n * 2, DT, 0, s>>>(slots, L->fit_one, L->fit);
     sptgb_count_launch(2);
-    return cudaGetLastError();
-}
-
-extern "C" cudaError_t sptgb_pack_records4(const uint32_t *rows, const uint32_t *ia, const uint32_t *ib,
-                                           const uint32_t *ic, void *rec, uint64_t n, cudaStream_t s) {
-    if (n == 0) return cudaSuccess;
-    uint64_t g = (n + 255) / 256;
-    if (g > 152ull * 16) g = 152ull * 16;
-    k_pack_records4<<<(unsigned)g, 256, 0, s>>>(rows, ia, ib, ic, static_cast<uint4 *>(rec), n);
-    sptgb_count_launch(1);
     return cudaGetLastError();
 }
 

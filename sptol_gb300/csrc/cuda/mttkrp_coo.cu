@@ -14,7 +14,9 @@
 // pipelined (the next batch is in flight while the current batch's factor rows
 // are gathered) and the Hadamard product uses packed FP32x2 arithmetic.  The
 // output is zeroed by one memset; rows inside a unit are written with plain
-// stores, rows shared by neighbouring units with vector atomics.  Other orders
+// stores, rows shared by neighbouring units with vector atomics.  Order 4
+// runs k_mttkrp_rec4 the same way over records {row, idx_a, idx_b, idx_c}
+// with the values in their own array (batches of two records).  Other orders
 // run k_mttkrp_seg below.
 //
 // Work decomposition.  A "worker" is a group of W lanes that owns one nonzero
@@ -184,6 +186,27 @@ k_mttkrp_rec(const uint4 *__restrict__ rec, const void *__restrict__ Fa, const v
     }
 }
 
+// Order-4 record kernel: records {row, a, b, c} with the values in `vals`
+// (same order), batches of NB records; otherwise as k_mttkrp_rec.
+template <int W, bool BF16, bool FULL, int NB>
+__global__ void __launch_bounds__(BLOCK, 3)
+k_mttkrp_rec4(const uint4 *__restrict__ rec, const float *__restrict__ vals, const void *__restrict__ Fa,
+              const void *__restrict__ Fb, const void *__restrict__ Fc, float *__restrict__ out, uint64_t nnz,
+              uint32_t stride, uint32_t rank, uint32_t ul, uint64_t u0, uint64_t nunits) {
+    const int sl = (threadIdx.x & 31) % W;
+    const uint32_t elem = BF16 ? 2u : 4u;
+    const size_t off = (size_t)sl * 4 * elem;
+    const char *F[3] = {static_cast<const char *>(Fa) + off, static_cast<const char *>(Fb) + off,
+                        static_cast<const char *>(Fc) + off};
+    const uint64_t worker = ((uint64_t)blockIdx.x * BLOCK + threadIdx.x) / W;
+    const uint64_t nworkers = ((uint64_t)gridDim.x * BLOCK) / W;
+    for (uint64_t u = u0 + worker; u < nunits; u += nworkers) {
+        const uint64_t start = u * ul;
+        const uint32_t len = (uint32_t)min((uint64_t)ul, nnz - start);
+        sptgb_mttkrp::unit<BF16, FULL, 3, NB>(rec, vals, F, stride * elem, out, nnz, start, len, stride, rank, sl);
+    }
+}
+
 __global__ void k_pack_records(const uint32_t *__restrict__ rows, const uint32_t *__restrict__ ia,
                                const uint32_t *__restrict__ ib, const float *__restrict__ vals, uint32_t lim_a,
                                uint32_t lim_b, unsigned int *__restrict__ bad, uint4 *__restrict__ rec, uint64_t n) {
@@ -193,6 +216,22 @@ __global__ void k_pack_records(const uint32_t *__restrict__ rows, const uint32_t
         const bool ok = a < lim_a && c < lim_b;
         b |= !ok;
         rec[i] = make_uint4(rows[i], ok ? a : 0u, ok ? c : 0u, __float_as_uint(vals[i]));
+    }
+    if (__any_sync(0xffffffffu, b) && (threadIdx.x & 31) == 0 && bad) atomicOr(bad, 1u);
+}
+
+// Order-4 records {rows, ia, ib, ic}; out-of-range ia / ib / ic as in
+// k_pack_records.
+__global__ void k_pack_records4(const uint32_t *__restrict__ rows, const uint32_t *__restrict__ ia,
+                                const uint32_t *__restrict__ ib, const uint32_t *__restrict__ ic, uint32_t lim_a,
+                                uint32_t lim_b, uint32_t lim_c, unsigned int *__restrict__ bad,
+                                uint4 *__restrict__ rec, uint64_t n) {
+    unsigned int b = 0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t x = ia[i], y = ib[i], z = ic[i];
+        const bool ok = x < lim_a && y < lim_b && z < lim_c;
+        b |= !ok;
+        rec[i] = make_uint4(rows[i], ok ? x : 0u, ok ? y : 0u, ok ? z : 0u);
     }
     if (__any_sync(0xffffffffu, b) && (threadIdx.x & 31) == 0 && bad) atomicOr(bad, 1u);
 }
@@ -245,14 +284,18 @@ cudaError_t launch(const sptgb_mttkrp_args &a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-template <int W, bool BF16, bool FULL>
+template <int W, bool BF16, bool FULL, int NF>
 cudaError_t launch_rec_k(const sptgb_mttkrp_args &a, cudaStream_t s) {
+    constexpr int NB = 2;   // order-4 records per batch (3: register spills at 3 CTAs/SM)
     static int max_blocks = 0;
     if (max_blocks == 0) {
         int dev = 0, nsm = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mttkrp_rec<W, BF16, FULL>, BLOCK, 0);
+        if (NF == 2)
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mttkrp_rec<W, BF16, FULL>, BLOCK, 0);
+        else
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mttkrp_rec4<W, BF16, FULL, NB>, BLOCK, 0);
         max_blocks = (per_sm < 1 ? 1 : per_sm) * nsm;
     }
     // 256-nonzero units: enough of them to balance a power-law row distribution
@@ -267,21 +310,27 @@ cudaError_t launch_rec_k(const sptgb_mttkrp_args &a, cudaStream_t s) {
         cudaError_t e = cudaMemsetAsync(a.out, 0, (size_t)a.out_rows * a.stride * sizeof(float), s);
         if (e != cudaSuccess) return e;
     }
-    k_mttkrp_rec<W, BF16, FULL><<<(unsigned)blocks, BLOCK, 0, s>>>(static_cast<const uint4 *>(a.rec), a.fac[0],
-                                                                  a.fac[1], a.out, a.nnz, a.stride, a.rank, ul,
-                                                                  a.unit_begin, u1);
+    if (NF == 2)
+        k_mttkrp_rec<W, BF16, FULL><<<(unsigned)blocks, BLOCK, 0, s>>>(static_cast<const uint4 *>(a.rec), a.fac[0],
+                                                                      a.fac[1], a.out, a.nnz, a.stride, a.rank, ul,
+                                                                      a.unit_begin, u1);
+    else
+        k_mttkrp_rec4<W, BF16, FULL, NB><<<(unsigned)blocks, BLOCK, 0, s>>>(
+            static_cast<const uint4 *>(a.rec), a.vals, a.fac[0], a.fac[1], a.fac[2], a.out, a.nnz, a.stride, a.rank,
+            ul, a.unit_begin, u1);
     sptgb_count_launch(1);
     return cudaGetLastError();
 }
 
-template <int W, bool BF16>
+template <int W, bool BF16, int NF>
 cudaError_t launch_rec(const sptgb_mttkrp_args &a, cudaStream_t s) {
-    return a.stride == 4u * W ? launch_rec_k<W, BF16, true>(a, s) : launch_rec_k<W, BF16, false>(a, s);
+    return a.stride == 4u * W ? launch_rec_k<W, BF16, true, NF>(a, s) : launch_rec_k<W, BF16, false, NF>(a, s);
 }
 
 template <int W, bool BF16>
 cudaError_t dispatch_np(const sptgb_mttkrp_args &a, cudaStream_t s) {
-    if (a.rec && a.nprod == 2) return launch_rec<W, BF16>(a, s);
+    if (a.rec && a.nprod == 2) return launch_rec<W, BF16, 2>(a, s);
+    if (a.rec && a.nprod == 3) return launch_rec<W, BF16, 3>(a, s);
     switch (a.nprod) {
         case 1: return launch<W, 1, BF16>(a, s);
         case 2: return launch<W, 2, BF16>(a, s);
@@ -346,4 +395,16 @@ extern "C" cudaError_t sptgb_mttkrp_coo(const sptgb_mttkrp_args *a, cudaStream_t
         return cudaMemsetAsync(a->out, 0, (size_t)a->out_rows * a->stride * sizeof(float), s);
     }
     return a->bf16 ? dispatch_w<true>(*a, s) : dispatch_w<false>(*a, s);
+}
+
+extern "C" cudaError_t sptgb_pack_records4(const uint32_t *rows, const uint32_t *ia, const uint32_t *ib,
+                                           const uint32_t *ic, uint32_t lim_a, uint32_t lim_b, uint32_t lim_c,
+                                           unsigned int *bad, void *rec, uint64_t n, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    uint64_t g = (n + 255) / 256;
+    if (g > 152ull * 16) g = 152ull * 16;
+    k_pack_records4<<<(unsigned)g, 256, 0, s>>>(rows, ia, ib, ic, lim_a, lim_b, lim_c, bad, static_cast<uint4 *>(rec),
+                                                n);
+    sptgb_count_launch(1);
+    return cudaGetLastError();
 }

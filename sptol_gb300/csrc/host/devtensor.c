@@ -411,6 +411,21 @@ int sptgbCooPrepareMode(sptgbCoo *t, sptIndex mode, void *stream) {
         if (e != cudaSuccess) r = sptgb_cuda_fail(e, "GPU COO prepare", __FILE__, __LINE__);
         t->bytes += (size_t)n * 16;
     }
+    if (!r && N == 4) {
+        /* records {row, idx_a, idx_b, idx_c}, a < b < c the other modes; the
+         * values stay in the mode-sorted value array */
+        uint32_t o[3];
+        int k3 = 0;
+        for (int m = 0; m < 4; ++m)
+            if ((sptIndex)m != mode) o[k3++] = (uint32_t)m;
+        cudaError_t e = cudaMalloc(&t->mrec[mode], (n ? n : 1) * 16);
+        if (e == cudaSuccess)
+            e = sptgb_pack_records4(t->minds[mode][mode], t->minds[mode][o[0]], t->minds[mode][o[1]],
+                                    t->minds[mode][o[2]], 0xffffffffu, 0xffffffffu, 0xffffffffu, NULL,
+                                    t->mrec[mode], n, s);
+        if (e != cudaSuccess) r = sptgb_cuda_fail(e, "GPU COO prepare", __FILE__, __LINE__);
+        t->bytes += (size_t)n * 16;
+    }
     if (!r) {
         cudaError_t e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) r = sptgb_cuda_fail(e, "GPU COO prepare", __FILE__, __LINE__);
@@ -434,12 +449,12 @@ static int coo_mttkrp(sptgbCoo *t, sptIndex mode, const sptIndex *mats_order, co
         a.idx[i - 1] = t->minds[mode][pm];
         a.fac[i - 1] = d_mats[pm];
     }
-    if (t->nmodes == 3 && t->mrec[mode]) {
-        /* the records hold the two other modes in ascending order */
-        const sptIndex ma = mode == 0 ? 1 : 0, mb = mode == 2 ? 1 : 2;
+    if ((t->nmodes == 3 || t->nmodes == 4) && t->mrec[mode]) {
+        /* the records hold the other modes in ascending order */
+        int k = 0;
+        for (sptIndex m = 0; m < t->nmodes; ++m)
+            if (m != mode) a.fac[k++] = d_mats[m];
         a.rec = t->mrec[mode];
-        a.fac[0] = d_mats[ma];
-        a.fac[1] = d_mats[mb];
     }
     a.vals = t->mvals[mode];
     a.out = d_out;

@@ -72,7 +72,7 @@ struct sptgbCoo {
     int ready[SPTGB_MAX_MODES];
     uint32_t *minds[SPTGB_MAX_MODES][SPTGB_MAX_MODES];
     float *mvals[SPTGB_MAX_MODES];
-    void *mrec[SPTGB_MAX_MODES];   /* order 3: 16-byte records of the mode copy */
+    void *mrec[SPTGB_MAX_MODES];   /* orders 3 and 4: 16-byte records of the mode copy */
     size_t bytes;
     int timing;
     cudaEvent_t ev0, ev1;

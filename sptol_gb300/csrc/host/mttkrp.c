@@ -102,7 +102,7 @@ static int mttkrp_host_locked(sptSparseTensor const *X, sptMatrix *mats[], sptIn
                                   "a coordinate is not smaller than its mode size");
                 return SPTERR_VALUE_ERROR;
             }
-        const int rec3 = N == 3;
+        const int recs = N == 3 || N == 4;   /* 16-byte records (order 4: the values in their own array) */
         /* Every buffer is reserved before the first copy: growing one frees
          * and reallocates, which would serialise the two streams. */
         SPTGB_CHECK(sptgb_ws_sync_objects(), module);
@@ -115,10 +115,11 @@ static int mttkrp_host_locked(sptSparseTensor const *X, sptMatrix *mats[], sptIn
             SPTGB_CHECK(sptgb_dbuf_reserve(&g_ws.fac[pm], bytes ? bytes : 16), module);
         }
         SPTGB_CHECK(sptgb_dbuf_reserve(&g_ws.flag, 32 * sizeof(unsigned int)), module);
-        if (rec3) {
+        if (recs) {
             SPTGB_CHECK(sptgb_dbuf_reserve(&g_ws.misc[0], n * 16), module);
             SPTGB_CHECK(sptgb_dbuf_reserve(&g_ws.misc[1], n * 16), module);
         }
+        if (N == 4) SPTGB_CHECK(sptgb_dbuf_reserve(&g_ws.svals, n * sizeof(float)), module);
         uint32_t *din[SPTGB_MAX_MODES] = {0};
         for (sptIndex m = 0; m < N; ++m)
             if (need[m]) din[m] = (uint32_t *)g_ws.inds[m].ptr;
@@ -188,14 +189,28 @@ static int mttkrp_host_locked(sptSparseTensor const *X, sptMatrix *mats[], sptIn
 
         sptgb_mttkrp_args a;
         memset(&a, 0, sizeof a);
-        if (rec3) {
+        if (recs) {
             /* 4. records in the caller's order with the other coordinates
              *    range-checked (an out-of-range one becomes row 0 and flags
              *    the call), then whole records through the permutation. */
             const sptIndex pa = mats_order[1], pb = mats_order[2];
             void *rec = g_ws.misc[0].ptr, *tmp = g_ws.misc[1].ptr;
-            e = sptgb_pack_records(din[mode], din[pa], din[pb], (const float *)g_ws.vals.ptr, X->ndims[pa],
-                                   X->ndims[pb], dflag + 2, unsorted ? tmp : rec, n, s);
+            if (N == 3) {
+                e = sptgb_pack_records(din[mode], din[pa], din[pb], (const float *)g_ws.vals.ptr, X->ndims[pa],
+                                       X->ndims[pb], dflag + 2, unsorted ? tmp : rec, n, s);
+                a.vals = NULL;
+            } else {
+                /* order 4: {row, a, b, c} in the caller's product order, the
+                 * values permuted alongside */
+                const sptIndex pc = mats_order[3];
+                e = sptgb_pack_records4(din[mode], din[pa], din[pb], din[pc], X->ndims[pa], X->ndims[pb],
+                                        X->ndims[pc], dflag + 2, unsorted ? tmp : rec, n, s);
+                a.vals = (const float *)g_ws.vals.ptr;
+                if (e == cudaSuccess && unsorted) {
+                    e = sptgb_gather_u32((const uint32_t *)g_ws.vals.ptr, perm, (uint32_t *)g_ws.svals.ptr, n, s);
+                    a.vals = (const float *)g_ws.svals.ptr;
+                }
+            }
             if (e == cudaSuccess && unsorted) e = sptgb_gather_records(tmp, perm, rec, n, s);
             if (e != cudaSuccess) return drain_copies(sptgb_cuda_fail(e, module, __FILE__, __LINE__));
             a.rec = rec;
@@ -208,7 +223,7 @@ static int mttkrp_host_locked(sptSparseTensor const *X, sptMatrix *mats[], sptIn
         if (e == cudaSuccess) e = cudaStreamWaitEvent(s, g_ws.ev[1], 0);
         if (e != cudaSuccess) return drain_copies(sptgb_cuda_fail(e, module, __FILE__, __LINE__));
         TRACE("h2d rest");
-        if (!rec3) {
+        if (!recs) {
             /* other orders read the coordinate arrays directly: check them
              * all before the kernel runs */
             SPTGB_CHECK(sptgb_validate(din, X->ndims, (int)N, n, NULL, NULL, s), module);
@@ -240,11 +255,11 @@ static int mttkrp_host_locked(sptSparseTensor const *X, sptMatrix *mats[], sptIn
         a.rank = R;
         a.stride = stride;
         const uint64_t nunits = (n + SPTGB_REC_UNIT - 1) / SPTGB_REC_UNIT;
-        const int nchunk = rec3 && tmpI && n >= CHUNKED_MIN_NNZ ? OUT_CHUNKS : 1;
+        const int nchunk = recs && tmpI && n >= CHUNKED_MIN_NNZ ? OUT_CHUNKS : 1;
         if (nchunk == 1) {
             SPTGB_CUDA(sptgb_mttkrp_coo(&a, s), module);
             TRACE("kernel");
-            if (rec3)
+            if (recs)
                 SPTGB_CUDA(cudaMemcpyAsync(hflag + 2, dflag + 2, sizeof(unsigned int), cudaMemcpyDeviceToHost, s),
                            module);
             if (tmpI)
@@ -304,7 +319,7 @@ static int mttkrp_host_locked(sptSparseTensor const *X, sptMatrix *mats[], sptIn
                    module);
     SPTGB_CUDA(cudaStreamSynchronize(s), module);
     TRACE("d2h out");
-    if (n && N == 3 && g_ws.hflag[2]) {
+    if (n && (N == 3 || N == 4) && g_ws.hflag[2]) {
         spt_ComplainError(module, SPTERR_VALUE_ERROR, __FILE__, __LINE__,
                           "a coordinate is not smaller than its mode size");
         return SPTERR_VALUE_ERROR;

@@ -84,8 +84,9 @@ typedef struct {
     uint32_t        stride;
     int             bf16;                      /* factors stored as bf16 */
     const void     *rec;                       /* order 3: [nnz] 16-byte records {row, idx[0], idx[1], value}
-                                                  (sptgb_pack_records); used instead of rows/idx/vals */
-    /* Order 3 only: run units [unit_begin, unit_end) of SPTGB_REC_UNIT
+                                                  (sptgb_pack_records), used instead of rows/idx/vals; order 4:
+                                                  {row, idx[0], idx[1], idx[2]} (sptgb_pack_records4) with vals */
+    /* Records only: run units [unit_begin, unit_end) of SPTGB_REC_UNIT
      * nonzeros (unit_end 0 = all) into an output that is already zero when
      * out_zeroed.  Ranges launched one after another on one stream give the
      * same result as one launch; rows below the first row of a later range
@@ -107,6 +108,11 @@ cudaError_t sptgb_mttkrp_coo(const sptgb_mttkrp_args *a, cudaStream_t s);
 cudaError_t sptgb_pack_records(const uint32_t *rows, const uint32_t *ia, const uint32_t *ib, const float *vals,
                                uint32_t lim_a, uint32_t lim_b, unsigned int *bad, void *rec, uint64_t n,
                                cudaStream_t s);
+/* Order-4 records {rows[i], ia[i], ib[i], ic[i]} (the values stay in their own
+ * array); out-of-range ia / ib / ic as in sptgb_pack_records. */
+cudaError_t sptgb_pack_records4(const uint32_t *rows, const uint32_t *ia, const uint32_t *ib, const uint32_t *ic,
+                                uint32_t lim_a, uint32_t lim_b, uint32_t lim_c, unsigned int *bad, void *rec,
+                                uint64_t n, cudaStream_t s);
 /* dst[i] = src[perm[i]] for 16-byte records. */
 cudaError_t sptgb_gather_records(const void *src, const uint32_t *perm, void *dst, uint64_t n, cudaStream_t s);
 
@@ -349,10 +355,6 @@ uint32_t sptgb_sumsq_blocks(uint64_t n);
 uint32_t sptgb_colnorm_blocks(uint32_t nrows);
 uint32_t sptgb_gram_blocks(uint32_t nrows);
 
-/* Records of one mode for a batch slot: order 3 as sptgb_pack_records, order
- * 4 with idx[2] in the fourth word and the values copied to val4. */
-cudaError_t sptgb_pack_records4(const uint32_t *rows, const uint32_t *ia, const uint32_t *ib, const uint32_t *ic,
-                                void *rec, uint64_t n, cudaStream_t s);
 
 /* ------------------------------------------------- BF16 conversion -- */
 cudaError_t sptgb_f32_to_bf16(const float *in, uint16_t *out, uint64_t n, cudaStream_t s);

@@ -267,3 +267,32 @@ def test_chunked_result_copy_with_a_row_across_chunks(shuffled, rank):
         assert rel_fro(out, ref) <= TOL, mode
         # padding columns of the output stay zero
         assert not mats[3].array()[: ndims[mode], rank:].any()
+
+
+@pytest.mark.parametrize("n,rank,shuffled", [(30_000, 16, False), (30_000, 20, True), (4_200_000, 16, True),
+                                            (4_200_000, 64, False)])
+@pytest.mark.parametrize("entry", ["sptMTTKRP", "sptCudaMTTKRP"])
+def test_order4_records(n, rank, shuffled, entry):
+    """Order 4 through the host-buffer entries: 16-byte records {row, a, b, c}
+    in the caller's product order, values in their own array permuted with
+    them when the input is not sorted by the output mode; >= 4M nonzeros also
+    runs the row-range result copy.  Every mode, a rotated and a reversed
+    mats_order, against the FP64 oracle."""
+    rng = np.random.default_rng(n + rank)
+    ndims = [700, 500, 300, 60]
+    inds = np.stack([rng.integers(0, d, n) for d in ndims]).astype(np.uint32)
+    inds[0, rng.random(n) < 0.2] = 123                      # one heavy row in mode 0
+    order = rng.permutation(n) if shuffled else np.lexsort(inds[::-1])
+    inds = np.ascontiguousarray(inds[:, order])
+    vals = rng.uniform(-1, 1, n).astype(np.float32)
+    t = S.Tensor.from_arrays(ndims, inds, vals)
+    mats = [S.Matrix.from_array(rng.uniform(-1, 1, (d, rank)).astype(np.float32)) for d in ndims]
+    mats.append(S.Matrix(max(ndims), rank))
+    facs = [m.array()[: ndims[k]].copy() for k, m in enumerate(mats[:4])]
+    for mode in range(4):
+        others = [(mode + i) % 4 for i in range(1, 4)]
+        for mo in ([mode] + others, [mode] + others[::-1]):
+            out = S.mttkrp(t, mats, mode, mats_order=mo, entry=entry)
+            ref = O.mttkrp(ndims, inds, vals, facs, rank, mode, precision="f64_omp")
+            assert rel_fro(out, ref) <= TOL, (mode, mo)
+            assert not mats[4].array()[: ndims[mode], rank:].any()

@@ -62,6 +62,7 @@ def test_fp32_and_bf16_against_fp64_oracle(tensor, rank):
     d16 = [f.to(torch.bfloat16).contiguous() for f in d32]
     out = torch.zeros((max(ndims), stride), dtype=torch.float32, device="cuda")
     coo = S.DeviceCoo(t)
+    coo.set_timing(True)
     for mode in range(4):
         order = [mode] + [(mode + i) % 4 for i in range(1, 4)]
         coo.prepare(mode)
@@ -72,8 +73,15 @@ def test_fp32_and_bf16_against_fp64_oracle(tensor, rank):
         coo.mttkrp(mode, order, [p.data_ptr() for p in d16], rank, stride, out.data_ptr(), bf16=True)
         torch.cuda.synchronize()
         e16 = rel_fro(out[: ndims[mode], :rank].cpu().numpy(), ref)
-        _results.append({"rank": rank, "mode": mode, "fp32_rel_fro": e32, "bf16_rel_fro": e16})
-        print("rank %d mode %d  fp32 %.3e  bf16 %.3e" % (rank, mode, e32, e16))
+        # kernel time of a repeated call (CUDA events around the launch)
+        ms = {}
+        for key, ptrs, b in (("fp32", d32, False), ("bf16", d16, True)):
+            coo.mttkrp(mode, order, [p.data_ptr() for p in ptrs], rank, stride, out.data_ptr(), bf16=b)
+            ms[key] = coo.last_ms()
+        _results.append({"rank": rank, "mode": mode, "fp32_rel_fro": e32, "bf16_rel_fro": e16,
+                         "fp32_ms": ms["fp32"], "bf16_ms": ms["bf16"]})
+        print("rank %d mode %d  fp32 %.3e  bf16 %.3e  (%.3f / %.3f ms)" % (rank, mode, e32, e16, ms["fp32"],
+                                                                         ms["bf16"]))
         assert e32 <= FP32_TOL, (rank, mode, e32)
         assert e16 <= BF16_TOL, (rank, mode, e16)
         assert e16 > e32
