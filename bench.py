@@ -67,7 +67,7 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--nnz", type=int, default=100_000_000)
     p.add_argument("--cpu-sample", type=int, default=10_000_000)
-    p.add_argument("--e2e-steps", type=int, default=5)
+    p.add_argument("--e2e-steps", type=int, default=20)
     p.add_argument("--skip-cpu", action="store_true")
     p.add_argument("--serve-requests", type=int, default=4096)
     p.add_argument("--plain-sample", type=int, default=256)
@@ -731,6 +731,7 @@ def run_ours(args, world, rank, local):
             "e2e": {"value": round(e2e, 2), "unit": "GB/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "entry": "sptCudaMTTKRP (host buffers)", "ms_per_step": e_s * 1e3,
                     "ms_each_step": [round(x * 1e3, 2) for x in e_each],
+                    "ms_median_step": round(float(np.median(e_each)) * 1e3, 2),
                     "host_link_h2d_gbs": link_gbs,
                     "link_floor_ms": round((h2d + d2h) / (link_gbs * 1e9) * 1e3, 2) if link_gbs else None},
             "gpu_launches": int(n1 - n0),
