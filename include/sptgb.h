@@ -31,6 +31,18 @@ uint64_t sptgbLaunchCount(void);
  * sptCpdAls (the reference seeds with time(NULL), matrix.c:69). */
 void  sptgbSetSeed(uint64_t seed);
 
+/* Page-locks (cudaHostRegister) the host arrays of a tensor or a matrix for
+ * callers that pass the same host objects to many calls: the host-buffer
+ * entry points (sptMTTKRP, sptCudaMTTKRP, sptCpdAls, ...) then copy them by
+ * DMA without address translation of pageable pages.  The arrays must not be
+ * reallocated or freed while pinned; unpin before freeing.  Pinning pinned
+ * memory, or unpinning memory that is not pinned, returns
+ * SPTERR_CUDA_ERROR + the CUDA error code. */
+int sptgbPinSparseTensor(const sptSparseTensor *X);
+int sptgbUnpinSparseTensor(const sptSparseTensor *X);
+int sptgbPinMatrix(const sptMatrix *M);
+int sptgbUnpinMatrix(const sptMatrix *M);
+
 /* ------------------------------------------- device-resident COO tensor --
  * A COO tensor uploaded once.  sptgbCooPrepareMode builds, on the device,
  * the copy sorted by `mode` (mode first, then the remaining modes in

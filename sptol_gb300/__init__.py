@@ -184,6 +184,10 @@ def _declare(L):
         "sptgbStream": (C.c_void_p, []),
         "sptgbLaunchCount": (C.c_uint64, []),
         "sptgbSetSeed": (None, [C.c_uint64]),
+        "sptgbPinSparseTensor": (C.c_int, [T]),
+        "sptgbUnpinSparseTensor": (C.c_int, [T]),
+        "sptgbPinMatrix": (C.c_int, [M]),
+        "sptgbUnpinMatrix": (C.c_int, [M]),
         "sptgbGenerate": (C.c_int, [T, C.POINTER(GenSpec)]),
         "sptgbFillMatrix": (C.c_int, [M, C.c_uint64, C.c_uint64, C.c_float, C.c_float]),
         "sptgbCpdAls": (C.c_int, [T, C.c_uint32, C.c_uint32, C.c_double, MM, f32p, C.POINTER(C.c_double),

@@ -296,3 +296,33 @@ def test_order4_records(n, rank, shuffled, entry):
             ref = O.mttkrp(ndims, inds, vals, facs, rank, mode, precision="f64_omp")
             assert rel_fro(out, ref) <= TOL, (mode, mo)
             assert not mats[4].array()[: ndims[mode], rank:].any()
+
+
+def test_pinned_host_buffers_give_the_same_result():
+    """sptgbPinSparseTensor / sptgbPinMatrix: the host-buffer entry on page-
+    locked caller arrays returns the same bits as on pageable ones; pinning
+    twice and unpinning what is not pinned are errors."""
+    import ctypes as C
+    rng = np.random.default_rng(5)
+    ndims = [400, 300, 200]
+    n = 50_000
+    inds = np.stack([rng.integers(0, d, n) for d in ndims]).astype(np.uint32)
+    vals = rng.uniform(-1, 1, n).astype(np.float32)
+    t = S.Tensor.from_arrays(ndims, inds, vals)
+    mats = [S.Matrix.from_array(rng.uniform(0, 1, (d, 16)).astype(np.float32)) for d in ndims]
+    mats.append(S.Matrix(max(ndims), 16))
+    plain = [S.mttkrp(t, mats, m, entry="sptCudaMTTKRP") for m in range(3)]
+    L = S.lib()
+    assert L.sptgbPinSparseTensor(t.ptr()) == 0
+    for m in mats:
+        assert L.sptgbPinMatrix(C.byref(m.s)) == 0
+    try:
+        assert L.sptgbPinSparseTensor(t.ptr()) != 0          # already pinned
+        for mode in range(3):
+            assert np.array_equal(S.mttkrp(t, mats, mode, entry="sptCudaMTTKRP"), plain[mode])
+    finally:
+        assert L.sptgbUnpinSparseTensor(t.ptr()) == 0
+        for m in mats:
+            assert L.sptgbUnpinMatrix(C.byref(m.s)) == 0
+    assert L.sptgbUnpinMatrix(C.byref(mats[0].s)) != 0      # not pinned any more
+    S.lib().sptClearLastError()
