@@ -418,7 +418,7 @@ def peaks():
 
 def traffic_per_launch():
     """DRAM bytes per MTTKRP launch from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", "mttkrp_coo_c2.md")
+    path = os.path.join(ROOT, "profiles", "mttkrp_coo_powerlaw_100m.md")
     try:
         for line in open(path):
             if line.startswith("traffic_bytes_per_launch:"):

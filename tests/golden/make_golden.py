@@ -11,7 +11,7 @@ outputs:
   cpd_*.npz      corrected fit after every iteration of the reference's
                  CP-ALS loop, final factors and lambda (the loop is checked
                  here to end bit-for-bit where CpdAlsStep ends)
-  c1_summary.npz per-mode norms, sums and sample rows of sptMTTKRP on the
+  uniform_1m_summary.npz per-mode norms, sums and sample rows of sptMTTKRP on the
                  1024^3 / 1,000,000-draw tensor of the library generator
 Needs the reference sources (only present where the fixtures are made):
     python tests/golden/make_golden.py
@@ -112,7 +112,7 @@ def cpd_case(name, seed, ndims, n, rank, niters, noise):
          lam=t["loop_lambda"], **kw)
 
 
-def c1_summary():
+def uniform_1m_summary():
     import sptol_gb300 as S
     spec = S.GenSpec()
     spec.seed = 0
@@ -135,7 +135,7 @@ def c1_summary():
         kw["norm%d" % m] = np.sqrt((out ** 2).sum())
         kw["sum%d" % m] = out.sum()
         kw["rows%d" % m] = out[rows]
-    save("c1_summary", nnz=inds.shape[1], key_checksum=np.uint64(
+    save("uniform_1m_summary", nnz=inds.shape[1], key_checksum=np.uint64(
         (inds[0].astype(np.uint64) * 1048576 * 1024 + inds[1].astype(np.uint64) * 1024 + inds[2]).sum()),
          val_sum=np.float64(vals.astype(np.float64).sum()), sample_rows=rows, **kw)
 
@@ -152,7 +152,7 @@ def main():
     mttkrp_case("mttkrp_4d_r8", 33, [40, 30, 20, 10], 5000, 8)
     cpd_case("cpd_3d", 41, [30, 25, 20], 6000, 5, 10, 0.01)
     cpd_case("cpd_4d", 42, [12, 10, 9, 8], 4000, 3, 8, 0.01)
-    c1_summary()
+    uniform_1m_summary()
 
 
 if __name__ == "__main__":

@@ -5,8 +5,8 @@ iterations, FP32 MTTKRP with FP64 / double-float dense pieces on the GPU
 (sptgbCpdAls) against the FP64 oracle restatement of sptCpdAls (pinned to the
 reference's CpdAlsStep trace).  Tolerance: fit within 1e-4 at every iteration.
 
-The default size (2M nonzeros) runs in seconds; SPTGB_C4_NNZ=50000000 runs the
-full 50M-nonzero case and SPTGB_C4_REPORT=<file> writes fits and times as JSON.
+The default size (2M nonzeros) runs in seconds; SPTGB_CPALS_NNZ=50000000 runs the
+full 50M-nonzero case and SPTGB_CPALS_REPORT=<file> writes fits and times as JSON.
 """
 import json
 import os
@@ -20,7 +20,7 @@ import sptol_gb300 as S
 
 pytestmark = pytest.mark.gpu
 DIMS = [500_000, 300_000, 10_000]
-NNZ = int(float(os.environ.get("SPTGB_C4_NNZ", "2000000")))
+NNZ = int(float(os.environ.get("SPTGB_CPALS_NNZ", "2000000")))
 RANK, ITERS = 32, 20
 FIT_TOL = 1e-4
 
@@ -56,7 +56,7 @@ def test_planted_cpd_fits_match_oracle():
     diff = np.abs(fits - ofits)
     print("nnz %d  gpu %.2f s (%d iterations, upload and sort included)  oracle %.1f s  max |dfit| %.2e"
           % (t.nnz, gpu_s, ITERS, oracle_s, diff.max()))
-    report = os.environ.get("SPTGB_C4_REPORT")
+    report = os.environ.get("SPTGB_CPALS_REPORT")
     if report:
         with open(report, "w") as f:
             json.dump({"dims": DIMS, "nnz": int(t.nnz), "rank": RANK, "iterations": ITERS, "gpu_s": gpu_s,

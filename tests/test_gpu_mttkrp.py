@@ -166,7 +166,7 @@ def _c1_tensor():
 
 def test_c1_full_size_against_reference_summary_and_oracle():
     """The 1024^3 / 1,000,000-draw tensor, rank 16, every mode."""
-    g = golden("c1_summary")
+    g = golden("uniform_1m_summary")
     t = _c1_tensor()
     assert t.nnz == int(g["nnz"])
     inds, vals = t.arrays()
@@ -189,10 +189,10 @@ def test_c2_power_law_against_fp64():
     modes 0 and 1, lognormal values), rank 32: ours against the FP64 oracle
     within 1e-5 for every mode, and the reference-order sequential FP32 sum
     against FP64 reported beside it (its error on the hot rows is why this
-    tensor is adjudicated against FP64).  SPTGB_C2_NNZ (default 5M) sets the
+    tensor is adjudicated against FP64).  SPTGB_POWERLAW_NNZ (default 5M) sets the
     size; 100000000 is the full tensor."""
     import os
-    nnz = int(float(os.environ.get("SPTGB_C2_NNZ", "5000000")))
+    nnz = int(float(os.environ.get("SPTGB_POWERLAW_NNZ", "5000000")))
     dims = [4_000_000, 2_000_000, 25_000]
     spec = S.GenSpec()
     spec.seed = 20261203

@@ -7,8 +7,8 @@ Bounds: FP32 <= 1e-5 (the parity bar); BF16 <= 1e-2 (a BF16 factor entry
 carries a relative rounding error of at most 2^-9 ~ 2e-3; products of three
 factors and sums with cancellation stay well inside 1e-2).
 
-The default size (2M nonzeros) runs in seconds; SPTGB_C3_NNZ=200000000 runs the
-full 200M-nonzero study, and SPTGB_C3_REPORT=<file> writes the error table as
+The default size (2M nonzeros) runs in seconds; SPTGB_PRECISION_NNZ=200000000 runs the
+full 200M-nonzero study, and SPTGB_PRECISION_REPORT=<file> writes the error table as
 JSON.
 """
 import json
@@ -23,7 +23,7 @@ from conftest import rel_fro
 
 pytestmark = pytest.mark.gpu
 DIMS = [10_000, 5_000, 2_000, 500]
-NNZ = int(float(os.environ.get("SPTGB_C3_NNZ", "2000000")))
+NNZ = int(float(os.environ.get("SPTGB_PRECISION_NNZ", "2000000")))
 FP32_TOL = 1e-5
 BF16_TOL = 1e-2
 _results = []
@@ -42,7 +42,7 @@ def tensor():
     spec.value_dist = S.VAL_UPM1
     t = S.Tensor.generate(spec)
     yield t
-    report = os.environ.get("SPTGB_C3_REPORT")
+    report = os.environ.get("SPTGB_PRECISION_REPORT")
     if report and _results:
         with open(report, "w") as f:
             json.dump({"dims": DIMS, "nnz": NNZ, "values": "U[-1,1)", "factors": "U[0,1)", "results": _results}, f,

@@ -79,11 +79,11 @@ def test_cpd_fits(case):
                - g["fits"][-1]) <= 1e-6
 
 
-def test_c1_summary_from_generator():
+def test_uniform_1m_summary_from_generator():
     """The library generator reproduces the 1024^3 tensor the summary was taken
     on, and the oracle reproduces the reference's per-mode outputs on it."""
     import sptol_gb300 as S
-    g = golden("c1_summary")
+    g = golden("uniform_1m_summary")
     spec = S.GenSpec()
     spec.seed = 0
     spec.nmodes = 3
