@@ -164,7 +164,7 @@ def _c1_tensor():
     return S.Tensor.generate(spec)
 
 
-def test_c1_full_size_against_reference_summary_and_oracle():
+def test_uniform_1m_full_size_against_reference_summary_and_oracle():
     """The 1024^3 / 1,000,000-draw tensor, rank 16, every mode."""
     g = golden("uniform_1m_summary")
     t = _c1_tensor()
@@ -184,7 +184,7 @@ def test_c1_full_size_against_reference_summary_and_oracle():
         assert rel_fro(out[rows], g["rows%d" % mode]) <= TOL
 
 
-def test_c2_power_law_against_fp64():
+def test_power_law_against_fp64():
     """The 4,000,000 x 2,000,000 x 25,000 power-law tensor (Zipf(1.2) on
     modes 0 and 1, lognormal values), rank 32: ours against the FP64 oracle
     within 1e-5 for every mode, and the reference-order sequential FP32 sum
