@@ -106,9 +106,10 @@ def test_uniform_1m_summary_from_generator():
 
 
 @pytest.mark.skipif(not O.ref_available(), reason="reference sources not present")
-def test_reference_library_agrees_with_oracle_on_fresh_inputs():
-    rng = np.random.default_rng(99)
-    ndims = [70, 60, 50]
+@pytest.mark.parametrize("ndims", [[70, 60, 50], [30, 25, 20, 15]])
+def test_reference_library_agrees_with_oracle_on_fresh_inputs(ndims):
+    rng = np.random.default_rng(99 + len(ndims))
+    N = len(ndims)
     inds = np.unique(np.stack([rng.integers(0, d, 9000) for d in ndims]).astype(np.uint32), axis=1)
     inds = inds[:, rng.permutation(inds.shape[1])]
     vals = rng.random(inds.shape[1], dtype=np.float32)
@@ -116,9 +117,11 @@ def test_reference_library_agrees_with_oracle_on_fresh_inputs():
     p = O.sort_lex(inds)
     assert np.array_equal(si, inds[:, p])
     mats = [rng.random((d, 8), dtype=np.float32) for d in ndims]
-    for mode in range(3):
-        r, _ = O.ref_mttkrp(ndims, inds, vals, mats, 8, mode)
-        assert np.array_equal(r, O.mttkrp(ndims, inds, vals, mats, 8, mode))
+    for mode in range(N):
+        others = [(mode + i) % N for i in range(1, N)]
+        for order in ([mode] + others, [mode] + others[::-1]):
+            r, _ = O.ref_mttkrp(ndims, inds, vals, mats, 8, mode, order=order)
+            assert np.array_equal(r, O.mttkrp(ndims, inds, vals, mats, 8, mode, order=order)), (mode, order)
 
 
 def test_threaded_fp64_oracle_equals_sequential():
