@@ -155,3 +155,27 @@ def test_ttm_oracle_equals_reference(mode):
         if m != mode:
             assert np.array_equal(fib[m], rfib[m])
     assert np.array_equal(Y.view(np.uint32), rY.view(np.uint32))
+
+
+@pytest.mark.skipif(not O.ref_available(), reason="reference sources not present")
+@pytest.mark.parametrize("ndims,sb,sk", [([300, 200, 100], 3, 6), ([40, 30, 20, 10], 2, 4)])
+def test_reference_hicoo_agrees_with_oracle_on_fresh_inputs(ndims, sb, sk):
+    """The HiCOO restatement against the reference library built from its
+    sources: sort order, every conversion array and the HiCOO MTTKRP of each
+    mode, bit for bit, on fresh shuffled coordinates."""
+    rng = np.random.default_rng(7 + len(ndims))
+    N = len(ndims)
+    inds = np.unique(np.stack([rng.integers(0, d, 6000) for d in ndims]).astype(np.uint32), axis=1)
+    inds = inds[:, rng.permutation(inds.shape[1])]
+    vals = rng.random(inds.shape[1], dtype=np.float32)
+    ri, rv, rh = O.ref_hicoo(ndims, inds, vals, sb, sk)
+    p = O.sort_hicoo(inds, sk)
+    assert np.array_equal(ri, inds[:, p]) and np.array_equal(rv, vals[p])
+    h = O.hicoo_build(ndims, inds[:, p], sb, sk)
+    for k in ("kptr", "cptr", "bptr", "binds", "einds", "nkiters", "kschr_len", "kschr"):
+        assert np.array_equal(h[k], rh[k]), k
+    assert h["max_nnzb"] == rh["max_nnzb"]
+    mats = [rng.random((d, 8), dtype=np.float32) for d in ndims]
+    for mode in range(N):
+        r = O.ref_mttkrp_hicoo(ndims, inds, vals, sb, sk, mats, 8, mode)
+        assert np.array_equal(r, O.mttkrp_hicoo(ndims, h, vals[p], sb, mats, 8, mode)), mode
