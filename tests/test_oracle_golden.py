@@ -179,3 +179,23 @@ def test_reference_hicoo_agrees_with_oracle_on_fresh_inputs(ndims, sb, sk):
     for mode in range(N):
         r = O.ref_mttkrp_hicoo(ndims, inds, vals, sb, sk, mats, 8, mode)
         assert np.array_equal(r, O.mttkrp_hicoo(ndims, h, vals[p], sb, mats, 8, mode)), mode
+
+
+@pytest.mark.skipif(not O.ref_available(), reason="reference sources not present")
+@pytest.mark.parametrize("ndims,rank", [([60, 50, 40], 6), ([25, 20, 15, 10], 4)])
+def test_reference_cpd_agrees_with_oracle_on_fresh_inputs(ndims, rank):
+    """The FP64 CP-ALS restatement against the reference's own loop (built
+    from its sources) from the same initial factors: the fit of every
+    iteration within 1e-5 (FP64 against the reference's FP32 arithmetic)."""
+    rng = np.random.default_rng(31 + len(ndims))
+    inds = np.unique(np.stack([rng.integers(0, d, 4000) for d in ndims]).astype(np.uint32), axis=1)
+    vals = rng.random(inds.shape[1], dtype=np.float32)
+    init = [rng.random((d, rank), dtype=np.float32) for d in ndims]
+    niters = 6
+    ref = O.ref_cpd_trace(ndims, inds, vals, rank, niters, init)
+    # the traced loop is the reference's CpdAlsStep, bit for bit
+    assert all(np.array_equal(a, b) for a, b in zip(ref["loop_factors"], ref["step_factors"]))
+    assert np.array_equal(ref["loop_lambda"], ref["step_lambda"])
+    facs, lam, fits, it = O.cpd_als(ndims, inds, vals, rank, niters, 0.0, init)
+    assert it == niters
+    assert np.abs(np.asarray(fits) - ref["fits"]).max() <= 1e-5
