@@ -125,6 +125,7 @@ def ref():
         L.ref_ttm.restype = C.c_uint64
         L.ref_ttm.argtypes = [C.c_uint32, u32p, C.c_uint64, C.POINTER(u32p), f32p, C.c_uint32, f32p, C.c_uint32,
                               C.c_uint32, C.POINTER(u32p), f32p, u32p]
+        L.ref_load_tns.argtypes = [C.c_char_p, C.c_uint32, u32p, u32p, C.c_uint64, C.POINTER(u32p), f32p, u64p]
         _REF = L
     return _REF
 
@@ -455,6 +456,28 @@ def load_tns(path, start_index=1):
         raise ValueError("reader returned %d" % rc)
     n = int(nnz.value)
     return [int(nd[m]) for m in range(N.value)], np.stack([a[:n] for a in arrs[: N.value]]), vals[:n].copy()
+
+
+def _read_tns(fn, path, start_index):
+    size = os.path.getsize(path)
+    cap = size // 2 + 2
+    N = C.c_uint32()
+    nd = (C.c_uint32 * 8)()
+    arrs = [np.zeros(cap, np.uint32) for _ in range(8)]
+    ptrs = (u32p * 8)(*[a.ctypes.data_as(u32p) for a in arrs])
+    vals = np.zeros(cap, np.float32)
+    nnz = C.c_uint64()
+    rc = fn(path.encode(), start_index, C.byref(N), nd, cap, ptrs, vals.ctypes.data_as(f32p), C.byref(nnz))
+    if rc != 0:
+        raise ValueError("reader returned %d" % rc)
+    n = int(nnz.value)
+    return [int(nd[m]) for m in range(N.value)], np.stack([a[:n] for a in arrs[: N.value]]), vals[:n].copy()
+
+
+def ref_load_tns(path, start_index=1):
+    """The reference's own sptLoadSparseTensor (built from its sources), same
+    return convention as load_tns."""
+    return _read_tns(ref().ref_load_tns, path, start_index)
 
 
 def ttm(ndims, inds, vals, U, mode, sort=True):

@@ -291,3 +291,31 @@ uint64_t ref_ttm(uint32_t nmodes, const uint32_t *ndims, uint64_t nnz, uint32_t 
     sptFreeSparseTensor(&X);
     return nf;
 }
+
+/* The reference's text reader, sptLoadSparseTensor (sptensor/load.c with
+ * collect.c): the tensor it builds copied out into caller arrays of `cap`
+ * entries.  Returns the reader's own code (or -2 when the file does not
+ * open, -3 when cap is too small or the order above 8). */
+int ref_load_tns(const char *path, uint32_t start_index, uint32_t *nmodes_out, uint32_t *ndims_out, uint64_t cap,
+                 uint32_t *const *inds, float *vals, uint64_t *nnz_out) {
+    FILE *fp = fopen(path, "r");
+    if (!fp) return -2;
+    sptSparseTensor X;
+    memset(&X, 0, sizeof X);
+    const int r = sptLoadSparseTensor(&X, start_index, fp);
+    fclose(fp);
+    if (r) return r;
+    if (X.nmodes > 8 || X.nnz > cap) {
+        sptFreeSparseTensor(&X);
+        return -3;
+    }
+    *nmodes_out = X.nmodes;
+    for (uint32_t m = 0; m < X.nmodes; ++m) {
+        ndims_out[m] = X.ndims[m];
+        memcpy(inds[m], X.inds[m].data, X.nnz * sizeof(uint32_t));
+    }
+    memcpy(vals, X.values.data, X.nnz * sizeof(float));
+    *nnz_out = X.nnz;
+    sptFreeSparseTensor(&X);
+    return 0;
+}

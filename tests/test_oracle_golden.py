@@ -199,3 +199,39 @@ def test_reference_cpd_agrees_with_oracle_on_fresh_inputs(ndims, rank):
     facs, lam, fits, it = O.cpd_als(ndims, inds, vals, rank, niters, 0.0, init)
     assert it == niters
     assert np.abs(np.asarray(fits) - ref["fits"]).max() <= 1e-5
+
+
+_TNS_CASES = {
+    "basic": ("3\n4 5 6\n1 1 1 1.5\n4 5 6 -2.25e-3\n2 3 1 7\n1 2 3 0.1\n", 1),
+    "zeros_removed": ("3\n3 3 3\n1 1 1 0\n2 2 2 3.5\n3 3 3 0.0\n1 2 3 -0\n2 1 1 4e1\n", 1),
+    "duplicates_kept": ("2\n4 4\n1 1 2.0\n1 1 3.0\n4 4 1\n1 1 2.0\n", 1),
+    "zero_based": ("3\n2 2 2\n0 0 0 1\n1 1 1 2\n0 1 0 3.25\n", 0),
+    "crlf_and_spaces": ("3\r\n2 3 4\r\n 1\t2  3  9.5\r\n2 3 4 1E-2 \r\n\r\n", 1),
+    "four_modes": ("4\n3 4 5 6\n1 2 3 4 1\n3 4 5 6 2\n2 2 2 2 -3.5\n", 1),
+    "invalid_token_ends": ("3\n3 3 3\n1 1 1 1\n2 x 2 2\n3 3 3 3\n", 1),
+    "trailing_garbage_value": ("3\n3 3 3\n1 1 1 1.5zz\n2 2 2 2\n", 1),
+    "empty_body": ("3\n3 3 3\n", 1),
+}
+
+
+@pytest.mark.skipif(not O.ref_available(), reason="reference sources not present")
+@pytest.mark.parametrize("case", sorted(_TNS_CASES))
+def test_reference_reader_agrees_with_oracle(tmp_path, case):
+    """The text-reader restatement against the reference's own
+    sptLoadSparseTensor: order, mode sizes, coordinates and values bit for
+    bit (zero removal, duplicates, 0/1-based indices, the first unreadable
+    token ending the tensor)."""
+    text, start = _TNS_CASES[case]
+    path = str(tmp_path / (case + ".tns"))
+    with open(path, "w", newline="") as f:
+        f.write(text)
+    try:
+        ref = O.ref_load_tns(path, start)
+    except ValueError as e:
+        with pytest.raises(ValueError) as mine:
+            O.load_tns(path, start)
+        assert str(mine.value) == str(e)
+        return
+    got = O.load_tns(path, start)
+    assert got[0] == ref[0]
+    assert np.array_equal(got[1], ref[1]) and np.array_equal(got[2].view(np.uint32), ref[2].view(np.uint32))
