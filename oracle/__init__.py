@@ -126,6 +126,12 @@ def ref():
         L.ref_ttm.argtypes = [C.c_uint32, u32p, C.c_uint64, C.POINTER(u32p), f32p, C.c_uint32, f32p, C.c_uint32,
                               C.c_uint32, C.POINTER(u32p), f32p, u32p]
         L.ref_load_tns.argtypes = [C.c_char_p, C.c_uint32, u32p, u32p, C.c_uint64, C.POINTER(u32p), f32p, u64p]
+        L.ref_dotmul_triangle.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(f32p), C.c_uint32, f32p]
+        L.ref_colnorm.argtypes = [C.c_int, C.c_uint32, C.c_uint32, f32p, C.c_uint32, f32p]
+        L.ref_kruskal_normsq.restype = C.c_double
+        L.ref_kruskal_normsq.argtypes = [C.c_uint32, C.c_uint32, C.POINTER(f32p), C.c_uint32, f32p]
+        L.ref_kruskal_inner.restype = C.c_double
+        L.ref_kruskal_inner.argtypes = [C.c_uint32, C.c_uint32, u32p, C.POINTER(f32p), f32p, C.c_uint32, f32p]
         _REF = L
     return _REF
 
@@ -472,6 +478,49 @@ def _read_tns(fn, path, start_index):
         raise ValueError("reader returned %d" % rc)
     n = int(nnz.value)
     return [int(nd[m]) for m in range(N.value)], np.stack([a[:n] for a in arrs[: N.value]]), vals[:n].copy()
+
+
+def _padded(a, stride):
+    f = np.zeros((a.shape[0], stride), np.float32)
+    f[:, : a.shape[1]] = a
+    return f
+
+
+def ref_dotmul_triangle(grams, mode):
+    """sptMatrixDotMulSeqTriangle on R x R Grams; returns the R x R result."""
+    R = grams[0].shape[1]
+    st = stride_of(R)
+    gk, gp = _rows([_padded(g, st) for g in grams], f32p, np.float32)
+    out = np.zeros((R, st), np.float32)
+    assert ref().ref_dotmul_triangle(len(grams), mode, R, gp, st, out.ctypes.data_as(f32p)) == 0
+    return out[:, :R]
+
+
+def ref_colnorm(A, use_max):
+    """sptMatrix2Norm (use_max False) or sptMatrixMaxNorm: (normalised A, lambda)."""
+    n, R = A.shape
+    st = stride_of(R)
+    a = _padded(A, st)
+    lam = np.zeros(R, np.float32)
+    assert ref().ref_colnorm(int(use_max), n, R, a.ctypes.data_as(f32p), st, lam.ctypes.data_as(f32p)) == 0
+    return a[:, :R], lam
+
+
+def ref_kruskal_normsq(ata, lam):
+    R = ata[0].shape[1]
+    st = stride_of(R)
+    ak, ap = _rows([_padded(g, st) for g in ata], f32p, np.float32)
+    return ref().ref_kruskal_normsq(len(ata), R, ap, st, np.ascontiguousarray(lam, np.float32).ctypes.data_as(f32p))
+
+
+def ref_kruskal_inner(facs, mout, lam):
+    R = facs[0].shape[1]
+    st = stride_of(R)
+    fk, fp = _rows([_padded(f, st) for f in facs], f32p, np.float32)
+    nd, ndp = _u32([f.shape[0] for f in facs])
+    mo = _padded(mout, st)
+    return ref().ref_kruskal_inner(len(facs), R, ndp, fp, mo.ctypes.data_as(f32p), st,
+                                   np.ascontiguousarray(lam, np.float32).ctypes.data_as(f32p))
 
 
 def ref_load_tns(path, start_index=1):

@@ -319,3 +319,65 @@ int ref_load_tns(const char *path, uint32_t start_index, uint32_t *nmodes_out, u
     sptFreeSparseTensor(&X);
     return 0;
 }
+
+/* The reference's dense CP-ALS helpers on flat R x stride (Grams) or
+ * nrows x stride (factors) arrays: sptMatrixDotMulSeqTriangle,
+ * sptMatrix2Norm / sptMatrixMaxNorm, sptKruskalTensorFrobeniusNormSquared and
+ * sptSparseKruskalTensorInnerProduct. */
+static sptMatrix *mat_from(uint32_t nrows, uint32_t R, const float *vals, uint32_t stride) {
+    sptMatrix *M = (sptMatrix *)malloc(sizeof(sptMatrix));
+    sptNewMatrix(M, nrows, R);
+    if (M->stride != stride) abort();
+    if (vals) memcpy(M->values, vals, (size_t)nrows * stride * sizeof(float));
+    else memset(M->values, 0, (size_t)M->cap * stride * sizeof(float));
+    return M;
+}
+
+static void mats_free(sptMatrix **M, uint32_t n) {
+    for (uint32_t m = 0; m < n; ++m) {
+        sptFreeMatrix(M[m]);
+        free(M[m]);
+    }
+}
+
+int ref_dotmul_triangle(uint32_t nmodes, uint32_t mode, uint32_t R, float *const *grams, uint32_t stride, float *out) {
+    sptMatrix *M[9];
+    if (nmodes > 8) return -3;
+    for (uint32_t m = 0; m < nmodes; ++m) M[m] = mat_from(R, R, grams[m], stride);
+    M[nmodes] = mat_from(R, R, NULL, stride);
+    const int r = sptMatrixDotMulSeqTriangle(mode, nmodes, M);
+    memcpy(out, M[nmodes]->values, (size_t)R * stride * sizeof(float));
+    mats_free(M, nmodes + 1);
+    return r;
+}
+
+int ref_colnorm(int use_max, uint32_t nrows, uint32_t R, float *A, uint32_t stride, float *lambda) {
+    sptMatrix *M = mat_from(nrows, R, A, stride);
+    const int r = use_max ? sptMatrixMaxNorm(M, lambda) : sptMatrix2Norm(M, lambda);
+    memcpy(A, M->values, (size_t)nrows * stride * sizeof(float));
+    mats_free(&M, 1);
+    return r;
+}
+
+double ref_kruskal_normsq(uint32_t nmodes, uint32_t R, float *const *ata, uint32_t stride, const float *lambda) {
+    sptMatrix *M[9];
+    if (nmodes > 8) return NAN;
+    for (uint32_t m = 0; m < nmodes; ++m) M[m] = mat_from(R, R, ata[m], stride);
+    M[nmodes] = mat_from(R, R, NULL, stride);
+    const double v = sptKruskalTensorFrobeniusNormSquared(nmodes, (sptValue *)lambda, M);
+    mats_free(M, nmodes + 1);
+    return v;
+}
+
+/* mats[0..nmodes-1]: factors (only the last one is read), mout: the last
+ * mode's MTTKRP output, both I x stride with I the last mode's size. */
+double ref_kruskal_inner(uint32_t nmodes, uint32_t R, const uint32_t *ndims, float *const *mats, const float *mout,
+                         uint32_t stride, const float *lambda) {
+    sptMatrix *M[9];
+    if (nmodes > 8) return NAN;
+    for (uint32_t m = 0; m < nmodes; ++m) M[m] = mat_from(ndims[m], R, mats[m], stride);
+    M[nmodes] = mat_from(ndims[nmodes - 1], R, mout, stride);
+    const double v = sptSparseKruskalTensorInnerProduct(nmodes, (sptValue *)lambda, M);
+    mats_free(M, nmodes + 1);
+    return v;
+}
