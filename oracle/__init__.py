@@ -130,6 +130,8 @@ def ref():
         L.ref_colnorm.argtypes = [C.c_int, C.c_uint32, C.c_uint32, f32p, C.c_uint32, f32p]
         L.ref_kruskal_normsq.restype = C.c_double
         L.ref_kruskal_normsq.argtypes = [C.c_uint32, C.c_uint32, C.POINTER(f32p), C.c_uint32, f32p]
+        L.ref_solve_normals.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(f32p), C.c_uint32, C.c_uint32,
+                                        f32p]
         L.ref_kruskal_inner.restype = C.c_double
         L.ref_kruskal_inner.argtypes = [C.c_uint32, C.c_uint32, u32p, C.POINTER(f32p), f32p, C.c_uint32, f32p]
         _REF = L
@@ -504,6 +506,16 @@ def ref_colnorm(A, use_max):
     lam = np.zeros(R, np.float32)
     assert ref().ref_colnorm(int(use_max), n, R, a.ctypes.data_as(f32p), st, lam.ctypes.data_as(f32p)) == 0
     return a[:, :R], lam
+
+
+def ref_solve_normals(grams, mode, rhs):
+    """sptMatrixSolveNormals: X with X G = rhs (G the Hadamard of the other Grams)."""
+    R = grams[0].shape[1]
+    st = stride_of(R)
+    gk, gp = _rows([_padded(g, st) for g in grams], f32p, np.float32)
+    b = _padded(rhs, st)
+    assert ref().ref_solve_normals(len(grams), mode, R, gp, st, rhs.shape[0], b.ctypes.data_as(f32p)) == 0
+    return b[:, :R]
 
 
 def ref_kruskal_normsq(ata, lam):

@@ -381,3 +381,19 @@ double ref_kruskal_inner(uint32_t nmodes, uint32_t R, const uint32_t *ndims, flo
     mats_free(M, nmodes + 1);
     return v;
 }
+
+/* sptMatrixSolveNormals (matrix_solver.c:32-83): rhs (nrows x stride) is
+ * overwritten with X, X G = rhs, G the Hadamard of the other Grams. */
+int ref_solve_normals(uint32_t nmodes, uint32_t mode, uint32_t R, float *const *grams, uint32_t stride, uint32_t nrows,
+                      float *rhs) {
+    sptMatrix *M[9];
+    if (nmodes > 8) return -3;
+    for (uint32_t m = 0; m < nmodes; ++m) M[m] = mat_from(R, R, grams[m], stride);
+    M[nmodes] = mat_from(R, R, NULL, stride);
+    sptMatrix *B = mat_from(nrows, R, rhs, stride);
+    const int r = sptMatrixSolveNormals(mode, nmodes, M, B);
+    memcpy(rhs, B->values, (size_t)nrows * stride * sizeof(float));
+    mats_free(M, nmodes + 1);
+    mats_free(&B, 1);
+    return r;
+}

@@ -70,3 +70,21 @@ def test_kruskal_norm_and_inner_product_formulas():
     inner = float((facs[2].astype(np.float64) * mout.astype(np.float64)).sum(0) @ lam)
     got = O.ref_kruskal_inner(facs, mout, lam)
     assert abs(got - inner) <= 1e-5 * abs(inner)
+
+
+@pytest.mark.parametrize("N,rank,mode", [(3, 16, 1), (4, 32, 3)])
+def test_solve_normals_formula(N, rank, mode):
+    """X G = rhs with G the Hadamard of the other Grams (upper triangles
+    mirrored): the reference's FP32 Cholesky solve against the FP64 formula
+    the GPU test uses, within the GPU test's own 1e-5 (condition numbers ~60-70)."""
+    rng = np.random.default_rng(7 + rank)
+    gs = _grams(rng, N, rank)
+    rhs = rng.uniform(-1, 1, (500, rank)).astype(np.float32)
+    got = O.ref_solve_normals(gs, mode, rhs)
+    full = [np.triu(g.astype(np.float64)) + np.triu(g.astype(np.float64), 1).T for g in gs]
+    H = np.ones((rank, rank))
+    for m in range(1, N):
+        H *= full[(mode + m) % N]
+    X = np.linalg.solve(H, rhs.astype(np.float64).T).T
+    err = np.linalg.norm(got - X) / np.linalg.norm(X)
+    assert err <= 1e-5, err
