@@ -132,6 +132,9 @@ def ref():
         L.ref_kruskal_normsq.argtypes = [C.c_uint32, C.c_uint32, C.POINTER(f32p), C.c_uint32, f32p]
         L.ref_solve_normals.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(f32p), C.c_uint32, C.c_uint32,
                                         f32p]
+        L.ref_dump_tensor.argtypes = [C.c_uint32, u32p, C.c_uint64, C.POINTER(u32p), f32p, C.c_uint32, C.c_char_p]
+        L.ref_dump_matrix.argtypes = [C.c_uint32, C.c_uint32, f32p, C.c_uint32, C.c_char_p]
+        L.ref_dump_arrays.argtypes = [u32p, C.c_uint64, u64p, C.c_uint64, C.c_char_p]
         L.ref_kruskal_inner.restype = C.c_double
         L.ref_kruskal_inner.argtypes = [C.c_uint32, C.c_uint32, u32p, C.POINTER(f32p), f32p, C.c_uint32, f32p]
         _REF = L
@@ -533,6 +536,27 @@ def ref_kruskal_inner(facs, mout, lam):
     mo = _padded(mout, st)
     return ref().ref_kruskal_inner(len(facs), R, ndp, fp, mo.ctypes.data_as(f32p), st,
                                    np.ascontiguousarray(lam, np.float32).ctypes.data_as(f32p))
+
+
+def ref_dump_tensor(ndims, inds, vals, start_index, path):
+    ik, ip = _rows(list(inds), u32p, np.uint32)
+    v = np.ascontiguousarray(vals, np.float32)
+    nd, ndp = _u32(ndims)
+    assert ref().ref_dump_tensor(len(ndims), ndp, inds.shape[1], ip, v.ctypes.data_as(f32p), start_index,
+                                 path.encode()) == 0
+
+
+def ref_dump_matrix(a, path):
+    n, R = a.shape
+    st = stride_of(R)
+    p = _padded(a, st)
+    assert ref().ref_dump_matrix(n, R, p.ctypes.data_as(f32p), st, path.encode()) == 0
+
+
+def ref_dump_arrays(a, b, path):
+    a = np.ascontiguousarray(a, np.uint32)
+    b = np.ascontiguousarray(b, np.uint64)
+    assert ref().ref_dump_arrays(a.ctypes.data_as(u32p), len(a), b.ctypes.data_as(u64p), len(b), path.encode()) == 0
 
 
 def ref_load_tns(path, start_index=1):

@@ -397,3 +397,36 @@ int ref_solve_normals(uint32_t nmodes, uint32_t mode, uint32_t R, float *const *
     mats_free(&B, 1);
     return r;
 }
+
+/* The reference's text writers into `path`: sptDumpSparseTensor,
+ * sptDumpMatrix, sptDumpIndexArray, sptDumpNnzIndexArray. */
+int ref_dump_tensor(uint32_t nmodes, const uint32_t *ndims, uint64_t nnz, uint32_t *const *inds, const float *vals,
+                    uint32_t start_index, const char *path) {
+    sptSparseTensor X;
+    build_tensor(&X, nmodes, ndims, nnz, inds, vals);
+    FILE *fp = fopen(path, "w");
+    if (!fp) return -2;
+    const int r = sptDumpSparseTensor(&X, start_index, fp);
+    fclose(fp);
+    sptFreeSparseTensor(&X);
+    return r;
+}
+
+int ref_dump_matrix(uint32_t nrows, uint32_t ncols, const float *vals, uint32_t stride, const char *path) {
+    sptMatrix *M = mat_from(nrows, ncols, vals, stride);
+    FILE *fp = fopen(path, "w");
+    if (!fp) return -2;
+    const int r = sptDumpMatrix(M, fp);
+    fclose(fp);
+    mats_free(&M, 1);
+    return r;
+}
+
+int ref_dump_arrays(const uint32_t *a, uint64_t na, const uint64_t *b, uint64_t nb, const char *path) {
+    FILE *fp = fopen(path, "w");
+    if (!fp) return -2;
+    int r = sptDumpIndexArray((sptIndex *)a, na, fp);
+    if (!r) r = sptDumpNnzIndexArray((sptNnzIndex *)b, nb, fp);
+    fclose(fp);
+    return r;
+}

@@ -93,3 +93,38 @@ def test_dump_kruskal(tmp_path, rank_form):
     text = _write(tmp_path, lambda fp: fn(C.byref(k), fp))
     # one lambda entry per mode, as the reference prints
     assert text == _ktensor_text(3, rank, ndims, 0.8125, lam, facs)
+
+
+def _ref_or_skip():
+    import oracle as O
+    if not O.ref_available():
+        pytest.skip("reference sources not present")
+    return O
+
+
+@pytest.mark.parametrize("start", [0, 1])
+def test_dump_tensor_and_matrix_equal_the_reference_bytes(tmp_path, start):
+    """The writers against the reference's own sptDumpSparseTensor /
+    sptDumpMatrix / sptDump*Array on the same objects, byte for byte."""
+    O = _ref_or_skip()
+    rng = np.random.default_rng(11 + start)
+    ndims = [9, 7, 5]
+    inds = np.stack([rng.integers(0, d, 40) for d in ndims]).astype(np.uint32)
+    vals = (rng.standard_normal(40) * 10.0 ** rng.integers(-4, 5, 40)).astype(np.float32)
+    t = S.Tensor.from_arrays(ndims, inds, vals)
+    mine = _write(tmp_path, lambda fp: S.lib().sptDumpSparseTensor(t.ptr(), start, fp))
+    ref_path = str(tmp_path / "ref_t.txt")
+    O.ref_dump_tensor(ndims, inds, vals, start, ref_path)
+    assert mine == open(ref_path).read()
+    a = (rng.standard_normal((6, 11)) * 10.0 ** rng.integers(-3, 4, (6, 11))).astype(np.float32)
+    m = S.Matrix.from_array(a)
+    mine = _write(tmp_path, lambda fp: S.lib().sptDumpMatrix(C.byref(m.s), fp))
+    O.ref_dump_matrix(a, ref_path)
+    assert mine == open(ref_path).read()
+    ia = rng.integers(0, 2**32, 13, dtype=np.uint64).astype(np.uint32)
+    nb = rng.integers(0, 2**63, 5, dtype=np.uint64)
+    L = S.lib()
+    mine = _write(tmp_path, lambda fp: L.sptDumpIndexArray(ia.ctypes.data_as(S.u32p), len(ia), fp) or
+                  L.sptDumpNnzIndexArray(nb.ctypes.data_as(S.u64p), len(nb), fp))
+    O.ref_dump_arrays(ia, nb, ref_path)
+    assert mine == open(ref_path).read()
