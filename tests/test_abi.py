@@ -103,3 +103,42 @@ def test_mutex_pool_alloc_and_free():
         assert pool.initialized and pool.locks
         assert (pool.nlocks, pool.padsize) in ((1024, 16), (7, 3))
         L.sptMutexFree(p)
+
+
+def test_container_growth_rules_equal_the_reference():
+    """Capacities after New / Append / Resize and the matrix stride and cap
+    rules, side by side with the reference library built from its sources:
+    objects built by either library can be grown or freed by the other."""
+    import oracle as O
+    if not O.ref_available():
+        pytest.skip("reference sources not present")
+    R, L = O.ref(), S.lib()
+    for lib in (R, L):
+        lib.sptNewIndexVector.argtypes = [C.POINTER(S.IndexVector), C.c_uint64, C.c_uint64]
+        lib.sptAppendIndexVector.argtypes = [C.POINTER(S.IndexVector), C.c_uint32]
+        lib.sptResizeIndexVector.argtypes = [C.POINTER(S.IndexVector), C.c_uint64]
+        lib.sptFreeIndexVector.argtypes = [C.POINTER(S.IndexVector)]
+        lib.sptNewMatrix.argtypes = [C.POINTER(S.MatrixS), C.c_uint32, C.c_uint32]
+        lib.sptFreeMatrix.argtypes = [C.POINTER(S.MatrixS)]
+
+    def trace(lib):
+        out = []
+        for ln, cap in ((0, 0), (3, 1), (5, 9)):
+            v = S.IndexVector()
+            assert lib.sptNewIndexVector(C.byref(v), ln, cap) == 0
+            out.append((v.len, v.cap))
+            for k in range(37):
+                assert lib.sptAppendIndexVector(C.byref(v), k) == 0
+                out.append((v.len, v.cap))
+            for size in (1, 0, 100, 7):
+                assert lib.sptResizeIndexVector(C.byref(v), size) == 0
+                out.append((v.len, v.cap))
+            lib.sptFreeIndexVector(C.byref(v))
+        for nr, nc in ((0, 1), (5, 7), (3, 8), (2, 9), (10, 33)):
+            m = S.MatrixS()
+            assert lib.sptNewMatrix(C.byref(m), nr, nc) == 0
+            out.append((m.nrows, m.ncols, m.cap, m.stride))
+            lib.sptFreeMatrix(C.byref(m))
+        return out
+
+    assert trace(L) == trace(R)
