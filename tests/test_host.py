@@ -139,3 +139,27 @@ def test_generator_independent_of_thread_count():
         outs.append(subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True,
                                    check=True).stdout.strip())
     assert outs[0] == outs[1]
+
+
+def test_mode_orders_equal_the_reference():
+    """sptGetBestModeOrder / sptGetWorstModeOrder (sort.c:193-233) against the
+    reference library built from its sources, over random shapes with ties."""
+    import oracle as O
+    if not O.ref_available():
+        pytest.skip("reference sources not present")
+    R = O.ref()
+    rng = np.random.default_rng(4)
+    for lib in (R, S.lib()):
+        for f in (lib.sptGetBestModeOrder, lib.sptGetWorstModeOrder):
+            f.argtypes = [C.POINTER(C.c_uint32), C.c_uint32, C.POINTER(C.c_uint32), C.c_uint32]
+    for _ in range(200):
+        N = int(rng.integers(2, 9))
+        nd = rng.integers(1, 6, N).astype(np.uint32)            # small sizes: many ties
+        mode = int(rng.integers(0, N))
+        outs = []
+        for lib in (R, S.lib()):
+            for f in (lib.sptGetBestModeOrder, lib.sptGetWorstModeOrder):
+                o = np.zeros(N, np.uint32)
+                f(o.ctypes.data_as(C.POINTER(C.c_uint32)), mode, nd.ctypes.data_as(C.POINTER(C.c_uint32)), N)
+                outs.append(list(o))
+        assert outs[:2] == outs[2:], (list(nd), mode, outs)
