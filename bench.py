@@ -536,7 +536,7 @@ def cpu_leg(sample_nnz, reps, prefer_reference):
     t = S.Tensor.generate(spec_for(sample_nnz, seed=SEED + 1))
     mats = S.new_factors(DIMS, RANK, seed=2)
     kind = "port"
-    if prefer_reference and os.path.exists(O.REF_PATH):
+    if prefer_reference and O.ref_loadable():
         secs = cpu_reference_mttkrp(t, mats, threads, reps)
         kind = "reference"
     else:
@@ -558,7 +558,7 @@ def run_reference(args, world, rank):
     threads = os.cpu_count() or 1
     t = S.Tensor.generate(spec_for(args.cpu_sample, seed=SEED + 1))
     mats = S.new_factors(DIMS, RANK, seed=2)
-    kind = "reference" if os.path.exists(O.REF_PATH) else "port"
+    kind = "reference" if O.ref_loadable() else "port"
     f = cpu_reference_mttkrp if kind == "reference" else cpu_port_mttkrp
     for _ in range(max(0, min(warm, 1))):
         f(t, mats, threads, 0)

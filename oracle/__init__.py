@@ -90,6 +90,18 @@ def ref_available():
     return os.path.exists(REF_PATH) or os.path.isdir(os.path.join(REF_SRC, "src"))
 
 
+def ref_loadable():
+    """True when the reference library is already built and loads in this
+    process (a build for another machine's architecture does not)."""
+    if not os.path.exists(REF_PATH):
+        return False
+    try:
+        ref()
+        return True
+    except OSError:
+        return False
+
+
 def ref():
     """The reference library with its LAPACK calls forwarded to scipy's."""
     global _REF
