@@ -142,3 +142,40 @@ def test_container_growth_rules_equal_the_reference():
         return out
 
     assert trace(L) == trace(R)
+
+
+def test_hicoo_container_shape_equals_the_reference():
+    """sptNewSparseTensorHiCOO (hicoo.c:29-129) side by side with the
+    reference: the same scalar fields, vector lengths and capacities, and one
+    kernel-schedule vector per kernel row of every mode, so a HiCOO tensor
+    made by one library can be filled or freed by the other.  (nkiters is
+    left out: the reference allocates it without initialising it, this
+    library zero-fills it.)"""
+    import oracle as O
+    if not O.ref_available():
+        pytest.skip("reference sources not present")
+    R, L = O.ref(), S.lib()
+    H = C.POINTER(S.HiCOOS)
+    u32p = C.POINTER(C.c_uint32)
+    for lib in (R, L):
+        lib.sptNewSparseTensorHiCOO.argtypes = [H, C.c_uint32, u32p, C.c_uint64, C.c_uint8, C.c_uint8, C.c_uint8]
+        lib.sptFreeSparseTensorHiCOO.argtypes = [H]
+
+    def shape(lib, ndims, nnz, sb, sk, sc):
+        h = S.HiCOOS()
+        nd = (C.c_uint32 * len(ndims))(*ndims)
+        assert lib.sptNewSparseTensorHiCOO(C.byref(h), len(ndims), nd, nnz, sb, sk, sc) == 0
+        N = h.nmodes
+        vec = lambda v: (int(v.len), int(v.cap))
+        out = {"scalars": (N, int(h.nnz), h.sb_bits, h.sk_bits, h.sc_bits),
+               "ndims": [h.ndims[m] for m in range(N)], "sortorder": [h.sortorder[m] for m in range(N)],
+               "kptr": vec(h.kptr), "cptr": vec(h.cptr), "bptr": vec(h.bptr), "values": vec(h.values),
+               "binds": [vec(h.binds[m]) for m in range(N)], "einds": [vec(h.einds[m]) for m in range(N)],
+               "kschr": [[vec(h.kschr[m][i]) for i in range((ndims[m] + (1 << sk) - 1) >> sk)] for m in range(N)]}
+        lib.sptFreeSparseTensorHiCOO(C.byref(h))
+        return out
+
+    for args in (([300, 200, 100], 1000, 3, 6, 10), ([40, 30, 20, 10], 55, 2, 4, 7), ([5, 5, 5], 0, 1, 2, 2)):
+        mine, ref = shape(L, *args), shape(R, *args)
+        for k in ref:
+            assert mine[k] == ref[k], (args, k, mine[k], ref[k])
