@@ -179,3 +179,57 @@ def test_hicoo_container_shape_equals_the_reference():
         mine, ref = shape(L, *args), shape(R, *args)
         for k in ref:
             assert mine[k] == ref[k], (args, k, mine[k], ref[k])
+
+
+def test_other_containers_equal_the_reference():
+    """sptNewSparseTensor, sptNewRankMatrix, sptNewKruskalTensor and
+    sptNewRankKruskalTensor side by side with the reference: fields, vector
+    sizes, strides and which pointers start empty.  The Kruskal tensors are
+    released with this library's free functions: the reference's own
+    sptFreeKruskalTensor (ktensor.c:79-89) dereferences factors[i] even when
+    no factors were attached, which crashes on a fresh object."""
+    import oracle as O
+    if not O.ref_available():
+        pytest.skip("reference sources not present")
+    R, L = O.ref(), S.lib()
+    u32p = C.POINTER(C.c_uint32)
+    T, RM = C.POINTER(S.SparseTensorS), C.POINTER(S.RankMatrixS)
+    K, RK = C.POINTER(S.KruskalS), C.POINTER(S.RankKruskalS)
+    for lib in (R, L):
+        lib.sptNewSparseTensor.argtypes = [T, C.c_uint32, u32p]
+        lib.sptFreeSparseTensor.argtypes = [T]
+        lib.sptNewRankMatrix.argtypes = [RM, C.c_uint32, C.c_uint8]
+        lib.sptFreeRankMatrix.argtypes = [RM]
+        lib.sptNewKruskalTensor.argtypes = [K, C.c_uint32, u32p, C.c_uint32]
+        lib.sptFreeKruskalTensor.argtypes = [K]
+        lib.sptNewRankKruskalTensor.argtypes = [RK, C.c_uint32, u32p, C.c_uint8]
+        lib.sptFreeRankKruskalTensor.argtypes = [RK]
+
+    def shapes(lib):
+        out = []
+        for ndims in ([4, 5, 6], [7, 3, 2, 9]):
+            N = len(ndims)
+            nd = (C.c_uint32 * N)(*ndims)
+            t = S.SparseTensorS()
+            assert lib.sptNewSparseTensor(C.byref(t), N, nd) == 0
+            out.append(("tsr", t.nmodes, int(t.nnz), [t.sortorder[m] for m in range(N)],
+                        [t.ndims[m] for m in range(N)], [(int(t.inds[m].len), int(t.inds[m].cap)) for m in range(N)],
+                        (int(t.values.len), int(t.values.cap))))
+            lib.sptFreeSparseTensor(C.byref(t))
+            for rank in (3, 16):
+                k = S.KruskalS()
+                assert lib.sptNewKruskalTensor(C.byref(k), N, nd, rank) == 0
+                out.append(("ktsr", k.nmodes, k.rank, [k.ndims[m] for m in range(N)], k.fit, bool(k.factors)))
+                L.sptFreeKruskalTensor(C.byref(k))
+                rk = S.RankKruskalS()
+                assert lib.sptNewRankKruskalTensor(C.byref(rk), N, nd, rank) == 0
+                out.append(("rktsr", rk.nmodes, rk.rank, [rk.ndims[m] for m in range(N)], rk.fit, bool(rk.factors)))
+                L.sptFreeRankKruskalTensor(C.byref(rk))
+        for nr, nc in ((0, 1), (5, 7), (3, 8), (2, 9), (10, 33)):
+            m = S.RankMatrixS()
+            assert lib.sptNewRankMatrix(C.byref(m), nr, nc) == 0
+            out.append(("rmtx", m.nrows, m.ncols, m.cap, m.stride))
+            lib.sptFreeRankMatrix(C.byref(m))
+        return out
+
+    assert shapes(L) == shapes(R)
