@@ -235,3 +235,24 @@ def test_reference_reader_agrees_with_oracle(tmp_path, case):
     got = O.load_tns(path, start)
     assert got[0] == ref[0]
     assert np.array_equal(got[1], ref[1]) and np.array_equal(got[2].view(np.uint32), ref[2].view(np.uint32))
+
+
+@pytest.mark.skipif(not O.ref_available(), reason="reference sources not present")
+@pytest.mark.parametrize("tk", [1, 4])
+def test_reduce_port_agrees_with_the_reference(tk):
+    """The port of sptOmpMTTKRP_Reduce that serves as the CPU baseline where
+    the reference cannot be built, against the reference's own function at
+    the same thread count: bit for bit at one thread, within the FP32
+    reordering of the per-thread partial sums otherwise."""
+    rng = np.random.default_rng(17)
+    ndims = [300, 200, 100]
+    inds = np.unique(np.stack([rng.integers(0, d, 60000) for d in ndims]).astype(np.uint32), axis=1)
+    vals = rng.random(inds.shape[1], dtype=np.float32)
+    mats = [rng.random((d, 16), dtype=np.float32) for d in ndims]
+    for mode in range(3):
+        r, _ = O.ref_mttkrp(ndims, inds, vals, mats, 16, mode, which=1, tk=tk)
+        p = O.mttkrp(ndims, inds, vals, mats, 16, mode, precision="omp", tk=tk)
+        if tk == 1:
+            assert np.array_equal(r, p), mode
+        else:
+            assert rel_fro(p, r) <= 1e-6, mode
