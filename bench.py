@@ -73,8 +73,13 @@ def parse():
     p.add_argument("--skip-cpu", action="store_true")
     p.add_argument("--serve-requests", type=int, default=4096)
     p.add_argument("--plain-sample", type=int, default=256)
+    p.add_argument("--serve-cpu-sample", type=int, default=32)
     p.add_argument("--skip-serve", action="store_true")
     p.add_argument("--skip-hicoo", action="store_true")
+    p.add_argument("--skip-hostalloc", action="store_true")
+    p.add_argument("--skip-c1", action="store_true")
+    p.add_argument("--skip-cpals", action="store_true")
+    p.add_argument("--cpals-nnz", type=int, default=50_000_000)
     return p.parse_args()
 
 
@@ -341,6 +346,29 @@ def hicoo_cpu_leg(sample_nnz, reps):
             "seconds_per_step": step}
 
 
+def serve_cpu_leg(reqs, tensors, count):
+    """The reference's sptOmpCpdAls loop (OmpCpdAlsStep, use_reduce = 1,
+    every host thread) run on the stream's first `count` requests one after
+    another from the same initial factors as the GPU runs: seconds per
+    request (a CPU figure for context; the reference has no GPU CP-ALS)."""
+    import oracle as O
+    if count <= 0 or not O.ref_loadable():
+        return None
+    threads = os.cpu_count() or 1
+    secs, fits = [], []
+    for i in range(min(count, len(reqs))):
+        r = reqs[i]
+        init = [m.array()[: d, : r["rank"]].copy() for m, d in zip(request_init(r), r["dims"])]
+        inds, vals = tensors[i].arrays()
+        sec, fit, _ = O.ref_omp_cpd(r["dims"], inds, vals, r["rank"], SERVE_ITERS, init, threads)
+        secs.append(sec)
+        fits.append(fit)
+    return {"kind": "reference", "cores": threads, "requests": len(secs),
+            "solves_per_s": round(len(secs) / sum(secs), 2), "mean_s_per_request": round(float(np.mean(secs)), 4),
+            "sample": "first %d requests of the stream, %d iterations each, OmpCpdAlsStep (use_reduce = 1, tol 0), "
+                      "one request at a time with %d threads" % (len(secs), SERVE_ITERS, threads)}
+
+
 def serve_leg(args):
     import sptol_gb300 as S
     reqs = serve_stream(args.serve_requests)
@@ -360,6 +388,11 @@ def serve_leg(args):
                poisson=False, keep_fits=0)
     batched = run_served(reqs, tensors, inits, outs, poisson=False, keep_fits=sample)
     served = run_served(reqs, tensors, inits, outs, poisson=True, keep_fits=sample)
+    # the same arrivals as the plain run: the stream's first `sample`
+    # requests, so that served and plain latencies cover one population
+    prefix = run_served(reqs[:sample], tensors[:sample], inits[:sample], outs[:sample], poisson=True,
+                        keep_fits=sample)
+    cpu = serve_cpu_leg(reqs, tensors, args.serve_cpu_sample)
     plain = run_plain(reqs, tensors, inits, sample)   # last: overwrites inits[:sample]
     # fit agreement: requests on which the ALS iteration stays well defined in
     # both paths.  A run diverges when a fit is not finite, negative, or drops
@@ -396,8 +429,16 @@ def serve_leg(args):
                     "steps": batched["steps"], "gpu_launches": batched["launches"], "host_s": batched["host_s"]},
         "plain": {"solves_per_s": round(plain["solves_per_s"], 1), "p50_ms": pct(plain["lat"], 50),
                   "p99_ms": pct(plain["lat"], 99), "makespan_s": round(plain["makespan_s"], 3),
-                  "sample": "first %d requests of the same stream, back to back" % sample},
+                  "sample": "first %d requests of the same stream at their arrival times, one at a time "
+                            "(latency = completion - arrival)" % sample},
+        "served_same_requests_as_plain": {
+            "solves_per_s": round(prefix["solves_per_s"], 1), "p50_ms": pct(prefix["lat"], 50),
+            "p99_ms": pct(prefix["lat"], 99), "makespan_s": round(prefix["makespan_s"], 3),
+            "steps": prefix["steps"], "gpu_launches": prefix["launches"],
+            "sample": "first %d requests of the same stream at their arrival times through sptgbServer" % sample},
+        "cpu_baseline": cpu,
         "served_over_plain": round(served["solves_per_s"] / plain["solves_per_s"], 2),
+        "served_over_plain_same_requests": round(prefix["solves_per_s"] / plain["solves_per_s"], 2),
         "batched_over_plain": round(batched["solves_per_s"] / plain["solves_per_s"], 2),
         "fit_match": {"compared": sample, "well_posed": len(diffs), "max_diff_vs_plain": dfit, "tolerance": 1e-4,
                       "within_tolerance": int(sum(d <= 1e-4 for d in diffs)),
@@ -405,6 +446,208 @@ def serve_leg(args):
                                     "rank": reqs[i]["rank"]} for i in div]},
         "generate_s": round(gen_s, 1),
     }
+
+
+class HostAllocCopy:
+    """A second host copy of a tensor and its factor matrices in memory from
+    cudaHostAlloc (torch's pinned allocator), described by sptSparseTensor /
+    sptMatrix structures that point into it: the e2e leg's inputs allocated as
+    page-locked memory instead of registered (cudaHostRegister) caller memory."""
+
+    def __init__(self, t, mats):
+        import torch
+        import sptol_gb300 as S
+        self.keep = []
+        N, n = t.nmodes, t.nnz
+        self.nmodes, self.ndims = N, t.ndims
+        x = S.SparseTensorS()
+        x.nmodes = N
+        so = (ctypes.c_uint32 * N)(*t.sortorder)
+        nd = (ctypes.c_uint32 * N)(*t.ndims)
+        iv = (S.IndexVector * N)()
+        for m in range(N):
+            b = torch.empty(n, dtype=torch.int32, pin_memory=True)
+            b.numpy()[:] = t.inds(m).view(np.int32)
+            iv[m].len = iv[m].cap = n
+            iv[m].data = ctypes.cast(b.data_ptr(), S.u32p)
+            self.keep.append(b)
+        vb = torch.empty(n, dtype=torch.float32, pin_memory=True)
+        vb.numpy()[:] = t.vals()
+        self.keep += [vb, so, nd, iv]
+        x.sortorder = ctypes.cast(so, S.u32p)
+        x.ndims = ctypes.cast(nd, S.u32p)
+        x.nnz = n
+        x.inds = ctypes.cast(iv, ctypes.POINTER(S.IndexVector))
+        x.values.len = x.values.cap = n
+        x.values.data = ctypes.cast(vb.data_ptr(), S.f32p)
+        self.s = x
+        self.mats = []
+        for M in mats:
+            cap, st = int(M.s.cap), int(M.s.stride)
+            b = torch.empty(cap * st, dtype=torch.float32, pin_memory=True)
+            b.numpy()[:] = np.ctypeslib.as_array(M.s.values, shape=(cap * st,))
+            ms = S.MatrixS()
+            ms.nrows, ms.ncols, ms.cap, ms.stride = M.s.nrows, M.s.ncols, cap, st
+            ms.values = ctypes.cast(b.data_ptr(), S.f32p)
+            self.keep.append(b)
+            self.mats.append(ms)
+
+    def call(self, mode, order):
+        import sptol_gb300 as S
+        N = self.nmodes
+        self.mats[N].nrows = self.ndims[mode]
+        arr = (ctypes.POINTER(S.MatrixS) * (N + 1))(*[ctypes.pointer(m) for m in self.mats])
+        op = (ctypes.c_uint32 * N)(*order)
+        r = S.lib().sptCudaMTTKRP(ctypes.byref(self.s), arr, op, mode, 15)
+        if r:
+            raise RuntimeError("sptCudaMTTKRP failed (0x%x)" % r)
+
+
+C1_DIMS = [1024, 1024, 1024]
+C1_DRAWS = 1_000_000
+C1_RANK = 16
+
+
+def c1_leg(reps):
+    """The CPU-runnable reference configuration: 1024^3, 1,000,000 uniform
+    draws (seed 0) with duplicates merged by summation, values U[0,1), rank-16
+    factors U[0,1); mode 0 first, then every mode.  GPU: the resident kernel
+    (CUDA events) and the drop-in sptMTTKRP with host buffers (wall time);
+    beside them the reference's sequential sptMTTKRP (mttkrp.c:39-115) and
+    sptOmpMTTKRP_Reduce with every host thread (the oracle port of the latter
+    where the reference was not built).  Medians of `reps` calls after one
+    warm-up call each."""
+    import torch
+    import oracle as O
+    import sptol_gb300 as S
+    spec = S.GenSpec()
+    spec.seed = 0
+    spec.nmodes = 3
+    for m, d in enumerate(C1_DIMS):
+        spec.ndims[m] = d
+        spec.coord_dist[m] = S.DIST_UNIFORM
+    spec.count = C1_DRAWS
+    spec.merge_duplicates = 1
+    spec.value_dist = S.VAL_U01
+    t = S.Tensor.generate(spec)
+    ndims, nnz = t.ndims, t.nnz
+    stride = ((C1_RANK - 1) // 8 + 1) * 8
+    mats = S.new_factors(ndims, C1_RANK, seed=1)
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+    dfac = [torch.from_numpy(mats[m].array()[: ndims[m]].copy()).cuda() for m in range(3)]
+    dout = torch.zeros((max(ndims), stride), dtype=torch.float32, device="cuda")
+    coo = S.DeviceCoo(t, stream=sh)
+    orders = [[m] + [(m + i) % 3 for i in (1, 2)] for m in range(3)]
+    kern, call = [], []
+    for m in range(3):
+        coo.prepare(m, stream=sh)
+        ptrs = [f.data_ptr() for f in dfac]
+        ks = []
+        for r in range(reps + 1):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            coo.mttkrp(m, orders[m], ptrs, C1_RANK, stride, dout.data_ptr(), stream=sh)
+            b.record(stream)
+            b.synchronize()
+            if r:
+                ks.append(a.elapsed_time(b))
+        kern.append(float(np.median(ks)))
+        cs = []
+        for r in range(reps + 1):
+            a = time.perf_counter()
+            S.mttkrp(t, mats, m, mats_order=orders[m], entry="sptMTTKRP", copy=False)
+            if r:
+                cs.append((time.perf_counter() - a) * 1e3)
+        call.append(float(np.median(cs)))
+    coo.free()
+    threads = os.cpu_count() or 1
+    inds, vals = t.arrays()
+    facs = [mats[m].array()[: ndims[m]] for m in range(3)]
+    seq, red = [], []
+    kind = "reference" if O.ref_loadable() else "port"
+    for m in range(3):
+        if kind == "reference":
+            seq.append(O.ref_mttkrp(ndims, inds, vals, facs, C1_RANK, m, which=0, tk=1, reps=reps)[1] * 1e3)
+            red.append(O.ref_mttkrp(ndims, inds, vals, facs, C1_RANK, m, which=1, tk=threads, reps=reps)[1] * 1e3)
+        else:
+            for which, dst, tk in (("f32", seq, 1), ("omp", red, threads)):
+                ts = []
+                for r in range(reps + 1):
+                    a = time.perf_counter()
+                    O.mttkrp(ndims, inds, vals, facs, C1_RANK, m, precision=which, tk=tk)
+                    if r:
+                        ts.append((time.perf_counter() - a) * 1e3)
+                dst.append(float(np.median(ts)))
+    ab = algo_bytes(ndims, nnz, C1_RANK)
+
+    def gbs(ms):
+        return [round(ab / (x / 1e3) / 1e9, 2) for x in ms]
+
+    return {"workload": "mttkrp_uniform_coo_1024cubed_1Mdraws_merged_rank16", "nnz": nnz,
+            "algorithmic_bytes_per_mttkrp": ab,
+            "gpu_kernel_ms_by_mode": [round(x, 4) for x in kern], "gpu_kernel_gbs_by_mode": gbs(kern),
+            "sptMTTKRP_call_ms_by_mode": [round(x, 3) for x in call], "sptMTTKRP_call_gbs_by_mode": gbs(call),
+            "cpu": {"kind": kind, "cores": threads,
+                    "sequential_sptMTTKRP_ms_by_mode": [round(x, 3) for x in seq],
+                    "sequential_gbs_by_mode": gbs(seq),
+                    "omp_reduce_ms_by_mode": [round(x, 3) for x in red], "omp_reduce_gbs_by_mode": gbs(red),
+                    "omp_reduce_threads": threads},
+            "reps": reps}
+
+
+C4_DIMS = [500_000, 300_000, 10_000]
+
+
+def cpals_leg(nnz, iters=20):
+    """Full CP-ALS on the planted-model tensor 500,000 x 300,000 x 10,000
+    (coordinates Zipf(1.1) in every mode, 50M unique nonzeros, values a
+    planted rank-32 Kruskal model plus N(0, 0.01^2)), rank 32, 20 iterations
+    from seeded U[0,1) factors.  GPU: sptgbCpdAls (the device loop behind
+    sptCpdAls), wall time including upload and the per-mode device sorts.
+    cpu_baseline: the reference's sptOmpCpdAls loop, OmpCpdAlsStep with
+    use_reduce = 1 (cpd_omp.c:32-157), every host thread, from the same
+    factors; both fits are the corrected fit of the final model."""
+    import oracle as O
+    import sptol_gb300 as S
+    spec = S.GenSpec()
+    spec.seed = 404
+    spec.nmodes = 3
+    for m, d in enumerate(C4_DIMS):
+        spec.ndims[m] = d
+        spec.coord_dist[m] = S.DIST_ZIPF
+        spec.zipf_s[m] = 1.1
+    spec.count = nnz
+    spec.merge_duplicates = 0
+    spec.value_dist = S.VAL_PLANTED
+    spec.planted_rank = 32
+    spec.planted_seed = 405
+    spec.noise_sigma = 0.01
+    g0 = time.time()
+    t = S.Tensor.generate(spec)
+    gen_s = time.time() - g0
+    ndims = t.ndims
+    rng = np.random.default_rng(406)
+    init = [rng.random((d, 32), dtype=np.float32) for d in ndims]
+    S.cpd_als(t, 32, 1, 0.0, init)          # context and kernel modules loaded before timing
+    t0 = time.perf_counter()
+    _, _, fits, it = S.cpd_als(t, 32, iters, 0.0, init)
+    gpu_s = time.perf_counter() - t0
+    out = {"workload": "cpals_planted_rank32_500Kx300Kx10K_zipf1.1_%dnnz_rank32_%dit" % (t.nnz, iters),
+           "nnz": t.nnz, "rank": 32, "iterations": iters, "generate_s": round(gen_s, 2),
+           "gpu": {"seconds": round(gpu_s, 4), "s_per_iteration": round(gpu_s / iters, 5),
+                   "fit_final": float(fits[it - 1]), "entry": "sptgbCpdAls (upload, sorts and copies back included)"}}
+    if O.ref_loadable():
+        threads = os.cpu_count() or 1
+        inds, vals = t.arrays()
+        secs, fit, _ = O.ref_omp_cpd(ndims, inds, vals, 32, iters, init, threads)
+        out["cpu_baseline"] = {"seconds": round(secs, 3), "s_per_iteration": round(secs / iters, 4),
+                               "fit_final": fit, "kind": "reference", "cores": threads,
+                               "sample": "the full tensor, %d iterations, OmpCpdAlsStep (sptOmpCpdAls loop, "
+                                         "use_reduce = 1, tol 0) from the same initial factors" % iters}
+        out["fit_abs_diff"] = abs(float(fits[it - 1]) - fit)
+        out["gpu_over_cpu"] = round(secs / gpu_s, 1)
+    return out
 
 
 def peaks():
@@ -502,7 +745,7 @@ def barrier(world):
 
 
 def cpu_port_mttkrp(t, mats, threads, reps):
-    """sptOmpMTTKRP_Reduce restated (oracle) on the sample: seconds per step."""
+    """sptOmpMTTKRP_Reduce restated (oracle) on the host tensor: seconds per step."""
     import oracle as O
     inds, vals = t.arrays()
     facs = [m.array()[: t.ndims[i]] for i, m in enumerate(mats[:3])]
@@ -516,63 +759,101 @@ def cpu_port_mttkrp(t, mats, threads, reps):
     return float(np.mean(best)) if best else 0.0
 
 
-def cpu_reference_mttkrp(t, mats, threads, reps):
-    """The reference's own sptOmpMTTKRP_Reduce (when built here)."""
+def cpu_leg(t, mats, reps):
+    """cpu_baseline of the GPU arm: the reference's own sptOmpMTTKRP_Reduce
+    (mttkrp_omp.c:401-563) with every host thread on the arm's own host copy of
+    the full workload tensor, one warm-up call then `reps` timed calls per
+    mode; beside it the atomic sptOmpMTTKRP (mttkrp_omp.c:125-252), one timed
+    call per mode.  Where the reference was not built, the oracle port of
+    sptOmpMTTKRP_Reduce instead (kind "port")."""
     import oracle as O
+    threads = os.cpu_count() or 1
     inds, vals = t.arrays()
     facs = [m.array()[: t.ndims[i]] for i, m in enumerate(mats[:3])]
-    tot = 0.0
-    for mode in range(3):
-        _, s = O.ref_mttkrp(t.ndims, inds, vals, facs, RANK, mode, which=1, tk=threads, reps=reps)
-        tot += s
-    return tot
-
-
-def cpu_leg(sample_nnz, reps, prefer_reference):
-    import oracle as O
-    import sptol_gb300 as S
-    O.build(with_ref=False)
-    threads = os.cpu_count() or 1
-    t = S.Tensor.generate(spec_for(sample_nnz, seed=SEED + 1))
-    mats = S.new_factors(DIMS, RANK, seed=2)
-    kind = "port"
-    if prefer_reference and O.ref_loadable():
-        secs = cpu_reference_mttkrp(t, mats, threads, reps)
+    atomic = None
+    if O.ref_loadable():
         kind = "reference"
+        secs = 0.0
+        for mode in range(3):
+            secs += O.ref_mttkrp(t.ndims, inds, vals, facs, RANK, mode, which=1, tk=threads, reps=reps)[1]
+        asecs = []
+        for mode in range(3):
+            asecs.append(O.ref_mttkrp(t.ndims, inds, vals, facs, RANK, mode, which=2, tk=threads, reps=1)[1])
+        bstep = 3 * algo_bytes(DIMS, t.nnz, RANK)
+        atomic = {"value": round(bstep / sum(asecs) / 1e9, 3), "unit": "GB/s", "seconds_by_mode": asecs,
+                  "function": "sptOmpMTTKRP (OpenMP atomics), %d threads, 1 call per mode after the Reduce "
+                              "calls" % threads}
     else:
+        kind = "port"
         secs = cpu_port_mttkrp(t, mats, threads, reps)
     gbs = 3 * algo_bytes(DIMS, t.nnz, RANK) / secs / 1e9
-    sample = ("%d-nnz tensor of the same shape and distributions, all 3 modes, %d reps after 1 warm-up, "
+    sample = ("the full %d-nnz workload tensor, all 3 modes, %d timed calls per mode after 1 warm-up, "
               "sptOmpMTTKRP_Reduce with %d threads" % (t.nnz, reps, threads))
     return {"value": round(gbs, 3), "unit": "GB/s", "cores": threads, "kind": kind, "sample": sample,
-            "seconds_per_step": secs, "nnz_per_s": 3 * t.nnz / secs}
+            "seconds_per_step": secs, "nnz_per_s": 3 * t.nnz / secs, "atomic": atomic}
 
 
 def run_reference(args, world, rank):
+    """--impl reference: the reference's own sptOmpMTTKRP_Reduce
+    (mttkrp_omp.c:401-563) with every host thread on the full workload tensor,
+    in a process that loads nothing of libParTI.so: the tensor and factors are
+    made by the library's generator compiled into oracle/_ref/libparti_ref.so,
+    which builds them in the reference's own containers (ref_session_*).  One
+    step = MTTKRP of modes 0, 1, 2 (protocol of examples/mttkrp.c:240-274);
+    `warmup` untimed steps, then `steps` timed steps.  Where the reference was
+    not built, the oracle port on the tensor from libParTI.so's generator."""
     if rank != 0:
         return
-    steps, warm = max(1, args.steps if args.steps <= 20 else 5), args.warmup
     import oracle as O
-    import sptol_gb300 as S
-    O.build(with_ref=False)
     threads = os.cpu_count() or 1
-    t = S.Tensor.generate(spec_for(args.cpu_sample, seed=SEED + 1))
-    mats = S.new_factors(DIMS, RANK, seed=2)
-    kind = "reference" if O.ref_loadable() else "port"
-    f = cpu_reference_mttkrp if kind == "reference" else cpu_port_mttkrp
-    for _ in range(max(0, min(warm, 1))):
-        f(t, mats, threads, 0)
-    secs = f(t, mats, threads, steps)
-    gbs = 3 * algo_bytes(DIMS, t.nnz, RANK) / secs / 1e9
+    K, W = max(1, args.steps), max(0, args.warmup)
+    if not O.ref_loadable():
+        try:
+            O.build()
+        except Exception:
+            pass
+    g0 = time.time()
+    if O.ref_loadable():
+        kind = "reference"
+        sess = O.RefSession(spec_for(args.nnz), RANK, 1, threads)
+        nnz = sess.nnz
+
+        def step():
+            for m in range(3):
+                sess.mttkrp(m, "reduce")
+    else:
+        import sptol_gb300 as S
+        kind = "port"
+        t = S.Tensor.generate(spec_for(args.nnz))
+        mats = S.new_factors(DIMS, RANK, seed=1)
+        inds, vals = t.arrays()
+        facs = [m.array()[: t.ndims[i]] for i, m in enumerate(mats[:3])]
+        nnz = t.nnz
+
+        def step():
+            for m in range(3):
+                O.mttkrp(DIMS, inds, vals, facs, RANK, m, precision="omp", tk=threads)
+    gen_s = time.time() - g0
+    for _ in range(W):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(K):
+        step()
+    secs = (time.perf_counter() - t0) / K
+    gbs = 3 * algo_bytes(DIMS, nnz, RANK) / secs / 1e9
+    sample = ("the full %d-nnz workload tensor, 3 modes per step, sptOmpMTTKRP_Reduce with %d threads, "
+              "%d timed steps after %d warm-up steps" % (nnz, threads, K, W))
     line = {
-        "metric": METRIC, "value": round(gbs, 3), "unit": "GB/s", "n_gpus": args.gpus, "steps": steps,
-        "warmup": warm, "ms_per_step": secs * 1e3, "higher_is_better": True, "scaling": "weak",
+        "metric": METRIC, "value": round(gbs, 3), "unit": "GB/s", "n_gpus": args.gpus, "steps": K,
+        "warmup": W, "ms_per_step": secs * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
-        "config": workload_config(args.nnz, args.gpus),
-        "cpu_baseline": {"value": round(gbs, 3), "unit": "GB/s", "cores": threads, "kind": kind,
-                         "sample": "%d-nnz tensor of the workload's shape and distributions, 3 modes per step, "
-                                   "sptOmpMTTKRP_Reduce, %d threads" % (t.nnz, threads)},
+        "config": workload_config(nnz, args.gpus),
+        "cpu_baseline": {"value": round(gbs, 3), "unit": "GB/s", "cores": threads, "kind": kind, "sample": sample},
         "e2e": {"value": round(gbs, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "nnz_per_s": round(3 * nnz / secs, 1),
+        "setup_s": {"generate": round(gen_s, 2)},
+        "tensor_source": ("library generator linked into the reference build (reference containers)"
+                          if kind == "reference" else "libParTI.so generator (reference not built)"),
     }
     print(json.dumps(line), flush=True)
 
@@ -714,6 +995,27 @@ def run_ours(args, world, rank, local):
     S.lib().sptClearLastError()
     e2e = world * bytes_step / e_s / 1e9
 
+    # the same e2e steps with the caller's arrays in cudaHostAlloc memory
+    # instead of registered memory: do the occasional slow steps remain?
+    hostalloc = None
+    if world == 1 and not args.skip_hostalloc:
+        hc = HostAllocCopy(t, mats)
+        for _ in range(2):
+            for m in range(3):
+                hc.call(m, orders[m])
+        h_each = []
+        for _ in range(ke):
+            s0 = time.perf_counter()
+            for m in range(3):
+                hc.call(m, orders[m])
+            h_each.append(time.perf_counter() - s0)
+        del hc
+        hostalloc = {"value": round(bytes_step / float(np.mean(h_each)) / 1e9, 2), "unit": "GB/s",
+                     "ms_per_step": round(float(np.mean(h_each)) * 1e3, 2),
+                     "ms_median_step": round(float(np.median(h_each)) * 1e3, 2),
+                     "ms_each_step": [round(x * 1e3, 2) for x in h_each],
+                     "host_memory": "cudaHostAlloc (torch pinned allocator)"}
+
     hicoo = None
     if world == 1 and not args.skip_hicoo:
         coo.free()
@@ -726,9 +1028,18 @@ def run_ours(args, world, rank, local):
         coo.free()
         serve = serve_leg(args)
 
+    c1 = None
+    if world == 1 and not args.skip_c1:
+        c1 = c1_leg(5)
+
     cpu = None
     if rank == 0 and world == 1 and not args.skip_cpu:
-        cpu = cpu_leg(args.cpu_sample, 3, prefer_reference=False)
+        cpu = cpu_leg(t, mats, 2)
+
+    cpals = None
+    if world == 1 and not args.skip_cpals:
+        del t
+        cpals = cpals_leg(args.cpals_nnz)
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": world, "steps": K,
@@ -745,7 +1056,8 @@ def run_ours(args, world, rank, local):
                     "ms_median_step": round(float(np.median(e_each)) * 1e3, 2),
                     "host_memory": "pinned" if pinned and len(pinned_mats) == len(mats) else "pageable",
                     "host_link_h2d_gbs": link_gbs,
-                    "link_floor_ms": round((h2d + d2h) / (link_gbs * 1e9) * 1e3, 2) if link_gbs else None},
+                    "link_floor_ms": round((h2d + d2h) / (link_gbs * 1e9) * 1e3, 2) if link_gbs else None,
+                    "host_alloc_variant": hostalloc},
             "gpu_launches": int(n1 - n0),
             "clocks": clocks.summary(),
             "nnz_per_s": round(world * K * 3 * nnz / (ms_max / 1e3), 1),
@@ -754,6 +1066,8 @@ def run_ours(args, world, rank, local):
             "bf16_storage": bf16,
             "hicoo": hicoo,
             "serve": serve,
+            "c1": c1,
+            "cpals": cpals,
         }
         print(json.dumps(line), flush=True)
     coo.free()

@@ -18,7 +18,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORC_PATH = os.path.join(HERE, "_build", "liborc.so")
 REF_PATH = os.path.join(HERE, "_ref", "libparti_ref.so")
-REF_SRC = "/root/reference"
+# The staged copy of the reference sources that the `ref` target compiles
+# (made by `make stage` from the tree named by SPTGB_REFERENCE; git-ignored).
+REF_TREE = os.path.join(HERE, "_ref", "tree")
 
 u32p = C.POINTER(C.c_uint32)
 u64p = C.POINTER(C.c_uint64)
@@ -31,12 +33,28 @@ _REF = None
 
 
 def build(with_ref=None):
-    """Builds liborc.so, and the reference library when its sources exist."""
+    """Builds liborc.so, and the reference library when its sources are
+    staged.  With SPTGB_REFERENCE set to a reference checkout, the sources are
+    (re)staged from it first."""
     subprocess.run(["make", "-s", "-C", HERE, "orc"], check=True)
+    if os.environ.get("SPTGB_REFERENCE"):
+        stage_reference()
     if with_ref is None:
-        with_ref = os.path.isdir(os.path.join(REF_SRC, "src"))
+        with_ref = os.path.isdir(os.path.join(REF_TREE, "src"))
     if with_ref:
-        subprocess.run(["make", "-s", "-j8", "-C", HERE, "ref", "REF=" + REF_SRC], check=True)
+        if not os.path.isdir(os.path.join(REF_TREE, "src")):
+            raise RuntimeError("no staged reference sources under %s: set SPTGB_REFERENCE to a reference "
+                               "checkout and call oracle.stage_reference()" % REF_TREE)
+        subprocess.run(["make", "-s", "-j%d" % min(16, os.cpu_count() or 4), "-C", HERE, "ref"], check=True)
+
+
+def stage_reference():
+    """Copies the reference sources the `ref` target needs from the checkout
+    named by SPTGB_REFERENCE into oracle/_ref/tree (git-ignored)."""
+    src = os.environ.get("SPTGB_REFERENCE")
+    if not src:
+        raise RuntimeError("SPTGB_REFERENCE is not set: it must name a reference (ParTI!) source checkout")
+    subprocess.run(["make", "-s", "-C", HERE, "stage", "REF=" + src], check=True)
 
 
 def stride_of(rank):
@@ -87,7 +105,7 @@ def orc():
 
 
 def ref_available():
-    return os.path.exists(REF_PATH) or os.path.isdir(os.path.join(REF_SRC, "src"))
+    return os.path.exists(REF_PATH) or os.path.isdir(os.path.join(REF_TREE, "src"))
 
 
 def ref_loadable():
@@ -147,6 +165,19 @@ def ref():
         L.ref_dump_tensor.argtypes = [C.c_uint32, u32p, C.c_uint64, C.POINTER(u32p), f32p, C.c_uint32, C.c_char_p]
         L.ref_dump_matrix.argtypes = [C.c_uint32, C.c_uint32, f32p, C.c_uint32, C.c_char_p]
         L.ref_dump_arrays.argtypes = [u32p, C.c_uint64, u64p, C.c_uint64, C.c_char_p]
+        L.ref_session_open.restype = C.c_void_p
+        L.ref_session_open.argtypes = [C.c_void_p, C.c_uint32, C.c_uint64, C.c_int]
+        L.ref_session_close.argtypes = [C.c_void_p]
+        L.ref_session_nnz.restype = C.c_uint64
+        L.ref_session_nnz.argtypes = [C.c_void_p]
+        L.ref_session_ndims.argtypes = [C.c_void_p, u32p]
+        L.ref_session_mttkrp.restype = C.c_double
+        L.ref_session_mttkrp.argtypes = [C.c_void_p, C.c_int, C.c_uint32, f32p]
+        L.ref_session_cpd.restype = C.c_double
+        L.ref_session_cpd.argtypes = [C.c_void_p, C.c_uint32, C.c_int, f32p, f64p]
+        L.ref_omp_cpd.restype = C.c_double
+        L.ref_omp_cpd.argtypes = [C.c_uint32, u32p, C.c_uint64, C.POINTER(u32p), f32p, C.c_uint32, C.c_uint32,
+                                  C.POINTER(f32p), C.c_uint32, C.c_int, f32p, f64p]
         L.ref_kruskal_inner.restype = C.c_double
         L.ref_kruskal_inner.argtypes = [C.c_uint32, C.c_uint32, u32p, C.POINTER(f32p), f32p, C.c_uint32, f32p]
         _REF = L
@@ -400,8 +431,9 @@ def ref_mttkrp(ndims, inds, vals, mats, rank, mode, order=None, which=0, tk=1, r
     o, op = _u32(order)
     out = np.zeros((ndims[mode], stride), np.float32)
     secs = C.c_double()
-    r = ref().ref_mttkrp(N, ndp, n, ip, v.ctypes.data_as(f32p), rank, mp, stride, op, mode,
-                         out.ctypes.data_as(f32p), which, tk, reps, C.byref(secs))
+    with quiet_stdout():   # the sequential sptMTTKRP prints its time
+        r = ref().ref_mttkrp(N, ndp, n, ip, v.ctypes.data_as(f32p), rank, mp, stride, op, mode,
+                             out.ctypes.data_as(f32p), which, tk, reps, C.byref(secs))
     assert r == 0
     return out[:, :rank], secs.value
 
@@ -620,3 +652,87 @@ def ref_ttm(ndims, inds, vals, U, mode):
     nf = ref().ref_ttm(N, ndp, n, sp, sv.ctypes.data_as(f32p), mode, U.ctypes.data_as(f32p), U.shape[0], ncols, fp,
                        Y.ctypes.data_as(f32p), C.byref(ys))
     return np.stack([f[:nf] for f in fib]), Y[:nf, :ncols], np.stack(si), sv
+
+
+# ------------------------------------------------- reference timing sessions --
+class quiet_stdout:
+    """Sends the C library's stdout (the reference prints per-iteration
+    progress lines) to stderr for the duration of a call, so that a caller's
+    own stdout stays machine-readable."""
+
+    def __enter__(self):
+        import sys
+        sys.stdout.flush()
+        self._saved = os.dup(1)
+        os.dup2(2, 1)
+        return self
+
+    def __exit__(self, *exc):
+        import sys
+        sys.stdout.flush()
+        os.dup2(self._saved, 1)
+        os.close(self._saved)
+        return False
+
+
+class RefSession:
+    """The reference's own CPU MTTKRP / CP-ALS on a tensor held in the
+    reference's containers (ref_harness.c, ref_session_*): the tensor is made
+    by the library's seeded generator compiled into libparti_ref.so (spec: a
+    ctypes structure with the layout of sptgbGenSpec), the factors U[0,1) from
+    seed `fac_seed`, stream m for mode m, as sptgbFillMatrix makes them for the
+    GPU.  Nothing of libParTI.so is loaded."""
+
+    WHICH = {"seq": 0, "reduce": 1, "atomic": 2}
+
+    def __init__(self, spec, rank, fac_seed, threads):
+        L = ref()
+        self.rank = rank
+        self.threads = threads
+        self.h = L.ref_session_open(C.byref(spec), rank, fac_seed, threads)
+        if not self.h:
+            raise RuntimeError("ref_session_open failed")
+        self.nnz = int(L.ref_session_nnz(self.h))
+        nd = np.zeros(8, np.uint32)
+        L.ref_session_ndims(self.h, nd.ctypes.data_as(u32p))
+        self.ndims = [int(x) for x in nd[: spec.nmodes]]
+
+    def mttkrp(self, mode, which="reduce", out=None):
+        """Seconds of one call; out (ndims[mode] x stride float32) receives M."""
+        p = out.ctypes.data_as(f32p) if out is not None else None
+        with quiet_stdout():
+            t = ref().ref_session_mttkrp(self.h, self.WHICH[which], mode, p)
+        if t < 0:
+            raise RuntimeError("reference MTTKRP failed")
+        return t
+
+    def cpd(self, niters, use_reduce=1):
+        """OmpCpdAlsStep from the session's factors: (seconds, corrected fit, lambda)."""
+        lam = np.zeros(self.rank, np.float32)
+        fit = C.c_double()
+        with quiet_stdout():
+            t = ref().ref_session_cpd(self.h, niters, use_reduce, lam.ctypes.data_as(f32p), C.byref(fit))
+        return t, fit.value, lam
+
+    def close(self):
+        if self.h:
+            ref().ref_session_close(self.h)
+            self.h = None
+
+
+def ref_omp_cpd(ndims, inds, vals, rank, niters, init, tk):
+    """The reference's OmpCpdAlsStep (sptOmpCpdAls with use_reduce = 1) from
+    caller factors: (seconds, corrected fit, lambda)."""
+    N = len(ndims)
+    stride = stride_of(rank)
+    nd, ndp = _u32(ndims)
+    keep, ip = _rows(list(inds), u32p, np.uint32)
+    v = np.ascontiguousarray(vals, np.float32)
+    facs = [_padded(np.asarray(a, np.float32)[:, :rank], stride) for a in init]
+    fk, fp = _rows(facs, f32p, np.float32)
+    lam = np.zeros(rank, np.float32)
+    fit = C.c_double()
+    with quiet_stdout():
+        t = ref().ref_omp_cpd(N, ndp, v.shape[0], ip, v.ctypes.data_as(f32p), rank, niters, fp, stride, tk,
+                              lam.ctypes.data_as(f32p), C.byref(fit))
+    return t, fit.value, lam

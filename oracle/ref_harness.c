@@ -15,6 +15,14 @@
 #include <time.h>
 #include "clapack.h"
 
+/* Exported by the reference but declared in none of its headers
+ * (cpd.c:30-36, cpd_omp.c:32-41). */
+double CpdAlsStep(sptSparseTensor const *const spten, sptIndex const rank, sptIndex const niters, double const tol,
+                  sptMatrix **mats, sptValue *const lambda);
+double OmpCpdAlsStep(sptSparseTensor const *const spten, sptIndex const rank, sptIndex const niters,
+                     double const tol, const int tk, const int use_reduce, sptMatrix **mats, sptMatrix **copy_mats,
+                     sptValue *const lambda);
+
 static void build_tensor(sptSparseTensor *X, uint32_t nmodes, const uint32_t *ndims, uint64_t nnz,
                          uint32_t *const *inds, const float *vals) {
     sptNewSparseTensor(X, nmodes, ndims);
@@ -179,6 +187,7 @@ int ref_mttkrp_hicoo(uint32_t nmodes, const uint32_t *ndims, uint64_t nnz, uint3
 static double corrected_fit(const sptSparseTensor *X, sptMatrix **U, const sptValue *lambda, uint32_t R) {
     const uint32_t N = X->nmodes;
     double nx = 0, inner = 0, nk = 0;
+#pragma omp parallel for reduction(+ : nx, inner) schedule(static)
     for (uint64_t x = 0; x < X->nnz; ++x) {
         const double v = X->values.data[x];
         nx += v * v;
@@ -190,6 +199,7 @@ static double corrected_fit(const sptSparseTensor *X, sptMatrix **U, const sptVa
         }
         inner += v * s;
     }
+#pragma omp parallel for reduction(+ : nk) schedule(dynamic)
     for (uint32_t p = 0; p < R; ++p)
         for (uint32_t q = 0; q < R; ++q) {
             double h = 1;
@@ -429,4 +439,143 @@ int ref_dump_arrays(const uint32_t *a, uint64_t na, const uint64_t *b, uint64_t 
     if (!r) r = sptDumpNnzIndexArray((sptNnzIndex *)b, nb, fp);
     fclose(fp);
     return r;
+}
+
+/* ----------------------------------------------------- timing sessions --
+ * The reference's own CPU path timed on a tensor it holds in its own
+ * containers: the tensor comes from the library's seeded generator
+ * (sptgbGenerate, gen.c linked into this library, where it builds the tensor
+ * through the reference's sptNewSparseTensor), the factors from the same
+ * generator's sptgbFillMatrix, so a process timing the reference loads no
+ * part of libParTI.so.  Protocol of examples/mttkrp.c:160-274 (sortcase 0):
+ * the tensor is put in lexicographic order with sptSparseTensorSortIndex
+ * (force = 0: the generator's output is already in that order and its
+ * sortorder is the identity, so the reference skips the sort), mats_order =
+ * {mode, mode+1, ...}, and each call is timed alone. */
+int sptgbGenerate(sptSparseTensor *X, const void *spec);
+int sptgbFillMatrix(sptMatrix *mtx, uint64_t seed, uint64_t stream_id, float lo, float hi);
+
+typedef struct {
+    sptSparseTensor X;
+    sptMatrix **U;      /* nmodes factors, then the output mats[nmodes] */
+    sptMatrix **copies; /* tk thread-private outputs of sptOmpMTTKRP_Reduce */
+    uint32_t R;
+    int tk;
+} ref_session;
+
+void ref_session_close(ref_session *s) {
+    if (!s) return;
+    if (s->U) free_mats(s->U, s->X.nmodes);
+    if (s->copies) {
+        for (int t = 0; t < s->tk; ++t) {
+            sptFreeMatrix(s->copies[t]);
+            free(s->copies[t]);
+        }
+        free(s->copies);
+    }
+    sptFreeSparseTensor(&s->X);
+    free(s);
+}
+
+/* Generates the tensor and factors U[0,1) (seed fac_seed, stream m for mode
+ * m, as sptgbFillMatrix fills them for the GPU arm) and the tk copies. */
+ref_session *ref_session_open(const void *spec, uint32_t R, uint64_t fac_seed, int tk) {
+    ref_session *s = (ref_session *)calloc(1, sizeof *s);
+    if (!s) return NULL;
+    if (sptgbGenerate(&s->X, spec)) {
+        free(s);
+        return NULL;
+    }
+    sptSparseTensorSortIndex(&s->X, 0, tk);
+    const uint32_t N = s->X.nmodes;
+    uint32_t maxd = 0;
+    s->U = (sptMatrix **)malloc((N + 1) * sizeof(*s->U));
+    for (uint32_t m = 0; m < N; ++m) {
+        s->U[m] = (sptMatrix *)malloc(sizeof(sptMatrix));
+        sptNewMatrix(s->U[m], s->X.ndims[m], R);
+        sptgbFillMatrix(s->U[m], fac_seed, m, 0.0f, 1.0f);
+        if (s->X.ndims[m] > maxd) maxd = s->X.ndims[m];
+    }
+    s->U[N] = (sptMatrix *)malloc(sizeof(sptMatrix));
+    sptNewMatrix(s->U[N], maxd, R);
+    sptConstantMatrix(s->U[N], 0);
+    s->copies = (sptMatrix **)malloc(tk * sizeof(*s->copies));
+    for (int t = 0; t < tk; ++t) {
+        s->copies[t] = (sptMatrix *)malloc(sizeof(sptMatrix));
+        sptNewMatrix(s->copies[t], maxd, R);
+        sptConstantMatrix(s->copies[t], 0);
+    }
+    s->R = R;
+    s->tk = tk;
+    return s;
+}
+
+uint64_t ref_session_nnz(const ref_session *s) { return s->X.nnz; }
+
+void ref_session_ndims(const ref_session *s, uint32_t *out) {
+    for (uint32_t m = 0; m < s->X.nmodes; ++m) out[m] = s->X.ndims[m];
+}
+
+/* One MTTKRP of `mode`: which 0 sptMTTKRP, 1 sptOmpMTTKRP_Reduce,
+ * 2 sptOmpMTTKRP (atomics).  Returns the seconds of the call (negative when
+ * the call fails); out (ndims[mode] x stride, may be NULL) receives M. */
+double ref_session_mttkrp(ref_session *s, int which, uint32_t mode, float *out) {
+    const uint32_t N = s->X.nmodes;
+    sptIndex order[8];
+    order[0] = mode;
+    for (uint32_t i = 1; i < N; ++i) order[i] = (mode + i) % N;
+    s->U[N]->nrows = s->X.ndims[mode];
+    const double t0 = now_s();
+    int r;
+    if (which == 0) r = sptMTTKRP(&s->X, s->U, order, mode);
+    else if (which == 1) r = sptOmpMTTKRP_Reduce(&s->X, s->U, s->copies, order, mode, s->tk);
+    else r = sptOmpMTTKRP(&s->X, s->U, order, mode, s->tk);
+    const double dt = now_s() - t0;
+    if (out) memcpy(out, s->U[N]->values, (size_t)s->X.ndims[mode] * s->U[N]->stride * sizeof(float));
+    return r ? -1.0 : dt;
+}
+
+/* The reference's sptOmpCpdAls loop, OmpCpdAlsStep (cpd_omp.c:32-157), run
+ * from the session's factors as the initial guess (cpd_omp.c:166-228 only
+ * adds sptRandomizeMatrix initialisation and the allocations); the factors
+ * are overwritten with the result.  Returns the seconds of the call;
+ * *fit receives the corrected fit of the result (FP64, full symmetric Grams),
+ * lambda (R entries) the final lambda. */
+double ref_session_cpd(ref_session *s, uint32_t niters, int use_reduce, float *lambda, double *fit) {
+    const double t0 = now_s();
+    OmpCpdAlsStep(&s->X, s->R, niters, 0.0, s->tk, use_reduce, s->U, s->copies, lambda);
+    const double dt = now_s() - t0;
+    if (fit) *fit = corrected_fit(&s->X, s->U, lambda, s->R);
+    return dt;
+}
+
+/* OmpCpdAlsStep on a tensor given as flat arrays from caller factors (one
+ * request of a stream).  Returns the seconds of the OmpCpdAlsStep call. */
+double ref_omp_cpd(uint32_t nmodes, const uint32_t *ndims, uint64_t nnz, uint32_t *const *inds, const float *vals,
+                   uint32_t R, uint32_t niters, float *const *init, uint32_t stride, int tk, float *lambda,
+                   double *fit) {
+    sptSparseTensor X;
+    build_tensor(&X, nmodes, ndims, nnz, inds, vals);
+    sptMatrix **U = build_mats(nmodes, ndims, R, init, stride);
+    uint32_t maxd = 0;
+    for (uint32_t m = 0; m < nmodes; ++m)
+        if (ndims[m] > maxd) maxd = ndims[m];
+    sptMatrix **copies = (sptMatrix **)malloc(tk * sizeof(*copies));
+    for (int t = 0; t < tk; ++t) {
+        copies[t] = (sptMatrix *)malloc(sizeof(sptMatrix));
+        sptNewMatrix(copies[t], maxd, R);
+        sptConstantMatrix(copies[t], 0);
+    }
+    const double t0 = now_s();
+    OmpCpdAlsStep(&X, R, niters, 0.0, tk, 1, U, copies, lambda);
+    const double dt = now_s() - t0;
+    if (fit) *fit = corrected_fit(&X, U, lambda, R);
+    for (int t = 0; t < tk; ++t) {
+        sptFreeMatrix(copies[t]);
+        free(copies[t]);
+    }
+    free(copies);
+    free_mats(U, nmodes);
+    sptFreeSparseTensor(&X);
+    return dt;
 }

@@ -81,10 +81,10 @@ def test_ctypes_mirror_matches_header():
     assert int(ours["sptSparseTensorHiCOO.bptr"]) == S.HiCOOS.bptr.offset
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(O.REF_SRC, "include")), reason="reference headers not present")
+@pytest.mark.skipif(not os.path.isdir(os.path.join(O.REF_TREE, "include")), reason="reference headers not present")
 def test_struct_layouts_equal_reference():
     ours = layout(os.path.join(ROOT, "include"))
-    ref = layout(os.path.join(O.REF_SRC, "include"), ["-DPARTI_INDEX_TYPEWIDTH=32", "-DPARTI_VALUE_TYPEWIDTH=32",
+    ref = layout(os.path.join(O.REF_TREE, "include"), ["-DPARTI_INDEX_TYPEWIDTH=32", "-DPARTI_VALUE_TYPEWIDTH=32",
                                              "-DPARTI_ELEMENT_INDEX_TYPEWIDTH=8", "-DPARTI_USE_OPENMP", "-fopenmp"])
     assert ours == ref
 

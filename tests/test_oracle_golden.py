@@ -137,7 +137,7 @@ def test_threaded_fp64_oracle_equals_sequential():
         assert np.abs(a - b).max() <= 1e-13 * np.abs(a).max()
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(O.REF_SRC, "src")), reason="reference sources not present")
+@pytest.mark.skipif(not os.path.isdir(os.path.join(O.REF_TREE, "src")), reason="reference sources not present")
 @pytest.mark.parametrize("mode", [0, 1, 2])
 def test_ttm_oracle_equals_reference(mode):
     """The TTM restatement against the reference's own sptSparseTensorMulMatrix
