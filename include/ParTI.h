@@ -43,9 +43,22 @@ typedef unsigned __int128 sptMortonIndex;
 #define PARTI_VALUE_TYPEWIDTH 32
 #define PARTI_ELEMENT_INDEX_TYPEWIDTH 8
 #define PARTI_INDEX_MAX UINT32_MAX
+/* printf / scanf conversions of the types above (types.h:30-92); callers
+ * such as examples/mttkrp.c read their options with them */
 #define PARTI_PRI_INDEX PRIu32
-#define PARTI_PRI_NNZ_INDEX PRIu64
+#define PARTI_SCN_INDEX SCNu32
+#define PARTI_PRI_BLOCK_INDEX PRIu32
+#define PARTI_SCN_BLOCK_INDEX SCNu32
 #define PARTI_PRI_VALUE "f"
+#define PARTI_SCN_VALUE "f"
+#define PARTI_PRI_ELEMENT_INDEX PRIu8
+#define PARTI_SCN_ELEMENT_INDEX SCNu8
+#define PARTI_PRI_BLOCKMATRIX_INDEX PRIu16
+#define PARTI_SCN_BLOCKMATRIX_INDEX SCNu16
+#define PARTI_PRI_BLOCKNNZ_INDEX PARTI_PRI_BLOCK_INDEX
+#define PARTI_SCN_BLOCKNNZ_INDEX PARTI_SCN_BLOCK_INDEX
+#define PARTI_PRI_NNZ_INDEX PRIu64
+#define PARTI_SCN_NNZ_INDEX SCNu64
 
 /* --------------------------------------------------------------- errors --
  * Same codes as SptError (macros.h:44-52).  CUDA failures are reported as
@@ -179,6 +192,13 @@ typedef struct sptTagTimer *sptTimer;
 int  sptGetLastError(const char **module, const char **file, unsigned *line, const char **reason);
 void sptClearLastError(void);
 
+/* Assertion and helpers of include/includes/helper_funcs.h:35-51: sptAssert
+ * prints the failed expression and aborts (spt_Panic, src/error/error.c:75);
+ * sptBytesString returns a malloc'd "12.34MB"-style string (src/base.c:25). */
+void  spt_Panic(const char *file, unsigned line, const char *expr);
+#define sptAssert(expr) ((expr) ? (void)0 : spt_Panic(__FILE__, __LINE__, #expr))
+char *sptBytesString(uint64_t const bytes);
+
 /* ------------------------------------------------------------- timers -- */
 int    sptNewTimer(sptTimer *timer, int use_cuda);
 int    sptStartTimer(sptTimer timer);
@@ -243,6 +263,13 @@ int    sptNewSparseTensor(sptSparseTensor *tsr, sptIndex nmodes, const sptIndex 
 int    sptCopySparseTensor(sptSparseTensor *dest, const sptSparseTensor *src, int const nt);
 void   sptFreeSparseTensor(sptSparseTensor *tsr);
 double SparseTensorFrobeniusNormSquared(sptSparseTensor const *const spten);
+
+/* Host-side summaries and reorderings (src/sptensor/status.c:24-58,
+ * src/sptensor/sort.c:371-380): the density, a printed summary, and the
+ * reference's deterministic element shuffle (srand(z + 1) per position). */
+double sptSparseTensorDensity(sptSparseTensor const *const tsr);
+void   sptSparseTensorStatus(sptSparseTensor *tsr, FILE *fp);
+void   sptGetRandomShuffleElements(sptSparseTensor *tsr);
 
 void sptGetBestModeOrder(sptIndex *mode_order, sptIndex const mode, sptIndex const *ndims, sptIndex const nmodes);
 void sptGetWorstModeOrder(sptIndex *mode_order, sptIndex const mode, sptIndex const *ndims, sptIndex const nmodes);

@@ -193,6 +193,50 @@ int sptNewSparseTensor(sptSparseTensor *tsr, sptIndex nmodes, const sptIndex ndi
     return sptNewValueVector(&tsr->values, 0, 0);
 }
 
+/* status.c:24-34: the geometric-mean density nnz^(1/N) / ndims[m], multiplied over the modes. */
+double sptSparseTensorDensity(sptSparseTensor const *const tsr) {
+    const double root = pow((double)tsr->nnz, 1. / (double)tsr->nmodes);
+    double density = 1.0;
+    for (sptIndex m = 0; m < tsr->nmodes; ++m) density *= root / (double)tsr->ndims[m];
+    return density;
+}
+
+/* status.c:38-58: the same lines, in the same format. */
+void sptSparseTensorStatus(sptSparseTensor *tsr, FILE *fp) {
+    fprintf(fp, "COO Sparse Tensor information (use sptIndex, sptValue))---------\n");
+    fprintf(fp, "DIMS=%" PARTI_PRI_INDEX, tsr->ndims[0]);
+    for (sptIndex m = 1; m < tsr->nmodes; ++m) fprintf(fp, "x%" PARTI_PRI_INDEX, tsr->ndims[m]);
+    fprintf(fp, " NNZ=%" PARTI_PRI_NNZ_INDEX, tsr->nnz);
+    fprintf(fp, " DENSITY=%e\n", sptSparseTensorDensity(tsr));
+    fprintf(fp, "Average slice length (c): ");
+    for (sptIndex m = 0; m + 1 < tsr->nmodes; ++m) fprintf(fp, "%.2lf , ", (double)tsr->nnz / tsr->ndims[m]);
+    fprintf(fp, "%.2lf\n", (double)tsr->nnz / tsr->ndims[tsr->nmodes - 1]);
+    char *b = sptBytesString(tsr->nnz * (sizeof(sptIndex) * tsr->nmodes + sizeof(sptValue)));
+    fprintf(fp, "COO-STORAGE=%s\n", b ? b : "?");
+    fprintf(fp, "\n");
+    free(b);
+}
+
+/* sort.c:371-380: for every position z, srand(z + 1), one rand() scaled to a
+ * position, and a swap of the two nonzeros (all modes and the value); the C
+ * library's rand() makes it the reference's permutation on the same libc. */
+void sptGetRandomShuffleElements(sptSparseTensor *tsr) {
+    const sptNnzIndex nnz = tsr->nnz;
+    for (sptNnzIndex z = 0; z < nnz; ++z) {
+        srand((unsigned)(z + 1));
+        const sptValue u = (sptValue)rand() / (sptValue)RAND_MAX;
+        const sptNnzIndex w = (sptNnzIndex)(u * nnz) % nnz;
+        for (sptIndex m = 0; m < tsr->nmodes; ++m) {
+            const sptIndex t = tsr->inds[m].data[z];
+            tsr->inds[m].data[z] = tsr->inds[m].data[w];
+            tsr->inds[m].data[w] = t;
+        }
+        const sptValue t = tsr->values.data[z];
+        tsr->values.data[z] = tsr->values.data[w];
+        tsr->values.data[w] = t;
+    }
+}
+
 int sptCopySparseTensor(sptSparseTensor *dest, const sptSparseTensor *src, int const nt) {
     dest->nmodes = src->nmodes;
     dest->sortorder = malloc(src->nmodes * sizeof src->sortorder[0]);

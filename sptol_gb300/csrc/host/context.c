@@ -73,6 +73,24 @@ void sptClearLastError(void) {
     g_last.reason = NULL;
 }
 
+void spt_Panic(const char *file, unsigned line, const char *expr) {
+    fprintf(stderr, "%s:%u: assertion error: \"%s\"\n", file, line, expr);
+    abort();
+}
+
+char *sptBytesString(uint64_t const bytes) {
+    static const char *const suffix[] = {"B", "KB", "MB", "GB", "TB"};
+    double size = (double)bytes;
+    int k = 0;
+    while (size > 1024 && k < 4) {
+        size /= 1024.;
+        ++k;
+    }
+    char *ret = NULL;
+    if (asprintf(&ret, "%0.2f%s", size, suffix[k]) == -1) ret = NULL;
+    return ret;
+}
+
 int sptgb_cuda_fail(cudaError_t e, const char *module, const char *file, unsigned line) {
     const int code = SPTERR_CUDA_ERROR + (int)e;
     spt_ComplainError(module, code, file, line, cudaGetErrorString(e));
@@ -82,8 +100,6 @@ int sptgb_cuda_fail(cudaError_t e, const char *module, const char *file, unsigne
 static void ctx_init_once(void) {
     const char *d = getenv("SPTGB_DEVICE");
     g_device = d ? atoi(d) : 0;
-    const char *s = getenv("SPTGB_SEED");
-    if (s) g_seed = strtoull(s, NULL, 0);
     cudaError_t e = cudaSetDevice(g_device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g_copy_stream, cudaStreamNonBlocking);
@@ -100,6 +116,23 @@ int sptgb_ctx(void) {
         if (e != cudaSuccess) return sptgb_cuda_fail(e, "SpTns GPU init", __FILE__, __LINE__);
     }
     return 0;
+}
+
+/* Streaming multiprocessors of the library's device (grid caps of the
+ * grid-stride kernels are multiples of it); looked up once. */
+static _Atomic int g_sm_count = 0;
+
+int sptgb_sm_count(void) {
+    int n = atomic_load(&g_sm_count);
+    if (n > 0) return n;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
+        cudaGetLastError();
+        return 1;   /* not cached: a later call retries */
+    }
+    atomic_store(&g_sm_count, n);
+    return n;
 }
 
 cudaStream_t sptgb_stream(void) { return g_stream; }
@@ -150,11 +183,23 @@ void *sptgbStream(void) {
 
 uint64_t sptgbLaunchCount(void) { return atomic_load(&g_launches); }
 
-void sptgbSetSeed(uint64_t seed) { g_seed = seed; }
+/* SPTGB_SEED is read once, on the first use of the seed, whether or not a
+ * device call came first; sptgbSetSeed overrides it. */
+static pthread_once_t g_seed_once = PTHREAD_ONCE_INIT;
+static void seed_from_env(void) {
+    const char *s = getenv("SPTGB_SEED");
+    if (s) g_seed = strtoull(s, NULL, 0);
+}
+
+void sptgbSetSeed(uint64_t seed) {
+    pthread_once(&g_seed_once, seed_from_env);
+    g_seed = seed;
+}
 
 uint64_t sptgb_seed_next(void) {
     /* Each randomised matrix gets its own stream of the seed. */
     static _Atomic uint64_t counter = 0;
+    pthread_once(&g_seed_once, seed_from_env);
     return g_seed * 0x9E3779B97F4A7C15ULL + atomic_fetch_add(&counter, 1) + 1;
 }
 
