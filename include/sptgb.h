@@ -167,15 +167,17 @@ void sptgbServerFree(sptgbServer *s);
 
 /* ------------------------------------------------ without device allocation --
  * No counterpart in the reference.  ||X||^2 of the tensor's values, as
- * SparseTensorFrobeniusNormSquared computes it, for callers that must not
- * allocate device memory (their device memory is owned by another allocator,
- * or they cannot pay for cudaMalloc/cudaFree per call): the values and the
- * reduction partials are staged in a fixed 16 MiB array inside the library
- * instead.  At most 4,194,304 nonzeros (SPTERR_VALUE_ERROR above that).  The
- * first call on a device looks up that array's address and should come
- * before any stream capture.  All calls share the array, so calls that
- * overlap on the GPU race; serialise them.  stream: cudaStream_t as void*
- * (NULL = default stream); returns once *normsq is written. */
+ * SparseTensorFrobeniusNormSquared computes it (FP32 squares summed in FP64),
+ * for callers that must not allocate device memory (their device memory is
+ * owned by another allocator, or they cannot pay for cudaMalloc/cudaFree per
+ * call): the values and the reduction partials are staged in a fixed 16 MiB
+ * array inside the library instead.  At most 4,194,304 nonzeros
+ * (SPTERR_VALUE_ERROR above that).  Runs on the calling thread's current
+ * device; each call looks up the array's address in that device's context.
+ * All calls share the array, so calls that overlap on the GPU race; serialise
+ * them.  stream: cudaStream_t as void* (NULL = default stream); the call
+ * synchronises the stream and returns once *normsq is written, so it cannot
+ * be made while the stream is capturing a CUDA graph. */
 int sptgbSparseTensorFrobeniusNormSquaredNoAlloc(sptSparseTensor const *spten, double *normsq, void *stream);
 
 #ifdef __cplusplus

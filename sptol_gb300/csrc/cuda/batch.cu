@@ -414,7 +414,7 @@ extern "C" uint32_t sptgb_gram_blocks(uint32_t nrows) { return (uint32_t)nblocks
 
 extern "C" cudaError_t sptgb_adm_check(const sptgb_adm_group *g, cudaStream_t s) {
     if (g->total == 0) return cudaSuccess;
-    k_adm_check<<<grid_for(g->total, 152 * 16), 256, 0, s>>>(*g);
+    k_adm_check<<<grid_for(g->total, (unsigned)sptgb_sm_count() * 16), 256, 0, s>>>(*g);
     sptgb_count_launch(1);
     return cudaGetLastError();
 }
@@ -422,7 +422,7 @@ extern "C" cudaError_t sptgb_adm_check(const sptgb_adm_group *g, cudaStream_t s)
 extern "C" cudaError_t sptgb_adm_keys(const sptgb_adm_group *g, int mode, int rowbits, int kind,
                                       const uint32_t *perm, uint32_t *keys, cudaStream_t s) {
     if (g->total == 0) return cudaSuccess;
-    k_adm_keys<<<grid_for(g->total, 152 * 16), 256, 0, s>>>(*g, mode, rowbits, kind, perm, keys);
+    k_adm_keys<<<grid_for(g->total, (unsigned)sptgb_sm_count() * 16), 256, 0, s>>>(*g, mode, rowbits, kind, perm, keys);
     sptgb_count_launch(1);
     return cudaGetLastError();
 }
@@ -430,7 +430,7 @@ extern "C" cudaError_t sptgb_adm_keys(const sptgb_adm_group *g, int mode, int ro
 extern "C" cudaError_t sptgb_adm_pack(const sptgb_adm_group *g, const sptgb_slot *slots, int mode,
                                       const uint32_t *perm, cudaStream_t s) {
     if (g->total == 0) return cudaSuccess;
-    k_adm_pack<<<grid_for(g->total, 152 * 16), 256, 0, s>>>(*g, slots, mode, perm);
+    k_adm_pack<<<grid_for(g->total, (unsigned)sptgb_sm_count() * 16), 256, 0, s>>>(*g, slots, mode, perm);
     sptgb_count_launch(1);
     return cudaGetLastError();
 }

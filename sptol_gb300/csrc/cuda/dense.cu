@@ -100,7 +100,7 @@ extern "C" cudaError_t sptgb_normalize(float *X, uint32_t nrows, int rank, int s
     k_lambda<<<1, DT, 0, s>>>(ws, ws + NBLK * P, nb, rank, use_2norm, gram, lambda_f32, nullptr);
     uint64_t total = (uint64_t)nrows * rank;
     uint64_t g = (total + 255) / 256;
-    if (g > 152 * 16) g = 152 * 16;
+    if (g > (uint64_t)sptgb_sm_count() * 16) g = (uint64_t)sptgb_sm_count() * 16;
     if (g < 1) g = 1;
     k_scale_cols<<<(unsigned)g, 256, 0, s>>>(X, nrows, rank, stride, lambda_f32);
     sptgb_count_launch(2);
@@ -143,7 +143,7 @@ extern "C" cudaError_t sptgb_colnorm_scale(float *A, uint32_t nrows, int rank, i
     k_colnorm_final<<<1, 64, 0, s>>>(ws, nb, rank, lambda_mul, norms);
     uint64_t total = (uint64_t)nrows * rank;
     uint64_t g = (total + 255) / 256;
-    if (g > 152 * 16) g = 152 * 16;
+    if (g > (uint64_t)sptgb_sm_count() * 16) g = (uint64_t)sptgb_sm_count() * 16;
     if (g < 1) g = 1;
     k_scale_cols<<<(unsigned)g, 256, 0, s>>>(A, nrows, rank, stride, norms);
     sptgb_count_launch(3);
@@ -153,7 +153,7 @@ extern "C" cudaError_t sptgb_colnorm_scale(float *A, uint32_t nrows, int rank, i
 extern "C" cudaError_t sptgb_f32_to_bf16(const float *in, uint16_t *out, uint64_t n, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     uint64_t g = (n + 255) / 256;
-    if (g > 152 * 32) g = 152 * 32;
+    if (g > (uint64_t)sptgb_sm_count() * 32) g = (uint64_t)sptgb_sm_count() * 32;
     k_f32_to_bf16<<<(unsigned)g, 256, 0, s>>>(in, out, n);
     sptgb_count_launch(1);
     return cudaGetLastError();
@@ -305,7 +305,7 @@ extern "C" cudaError_t sptgb_colmax_scale(float *A, uint32_t nrows, int rank, in
     k_colmax_final<<<1, 64, 0, s>>>(ws, nb, rank, lambda);
     uint64_t total = (uint64_t)nrows * (stride / 4);
     uint64_t g = (total + 255) / 256;
-    if (g > 152 * 16) g = 152 * 16;
+    if (g > (uint64_t)sptgb_sm_count() * 16) g = (uint64_t)sptgb_sm_count() * 16;
     if (g < 1) g = 1;
     k_scale_cols<<<(unsigned)g, 256, 0, s>>>(A, nrows, rank, stride, lambda);
     sptgb_count_launch(3);

@@ -632,9 +632,11 @@ __device__ __forceinline__ void fit_final_body(const double *__restrict__ part, 
 __device__ __forceinline__ void sumsq_partial_body(const float *__restrict__ v, uint64_t n, double *part, unsigned bid, unsigned nbk) {
     __shared__ double red[DT];
     double s = 0.0;
+    // vals[n] * vals[n] rounded in FP32 and summed in FP64, as the reference's
+    // SparseTensorFrobeniusNormSquared (src/sptensor/sptensor.c:96-107) does
     for (uint64_t i = bid * (uint64_t)DT + threadIdx.x; i < n; i += (uint64_t)nbk * DT) {
-        const double x = v[i];
-        s += x * x;
+        const float x = v[i];
+        s += (double)__fmul_rn(x, x);
     }
     red[threadIdx.x] = s;
     __syncthreads();

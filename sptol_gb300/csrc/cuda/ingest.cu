@@ -166,7 +166,7 @@ __global__ void k_segment_sums(const uint64_t *__restrict__ starts, uint64_t ng,
 
 unsigned grid_for(uint64_t n) {
     uint64_t b = (n + 255) / 256;
-    if (b > 152 * 16) b = 152 * 16;
+    if (b > (uint64_t)sptgb_sm_count() * 16) b = (uint64_t)sptgb_sm_count() * 16;
     return b ? (unsigned)b : 1u;
 }
 

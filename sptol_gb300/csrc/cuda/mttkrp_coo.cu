@@ -380,7 +380,7 @@ extern "C" cudaError_t sptgb_pack_records(const uint32_t *rows, const uint32_t *
                                           void *rec, uint64_t n, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     uint64_t g = (n + 255) / 256;
-    if (g > 152ull * 16) g = 152ull * 16;
+    if (g > (uint64_t)sptgb_sm_count() * 16) g = (uint64_t)sptgb_sm_count() * 16;
     k_pack_records<<<(unsigned)g, 256, 0, s>>>(rows, ia, ib, vals, lim_a, lim_b, bad, static_cast<uint4 *>(rec), n);
     sptgb_count_launch(1);
     return cudaGetLastError();
@@ -402,7 +402,7 @@ extern "C" cudaError_t sptgb_pack_records4(const uint32_t *rows, const uint32_t 
                                            unsigned int *bad, void *rec, uint64_t n, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     uint64_t g = (n + 255) / 256;
-    if (g > 152ull * 16) g = 152ull * 16;
+    if (g > (uint64_t)sptgb_sm_count() * 16) g = (uint64_t)sptgb_sm_count() * 16;
     k_pack_records4<<<(unsigned)g, 256, 0, s>>>(rows, ia, ib, ic, lim_a, lim_b, lim_c, bad, static_cast<uint4 *>(rec),
                                                 n);
     sptgb_count_launch(1);

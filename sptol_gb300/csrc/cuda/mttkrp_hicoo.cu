@@ -613,7 +613,7 @@ extern "C" cudaError_t sptgb_hicoo_schedule(const uint32_t *binds_mode, const ui
     e = cudaMemcpyAsync(perm, vals[which], nb * 4, cudaMemcpyDeviceToDevice, s);
     if (e != cudaSuccess) return e;
     uint64_t g = (nb + 255) / 256;
-    if (g > 152 * 16) g = 152 * 16;
+    if (g > (uint64_t)sptgb_sm_count() * 16) g = (uint64_t)sptgb_sm_count() * 16;
     k_block_sizes<<<(unsigned)g, 256, 0, s>>>(perm, bptr, nb, w->flags);
     sptgb_count_launch(1);
     e = cudaGetLastError();
@@ -634,7 +634,7 @@ extern "C" cudaError_t sptgb_hicoo_schedule(const uint32_t *binds_mode, const ui
     *nwin_out = nwin;
     // the heavy windows, ascending
     uint64_t gw = (nwin + 255) / 256;
-    if (gw > 152 * 16) gw = 152 * 16;
+    if (gw > (uint64_t)sptgb_sm_count() * 16) gw = (uint64_t)sptgb_sm_count() * 16;
     k_window_heavy<<<(unsigned)gw, 256, 0, s>>>(wst, pnnz, nwin, SPTGB_HICOO_HEAVY, w->flags);
     sptgb_count_launch(1);
     e = cudaGetLastError();
@@ -661,7 +661,7 @@ extern "C" cudaError_t sptgb_hicoo_check_bptr(const uint64_t *bptr, uint64_t nb,
     cudaError_t e = cudaMemsetAsync(bad, 0, sizeof(unsigned int), s);
     if (e != cudaSuccess || nb == 0) return e;
     uint64_t g = (nb + 255) / 256;
-    if (g > 152 * 16) g = 152 * 16;
+    if (g > (uint64_t)sptgb_sm_count() * 16) g = (uint64_t)sptgb_sm_count() * 16;
     k_bptr_check<<<(unsigned)g, 256, 0, s>>>(bptr, nb, nnz, bad);
     sptgb_count_launch(1);
     return cudaGetLastError();
@@ -670,7 +670,7 @@ extern "C" cudaError_t sptgb_hicoo_check_bptr(const uint64_t *bptr, uint64_t nb,
 extern "C" cudaError_t sptgb_hicoo_check(const sptgb_hicoo_args *a, cudaStream_t s) {
     if (a->nb == 0) return cudaSuccess;
     uint64_t g = (a->nb + 255) / 256;
-    if (g > 152 * 16) g = 152 * 16;
+    if (g > (uint64_t)sptgb_sm_count() * 16) g = (uint64_t)sptgb_sm_count() * 16;
     k_hicoo_check<<<(unsigned)g, 256, 0, s>>>(a->bptr, *a, a->nb);
     sptgb_count_launch(1);
     return cudaGetLastError();

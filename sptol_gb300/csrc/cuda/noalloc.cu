@@ -15,15 +15,16 @@
 // (room for 4,194,304 float values, 304 partial sums and the result): every GPU
 // that loads the library holds it until the process exits.  Host code cannot
 // use the array's name as a device address (on the host it names a stand-in),
-// so the first call on each device, with that device current, looks the
-// address up with cudaGetSymbolAddress and caches it; that first call should
-// come before any stream capture.  All calls share the array and it keeps the
-// last call's contents: each call overwrites every partial slot and the
-// result slot it reads, so nothing has to start at zero, and calls that
-// overlap on the GPU (different streams or threads at the same time) race on
-// the array and must be serialised by the caller.
+// so every call looks the address up with cudaGetSymbolAddress on the device
+// (and CUDA context) current in the calling thread; the lookup is cheap once
+// the module is loaded, and no address outlives a context.  All calls share
+// the array and it keeps the last call's contents: each call overwrites every
+// partial slot and the result slot it reads, so nothing has to start at zero,
+// and calls that overlap on the GPU (different streams or threads at the same
+// time) race on the array and must be serialised by the caller.  Every call
+// ends by synchronising its stream and copying the result into host memory,
+// so it cannot be called while that stream is capturing a CUDA graph.
 #include <cuda_runtime.h>
-#include <pthread.h>
 #include <stdint.h>
 #include "../sptgb_internal.h"
 #include "../../../include/sptgb.h"
@@ -40,20 +41,17 @@ static __device__ __align__(256) unsigned char g_sptgb_noalloc_scratch[NA_SCRATC
 
 namespace {
 
-constexpr int NA_MAX_DEVICES = 64;
-pthread_mutex_t g_na_lock = PTHREAD_MUTEX_INITIALIZER;
-unsigned char *g_na_ptr[NA_MAX_DEVICES];
-
 // Each of the NA_BLOCKS blocks writes its own partial slot (zero when it has
 // no values), so no slot keeps a previous call's value.
 __global__ void __launch_bounds__(NA_THREADS)
 k_na_sumsq_partial(const float *__restrict__ v, uint64_t n, double *__restrict__ part) {
     __shared__ double red[NA_THREADS];
     double s = 0.0;
+    // FP32 products summed in FP64, as src/sptensor/sptensor.c:96-107
     for (uint64_t i = blockIdx.x * (uint64_t)NA_THREADS + threadIdx.x; i < n;
          i += (uint64_t)gridDim.x * NA_THREADS) {
-        const double x = v[i];
-        s += x * x;
+        const float x = v[i];
+        s += (double)__fmul_rn(x, x);
     }
     red[threadIdx.x] = s;
     __syncthreads();
@@ -72,28 +70,13 @@ __global__ void k_na_sum_final(const double *__restrict__ part, double *__restri
     }
 }
 
-// Device address of the scratch array on the current device (looked up once
-// per device).
+// Device address of the scratch array in the current device's context,
+// looked up on every call.
 int na_scratch(unsigned char **ptr) {
-    int dev = -1;
-    cudaError_t e = cudaGetDevice(&dev);
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_sptgb_noalloc_scratch);
     if (e != cudaSuccess) return sptgb_cuda_fail(e, "SpTns NormSq no-alloc", __FILE__, __LINE__);
-    if (dev < 0 || dev >= NA_MAX_DEVICES) {
-        spt_ComplainError("SpTns NormSq no-alloc", SPTERR_VALUE_ERROR, __FILE__, __LINE__, "device index too large");
-        return SPTERR_VALUE_ERROR;
-    }
-    pthread_mutex_lock(&g_na_lock);
-    if (!g_na_ptr[dev]) {
-        void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_sptgb_noalloc_scratch);
-        if (e != cudaSuccess) {
-            pthread_mutex_unlock(&g_na_lock);
-            return sptgb_cuda_fail(e, "SpTns NormSq no-alloc", __FILE__, __LINE__);
-        }
-        g_na_ptr[dev] = static_cast<unsigned char *>(p);
-    }
-    *ptr = g_na_ptr[dev];
-    pthread_mutex_unlock(&g_na_lock);
+    *ptr = static_cast<unsigned char *>(p);
     return 0;
 }
 

@@ -415,7 +415,7 @@ __global__ void k_hicoo_split(SplitArg a, int nmodes, int sb, uint64_t n, const 
 
 inline unsigned grid_for(uint64_t n, unsigned threads) {
     uint64_t g = (n + threads - 1) / threads;
-    if (g > 152ull * 32) g = 152ull * 32;
+    if (g > (uint64_t)sptgb_sm_count() * 32) g = (uint64_t)sptgb_sm_count() * 32;
     if (g == 0) g = 1;
     return (unsigned)g;
 }

@@ -49,7 +49,7 @@ template <int W>
 cudaError_t launch(const uint64_t *starts, uint64_t nfib, uint64_t nnz, const uint32_t *rows, const float *vals,
                    const float *U, uint32_t ustride, uint32_t ncols, float *Y, uint32_t ystride, cudaStream_t s) {
     uint64_t blocks = (nfib * W + BLOCK - 1) / BLOCK;
-    if (blocks > 152ull * 8) blocks = 152ull * 8;
+    if (blocks > (uint64_t)sptgb_sm_count() * 8) blocks = (uint64_t)sptgb_sm_count() * 8;
     if (blocks < 1) blocks = 1;
     k_ttm<W><<<(unsigned)blocks, BLOCK, 0, s>>>(starts, nfib, nnz, rows, vals, U, ustride, ncols, Y, ystride);
     sptgb_count_launch(1);

@@ -22,6 +22,7 @@ extern "C" {
 /* ----------------------------------------------------------- context -- */
 int          sptgb_ctx(void);            /* lazy init; returns SptError code */
 cudaStream_t sptgb_stream(void);
+int          sptgb_sm_count(void);        /* SMs of the library's device */
 cudaStream_t sptgb_copy_stream(void);
 void         sptgb_count_launch(unsigned n);
 

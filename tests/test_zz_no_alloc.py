@@ -41,7 +41,26 @@ def test_no_alloc_matches_allocating_entry_point_twice():
         assert f(t.ptr(), C.byref(got), None) == 0
         ref = S.lib().SparseTensorFrobeniusNormSquared(t.ptr())
         assert got.value == pytest.approx(ref, rel=1e-12)
-        assert got.value == pytest.approx(float((vals.astype(np.float64) ** 2).sum()), rel=1e-12)
+        # FP32 squares summed in FP64, as the reference's SparseTensorFrobeniusNormSquared
+        assert got.value == pytest.approx(float((vals * vals).astype(np.float64).sum()), rel=1e-12)
+
+
+def test_no_alloc_empty_tensor_and_caller_stream():
+    """nnz = 0 gives 0.0 (the partial slots are rewritten, not left from the
+    previous call), and a caller-created stream works like the default one."""
+    import torch
+    f = _entry()
+    t, vals = _tensor(200_000, 4)
+    got = C.c_double()
+    assert f(t.ptr(), C.byref(got), None) == 0 and got.value > 0.0
+    empty, _ = _tensor(0, 5)
+    got0 = C.c_double(-1.0)
+    assert f(empty.ptr(), C.byref(got0), None) == 0
+    assert got0.value == 0.0
+    stream = torch.cuda.Stream()
+    got1 = C.c_double()
+    assert f(t.ptr(), C.byref(got1), C.c_void_p(stream.cuda_stream)) == 0
+    assert got1.value == pytest.approx(float((vals * vals).astype(np.float64).sum()), rel=1e-12)
 
 
 def test_no_alloc_rejects_more_values_than_its_scratch_holds():
