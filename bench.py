@@ -11,10 +11,11 @@ Workload (one "step" = MTTKRP of every mode, 0, 1, 2, on one GPU):
           nnz*(4N+4) + sum_m I_m*R*4 (src/sptensor/mttkrp_cuda_onekernel.cu:94-97),
           with tensor copies and factors resident in HBM (sptgbCoo*).
   e2e     the same metric through the drop-in C entry point sptCudaMTTKRP with
-          host buffers (page-locked once with sptgbPinSparseTensor /
-          sptgbPinMatrix, outside the timed region): every call copies the
-          tensor and factors to the GPU, sorts by the output mode when needed
-          and copies the result back.
+          host buffers in page-locked memory from cudaHostAlloc (a caller that
+          allocates its arrays for the GPU): every call copies the tensor and
+          factors to the GPU, sorts by the output mode when needed and copies
+          the result back; beside it the same calls on arrays page-locked with
+          cudaHostRegister (sptgbPinSparseTensor / sptgbPinMatrix).
   roofline  the segmented MTTKRP launch (output memset + k_mttkrp_rec), per
           launch duration from CUDA events on the launching stream.
   cpu_baseline  the oracle port of sptOmpMTTKRP_Reduce (all host threads) on
@@ -76,7 +77,7 @@ def parse():
     p.add_argument("--serve-cpu-sample", type=int, default=32)
     p.add_argument("--skip-serve", action="store_true")
     p.add_argument("--skip-hicoo", action="store_true")
-    p.add_argument("--skip-hostalloc", action="store_true")
+    p.add_argument("--skip-registered", action="store_true")
     p.add_argument("--skip-c1", action="store_true")
     p.add_argument("--skip-cpals", action="store_true")
     p.add_argument("--cpals-nnz", type=int, default=50_000_000)
@@ -971,50 +972,48 @@ def run_ours(args, world, rank, local):
         d2h += ndims[m] * stride * 4
     ke = max(1, args.e2e_steps)
     link_gbs = host_link_gbs()
-    # the step's inputs come from page-locked host memory: the caller's arrays
-    # are pinned once (extension call), outside the timed region
     L = S.lib()
-    pinned = L.sptgbPinSparseTensor(t.ptr()) == 0
-    pinned_mats = [m for m in mats if L.sptgbPinMatrix(ctypes.byref(m.s)) == 0]
-    for _ in range(2):   # warm-up: grows the library's device buffers outside the timed region
-        for m in range(3):
-            S.mttkrp(t, mats, m, mats_order=orders[m], entry="sptCudaMTTKRP", copy=False)
-    barrier(world)
-    e_each = []
-    e0 = time.perf_counter()
-    for _ in range(ke):
-        s0 = time.perf_counter()
-        for m in range(3):
-            S.mttkrp(t, mats, m, mats_order=orders[m], entry="sptCudaMTTKRP", copy=False)
-        e_each.append(time.perf_counter() - s0)
-    e_s = reduce_max((time.perf_counter() - e0) / ke, world)
-    if pinned:
-        L.sptgbUnpinSparseTensor(t.ptr())
-    for m in pinned_mats:
-        L.sptgbUnpinMatrix(ctypes.byref(m.s))
-    S.lib().sptClearLastError()
-    e2e = world * bytes_step / e_s / 1e9
 
-    # the same e2e steps with the caller's arrays in cudaHostAlloc memory
-    # instead of registered memory: do the occasional slow steps remain?
-    hostalloc = None
-    if world == 1 and not args.skip_hostalloc:
-        hc = HostAllocCopy(t, mats)
+    def e2e_steps(call):
+        """Two untimed steps (grow the library's device buffers), then ke
+        timed steps of the three host-buffer calls: (seconds each step, mean)."""
         for _ in range(2):
             for m in range(3):
-                hc.call(m, orders[m])
-        h_each = []
+                call(m)
+        barrier(world)
+        each = []
+        e0 = time.perf_counter()
         for _ in range(ke):
             s0 = time.perf_counter()
             for m in range(3):
-                hc.call(m, orders[m])
-            h_each.append(time.perf_counter() - s0)
-        del hc
-        hostalloc = {"value": round(bytes_step / float(np.mean(h_each)) / 1e9, 2), "unit": "GB/s",
-                     "ms_per_step": round(float(np.mean(h_each)) * 1e3, 2),
-                     "ms_median_step": round(float(np.median(h_each)) * 1e3, 2),
-                     "ms_each_step": [round(x * 1e3, 2) for x in h_each],
-                     "host_memory": "cudaHostAlloc (torch pinned allocator)"}
+                call(m)
+            each.append(time.perf_counter() - s0)
+        return each, reduce_max((time.perf_counter() - e0) / ke, world)
+
+    # headline: the caller's tensor and factors live in page-locked memory
+    # from cudaHostAlloc (torch's pinned allocator) -- a caller that allocates
+    # its arrays for the GPU; every call copies them in and the result out
+    hc = HostAllocCopy(t, mats)
+    e_each, e_s = e2e_steps(lambda m: hc.call(m, orders[m]))
+    del hc
+    e2e = world * bytes_step / e_s / 1e9
+    # the same calls on the library-allocated arrays page-locked afterwards
+    # with cudaHostRegister (sptgbPinSparseTensor / sptgbPinMatrix)
+    registered = None
+    if world == 1 and not args.skip_registered:
+        pinned = L.sptgbPinSparseTensor(t.ptr()) == 0
+        pinned_mats = [m for m in mats if L.sptgbPinMatrix(ctypes.byref(m.s)) == 0]
+        r_each, r_s = e2e_steps(lambda m: S.mttkrp(t, mats, m, mats_order=orders[m], entry="sptCudaMTTKRP",
+                                                   copy=False))
+        if pinned:
+            L.sptgbUnpinSparseTensor(t.ptr())
+        for m in pinned_mats:
+            L.sptgbUnpinMatrix(ctypes.byref(m.s))
+        S.lib().sptClearLastError()
+        registered = {"value": round(bytes_step / r_s / 1e9, 2), "unit": "GB/s", "ms_per_step": round(r_s * 1e3, 2),
+                      "ms_median_step": round(float(np.median(r_each)) * 1e3, 2),
+                      "ms_each_step": [round(x * 1e3, 2) for x in r_each],
+                      "host_memory": "cudaHostRegister" if pinned and len(pinned_mats) == len(mats) else "pageable"}
 
     hicoo = None
     if world == 1 and not args.skip_hicoo:
@@ -1054,10 +1053,10 @@ def run_ours(args, world, rank, local):
                     "entry": "sptCudaMTTKRP (host buffers)", "ms_per_step": e_s * 1e3,
                     "ms_each_step": [round(x * 1e3, 2) for x in e_each],
                     "ms_median_step": round(float(np.median(e_each)) * 1e3, 2),
-                    "host_memory": "pinned" if pinned and len(pinned_mats) == len(mats) else "pageable",
+                    "host_memory": "cudaHostAlloc (torch pinned allocator)",
                     "host_link_h2d_gbs": link_gbs,
                     "link_floor_ms": round((h2d + d2h) / (link_gbs * 1e9) * 1e3, 2) if link_gbs else None,
-                    "host_alloc_variant": hostalloc},
+                    "registered_variant": registered},
             "gpu_launches": int(n1 - n0),
             "clocks": clocks.summary(),
             "nnz_per_s": round(world * K * 3 * nnz / (ms_max / 1e3), 1),

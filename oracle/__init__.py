@@ -83,6 +83,7 @@ def orc():
         L.orc_mttkrp_f64.argtypes = mt + [f64p]
         L.orc_omp_mttkrp_f64.argtypes = mt + [f64p, C.c_int]
         L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_sort_keyed_check.argtypes = [C.c_uint32, C.c_uint64, C.POINTER(u32p), u32p, C.c_int]
         L.orc_ttm.restype = C.c_uint64
         L.orc_ttm.argtypes = [C.c_uint32, C.c_uint64, C.POINTER(u32p), f32p, C.c_uint32, f32p, C.c_uint32,
                               C.c_uint32, C.c_uint32, C.POINTER(u32p), f32p]
@@ -218,6 +219,18 @@ def sort_lex(inds, order=None):
     perm = np.zeros(n, np.uint64)
     orc().orc_sort_lex(N, n, ip, op, perm.ctypes.data_as(u64p))
     return perm.astype(np.int64)
+
+
+def sort_keyed_check(inds, order=None, sk_bits=None):
+    """True when the packed-key sort (used from 2^20 nonzeros up) and the
+    comparison merge sort give one permutation: lexicographic in `order`, or
+    the HiCOO order of kernel size 2^sk_bits when order is None."""
+    N, n = inds.shape
+    keep, ip = _rows(list(inds), u32p, np.uint32)
+    if order is not None:
+        o, op = _u32(order)
+        return orc().orc_sort_keyed_check(N, n, ip, op, 0) == 0
+    return orc().orc_sort_keyed_check(N, n, ip, None, sk_bits) == 0
 
 
 def sort_hicoo(inds, sk_bits):
@@ -670,6 +683,7 @@ class quiet_stdout:
     def __exit__(self, *exc):
         import sys
         sys.stdout.flush()
+        C.CDLL(None).fflush(None)   # the C library's buffered stdout, while fd 1 still points at stderr
         os.dup2(self._saved, 1)
         os.close(self._saved)
         return False

@@ -58,7 +58,131 @@ static int cmp_lex(const void *c, uint64_t a, uint64_t b) {
     return 0;
 }
 
+/* The same orders through packed keys, for inputs of 10^8 nonzeros: each
+ * nonzero gets a 192-bit key (w[0] most significant) whose unsigned order is
+ * the comparison order above, and (key, position) pairs are merge-sorted in
+ * parallel (ties keep input order, as msort does).  orc_sort_keyed_check
+ * (tests/test_oracle_sorts.py) checks both paths give one permutation. */
+typedef struct {
+    uint64_t w[3];
+    uint64_t i;
+} keyed;
+
+static inline int keyed_less(const keyed *a, const keyed *b) {
+    for (int k = 0; k < 3; ++k)
+        if (a->w[k] != b->w[k]) return a->w[k] < b->w[k];
+    return a->i < b->i;
+}
+
+static void keyed_merge(const keyed *a, uint64_t na, const keyed *b, uint64_t nb, keyed *out) {
+    uint64_t i = 0, j = 0, k = 0;
+    while (i < na && j < nb) out[k++] = keyed_less(&b[j], &a[i]) ? b[j++] : a[i++];
+    while (i < na) out[k++] = a[i++];
+    while (j < nb) out[k++] = b[j++];
+}
+
+static void keyed_msort_seq(keyed *a, keyed *tmp, uint64_t n) {
+    if (n < 2) return;
+    if (n <= 16) {
+        for (uint64_t i = 1; i < n; ++i) {
+            keyed x = a[i];
+            uint64_t j = i;
+            while (j > 0 && keyed_less(&x, &a[j - 1])) {
+                a[j] = a[j - 1];
+                --j;
+            }
+            a[j] = x;
+        }
+        return;
+    }
+    const uint64_t h = n / 2;
+    keyed_msort_seq(a, tmp, h);
+    keyed_msort_seq(a + h, tmp + h, n - h);
+    keyed_merge(a, h, a + h, n - h, tmp);
+    memcpy(a, tmp, n * sizeof *a);
+}
+
+/* T sorted runs (one per thread), then log2(T) rounds of pairwise merges. */
+static int keyed_sort(keyed *a, uint64_t n) {
+    keyed *tmp = (keyed *)malloc((n ? n : 1) * sizeof *tmp);
+    if (!tmp) return 1;
+    int T = omp_get_max_threads();
+    if (T < 1) T = 1;
+    if ((uint64_t)T > n / 4096 + 1) T = (int)(n / 4096 + 1);
+    uint64_t *cut = (uint64_t *)malloc((T + 1) * sizeof *cut);
+    for (int t = 0; t <= T; ++t) cut[t] = n * (uint64_t)t / (uint64_t)T;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(T)
+    for (int t = 0; t < T; ++t) keyed_msort_seq(a + cut[t], tmp + cut[t], cut[t + 1] - cut[t]);
+    keyed *src = a, *dst = tmp;
+    for (int width = 1; width < T; width *= 2) {
+#pragma omp parallel for schedule(dynamic, 1)
+        for (int t = 0; t < T; t += 2 * width) {
+            const int m = t + width < T ? t + width : T, e = t + 2 * width < T ? t + 2 * width : T;
+            keyed_merge(src + cut[t], cut[m] - cut[t], src + cut[m], cut[e] - cut[m], dst + cut[t]);
+        }
+        keyed *x = src;
+        src = dst;
+        dst = x;
+    }
+    if (src != a) memcpy(a, src, n * sizeof *a);
+    free(cut);
+    free(tmp);
+    return 0;
+}
+
+static int bits_of(uint32_t v) {
+    int b = 0;
+    while (v) {
+        ++b;
+        v >>= 1;
+    }
+    return b;
+}
+
+/* Appends the low `bits` bits of v (bits <= 32) below the `used` bits
+ * already placed in the 192-bit key w (w[0] most significant). */
+static inline void key_push(uint64_t *w, int *used, uint64_t v, int bits) {
+    if (bits == 0) return;
+    const int lo = 192 - *used - bits;   /* bit index of v's bit 0, from the least significant end */
+    const int q = 2 - lo / 64, off = lo % 64;
+    w[q] |= v << off;
+    if (off + bits > 64) w[q - 1] |= v >> (64 - off);
+    *used += bits;
+}
+
+static int orc_sort_lex_keyed(uint32_t nmodes, uint64_t nnz, const uint32_t *const *inds, const uint32_t *order,
+                              uint64_t *perm) {
+    int bits[ORC_MAX_MODES], total = 0;
+    for (uint32_t k = 0; k < nmodes; ++k) {
+        uint32_t mx = 0;
+        const uint32_t *a = inds[order[k]];
+#pragma omp parallel for reduction(max : mx)
+        for (uint64_t x = 0; x < nnz; ++x) mx = a[x] > mx ? a[x] : mx;
+        bits[k] = bits_of(mx);
+        total += bits[k];
+    }
+    if (total > 192) return -1;
+    keyed *a = (keyed *)malloc((nnz ? nnz : 1) * sizeof *a);
+    if (!a) return 1;
+#pragma omp parallel for schedule(static)
+    for (uint64_t x = 0; x < nnz; ++x) {
+        keyed e = {{0, 0, 0}, x};
+        int used = 0;
+        for (uint32_t k = 0; k < nmodes; ++k) key_push(e.w, &used, inds[order[k]][x], bits[k]);
+        a[x] = e;
+    }
+    int r = keyed_sort(a, nnz);
+#pragma omp parallel for schedule(static)
+    for (uint64_t x = 0; x < nnz; ++x) perm[x] = a[x].i;
+    free(a);
+    return r;
+}
+
 int orc_sort_lex(uint32_t nmodes, uint64_t nnz, const uint32_t *const *inds, const uint32_t *order, uint64_t *perm) {
+    if (nnz >= (1u << 20)) {
+        const int r = orc_sort_lex_keyed(nmodes, nnz, inds, order, perm);
+        if (r >= 0) return r;
+    }
     uint64_t *tmp = (uint64_t *)malloc((nnz ? nnz : 1) * sizeof *tmp);
     if (!tmp) return 1;
     for (uint64_t i = 0; i < nnz; ++i) perm[i] = i;
@@ -118,7 +242,70 @@ static int cmp_hicoo(const void *c, uint64_t a, uint64_t b) {
     return ka < kb ? -1 : (ka > kb ? 1 : 0);
 }
 
+/* HiCOO order through keys: w[0] the kernel coordinates (idx >> sk_bits,
+ * mode 0 most significant), w[1..2] the Morton key of morton3 / morton4. */
+static int orc_sort_hicoo_keyed(uint32_t nmodes, uint64_t nnz, const uint32_t *const *inds, int sk_bits,
+                                uint64_t *perm) {
+    if (nmodes != 3 && nmodes != 4) return -1;
+    int bits[ORC_MAX_MODES], total = 0;
+    for (uint32_t m = 0; m < nmodes; ++m) {
+        uint32_t mx = 0;
+        const uint32_t *a = inds[m];
+#pragma omp parallel for reduction(max : mx)
+        for (uint64_t x = 0; x < nnz; ++x) mx = a[x] > mx ? a[x] : mx;
+        bits[m] = bits_of(mx >> sk_bits);
+        total += bits[m];
+    }
+    if (total > 64) return -1;
+    keyed *a = (keyed *)malloc((nnz ? nnz : 1) * sizeof *a);
+    if (!a) return 1;
+#pragma omp parallel for schedule(static)
+    for (uint64_t x = 0; x < nnz; ++x) {
+        keyed e = {{0, 0, 0}, x};
+        uint64_t kk = 0;
+        for (uint32_t m = 0; m < nmodes; ++m) kk = (kk << bits[m]) | (uint64_t)(inds[m][x] >> sk_bits);
+        const unsigned __int128 mk = nmodes == 3 ? morton3(inds[0][x], inds[1][x], inds[2][x])
+                                                 : morton4(inds[0][x], inds[1][x], inds[2][x], inds[3][x]);
+        e.w[0] = kk;
+        e.w[1] = (uint64_t)(mk >> 64);
+        e.w[2] = (uint64_t)mk;
+        a[x] = e;
+    }
+    int r = keyed_sort(a, nnz);
+#pragma omp parallel for schedule(static)
+    for (uint64_t x = 0; x < nnz; ++x) perm[x] = a[x].i;
+    free(a);
+    return r;
+}
+
+/* Both paths on one input (test hook): 0 when they give one permutation. */
+int orc_sort_keyed_check(uint32_t nmodes, uint64_t nnz, const uint32_t *const *inds, const uint32_t *order,
+                         int sk_bits) {
+    uint64_t *p1 = (uint64_t *)malloc((nnz ? nnz : 1) * 8), *p2 = (uint64_t *)malloc((nnz ? nnz : 1) * 8);
+    uint64_t *tmp = (uint64_t *)malloc((nnz ? nnz : 1) * 8);
+    int bad = 0;
+    for (uint64_t i = 0; i < nnz; ++i) p1[i] = i;
+    if (order) {
+        sort_ctx c = {nmodes, inds, order, 0};
+        msort(p1, tmp, nnz, cmp_lex, &c);
+        bad = orc_sort_lex_keyed(nmodes, nnz, inds, order, p2) != 0;
+    } else {
+        sort_ctx c = {nmodes, inds, NULL, sk_bits};
+        msort(p1, tmp, nnz, cmp_hicoo, &c);
+        bad = orc_sort_hicoo_keyed(nmodes, nnz, inds, sk_bits, p2) != 0;
+    }
+    for (uint64_t i = 0; i < nnz && !bad; ++i) bad = p1[i] != p2[i];
+    free(p1);
+    free(p2);
+    free(tmp);
+    return bad;
+}
+
 int orc_sort_hicoo(uint32_t nmodes, uint64_t nnz, const uint32_t *const *inds, int sk_bits, uint64_t *perm) {
+    if (nnz >= (1u << 20)) {
+        const int r = orc_sort_hicoo_keyed(nmodes, nnz, inds, sk_bits, perm);
+        if (r >= 0) return r;
+    }
     uint64_t *tmp = (uint64_t *)malloc((nnz ? nnz : 1) * sizeof *tmp);
     if (!tmp) return 1;
     for (uint64_t i = 0; i < nnz; ++i) perm[i] = i;

@@ -11,6 +11,10 @@ GOLDEN = os.path.join(ROOT, "tests", "golden")
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+    # the slowest tests with their run times (the full-size configs carry
+    # their nonzero count in the test id)
+    if not config.option.durations:
+        config.option.durations = 15
 
 
 @pytest.fixture(scope="session", autouse=True)

@@ -5,8 +5,8 @@ iterations, FP32 MTTKRP with FP64 / double-float dense pieces on the GPU
 (sptgbCpdAls) against the FP64 oracle restatement of sptCpdAls (pinned to the
 reference's CpdAlsStep trace).  Tolerance: fit within 1e-4 at every iteration.
 
-The default size (2M nonzeros) runs in seconds; SPTGB_CPALS_NNZ=50000000 runs the
-full 50M-nonzero case and SPTGB_CPALS_REPORT=<file> writes fits and times as JSON.
+The default is the full 50M-nonzero case; SPTGB_CPALS_NNZ sets another size and
+SPTGB_CPALS_REPORT=<file> writes fits and times as JSON.
 """
 import json
 import os
@@ -20,12 +20,13 @@ import sptol_gb300 as S
 
 pytestmark = pytest.mark.gpu
 DIMS = [500_000, 300_000, 10_000]
-NNZ = int(float(os.environ.get("SPTGB_CPALS_NNZ", "2000000")))
+NNZ = int(float(os.environ.get("SPTGB_CPALS_NNZ", "50000000")))
 RANK, ITERS = 32, 20
 FIT_TOL = 1e-4
 
 
-def test_planted_cpd_fits_match_oracle():
+@pytest.mark.parametrize("nnz", [NNZ], ids=lambda n: "nnz%d" % n)
+def test_planted_cpd_fits_match_oracle(nnz):
     spec = S.GenSpec()
     spec.seed = 404
     spec.nmodes = 3
@@ -33,7 +34,7 @@ def test_planted_cpd_fits_match_oracle():
         spec.ndims[m] = d
         spec.coord_dist[m] = S.DIST_ZIPF
         spec.zipf_s[m] = 1.1
-    spec.count = NNZ
+    spec.count = nnz
     spec.merge_duplicates = 0
     spec.value_dist = S.VAL_PLANTED
     spec.planted_rank = 32

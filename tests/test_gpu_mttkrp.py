@@ -184,15 +184,17 @@ def test_uniform_1m_full_size_against_reference_summary_and_oracle():
         assert rel_fro(out[rows], g["rows%d" % mode]) <= TOL
 
 
-def test_power_law_against_fp64():
+POWERLAW_NNZ = int(float(__import__("os").environ.get("SPTGB_POWERLAW_NNZ", "100000000")))
+
+
+@pytest.mark.parametrize("nnz", [POWERLAW_NNZ], ids=lambda n: "nnz%d" % n)
+def test_power_law_against_fp64(nnz):
     """The 4,000,000 x 2,000,000 x 25,000 power-law tensor (Zipf(1.2) on
     modes 0 and 1, lognormal values), rank 32: ours against the FP64 oracle
     within 1e-5 for every mode, and the reference-order sequential FP32 sum
     against FP64 reported beside it (its error on the hot rows is why this
-    tensor is adjudicated against FP64).  SPTGB_POWERLAW_NNZ (default 5M) sets the
-    size; 100000000 is the full tensor."""
-    import os
-    nnz = int(float(os.environ.get("SPTGB_POWERLAW_NNZ", "5000000")))
+    tensor is adjudicated against FP64).  SPTGB_POWERLAW_NNZ sets the size
+    (default the full 100000000)."""
     dims = [4_000_000, 2_000_000, 25_000]
     spec = S.GenSpec()
     spec.seed = 20261203
@@ -300,8 +302,10 @@ def test_order4_records(n, rank, shuffled, entry):
 
 def test_pinned_host_buffers_give_the_same_result():
     """sptgbPinSparseTensor / sptgbPinMatrix: the host-buffer entry on page-
-    locked caller arrays returns the same bits as on pageable ones; pinning
-    twice and unpinning what is not pinned are errors."""
+    locked caller arrays returns the same result as on pageable ones (within
+    1e-6: a row spread over three or more work units is summed with float
+    atomics in whatever order they land); pinning twice and unpinning what is
+    not pinned are errors."""
     import ctypes as C
     rng = np.random.default_rng(5)
     ndims = [400, 300, 200]
@@ -319,7 +323,7 @@ def test_pinned_host_buffers_give_the_same_result():
     try:
         assert L.sptgbPinSparseTensor(t.ptr()) != 0          # already pinned
         for mode in range(3):
-            assert np.array_equal(S.mttkrp(t, mats, mode, entry="sptCudaMTTKRP"), plain[mode])
+            assert rel_fro(S.mttkrp(t, mats, mode, entry="sptCudaMTTKRP"), plain[mode]) <= 1e-6
     finally:
         assert L.sptgbUnpinSparseTensor(t.ptr()) == 0
         for m in mats:

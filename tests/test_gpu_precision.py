@@ -7,9 +7,8 @@ Bounds: FP32 <= 1e-5 (the parity bar); BF16 <= 1e-2 (a BF16 factor entry
 carries a relative rounding error of at most 2^-9 ~ 2e-3; products of three
 factors and sums with cancellation stay well inside 1e-2).
 
-The default size (2M nonzeros) runs in seconds; SPTGB_PRECISION_NNZ=200000000 runs the
-full 200M-nonzero study, and SPTGB_PRECISION_REPORT=<file> writes the error table as
-JSON.
+The default is the full 200M-nonzero study; SPTGB_PRECISION_NNZ sets another size,
+and SPTGB_PRECISION_REPORT=<file> writes the error table as JSON.
 """
 import json
 import os
@@ -23,7 +22,7 @@ from conftest import rel_fro
 
 pytestmark = pytest.mark.gpu
 DIMS = [10_000, 5_000, 2_000, 500]
-NNZ = int(float(os.environ.get("SPTGB_PRECISION_NNZ", "2000000")))
+NNZ = int(float(os.environ.get("SPTGB_PRECISION_NNZ", "200000000")))
 FP32_TOL = 1e-5
 BF16_TOL = 1e-2
 _results = []
@@ -49,7 +48,7 @@ def tensor():
                       indent=1)
 
 
-@pytest.mark.parametrize("rank", [16, 64])
+@pytest.mark.parametrize("rank", [16, 64], ids=lambda r: "nnz%d-rank%d" % (NNZ, r))
 def test_fp32_and_bf16_against_fp64_oracle(tensor, rank):
     torch = pytest.importorskip("torch")
     t = tensor

@@ -2,6 +2,7 @@
 own outputs (tests/golden) and against the oracle on larger inputs; HiCOO
 MTTKRP within the MTTKRP tolerance."""
 import ctypes as C
+import os
 
 import numpy as np
 import pytest
@@ -357,3 +358,66 @@ def test_dump_hicoo(tmp_path):
     exp += "values:\n" + lst("sptValueVector", "%f", [float(v) for v in A["values"]])
     assert open(path).read() == exp
     h.free()
+
+
+C2_DIMS = [4_000_000, 2_000_000, 25_000]
+C2_NNZ = int(float(os.environ.get("SPTGB_C2_NNZ", "100000000")))
+
+
+@pytest.mark.parametrize("nnz", [C2_NNZ], ids=lambda n: "nnz%d" % n)
+def test_power_law_full_size_sorts_and_hicoo_bit_exact(nnz):
+    """The 100M-nonzero power-law tensor (4,000,000 x 2,000,000 x 25,000,
+    Zipf(1.2) on modes 0 and 1, lognormal values): the device HiCOO order and
+    every HiCOO array (blocks 2^7, kernels 2^17: kptr, kschr, nkiters, cptr,
+    bptr, binds, einds, values), the lexicographic sort and each mode's
+    custom-order sort (the mode first, the others ascending) are equal bit
+    for bit to the oracle's (sort.c:410-585, hicoo/convert.c:300-497).
+    SPTGB_C2_NNZ sets the size (default the full 1e8)."""
+    import time
+    spec = S.GenSpec()
+    spec.seed = 20261203
+    spec.nmodes = 3
+    for m, d in enumerate(C2_DIMS):
+        spec.ndims[m] = d
+    spec.coord_dist[0] = spec.coord_dist[1] = S.DIST_ZIPF
+    spec.zipf_s[0] = spec.zipf_s[1] = 1.2
+    spec.count = nnz
+    spec.merge_duplicates = 0
+    spec.value_dist = S.VAL_LOGNORMAL
+    t0 = time.time()
+    g = S.Tensor.generate(spec)
+    ndims = g.ndims
+    assert g.nnz == nnz
+    # the generator emits lexicographic order: shuffle so that every sort has work to do
+    shuf = np.random.default_rng(7).permutation(g.nnz)
+    inds, vals = g.arrays()
+    g.free()
+    inds, vals = np.ascontiguousarray(inds[:, shuf]), vals[shuf]
+    del shuf
+    t = S.Tensor.from_arrays(ndims, inds, vals)
+    h = S.HiCOO(t, 7, 17)
+    i2, v2 = t.arrays()
+    p = O.sort_hicoo(inds, 17)
+    assert np.array_equal(i2, inds[:, p]) and np.array_equal(v2, vals[p])
+    del i2, v2
+    oh = O.hicoo_build(ndims, inds[:, p], 7, 17)
+    _check_hicoo(h, oh, t.nnz)
+    assert np.array_equal(h.arrays()["values"], vals[p])
+    nb = len(oh["bptr"]) - 1
+    del oh, p
+    h.free()
+    t.free()
+    for order in ([0, 1, 2], [1, 0, 2], [2, 0, 1]):
+        x = S.Tensor.from_arrays(ndims, inds, vals)
+        o = np.ascontiguousarray(order, np.uint32)
+        if order == [0, 1, 2]:
+            S.lib().sptSparseTensorSortIndex(x.ptr(), 1, 1)
+        else:
+            S.lib().sptSparseTensorSortIndexCustomOrder(x.ptr(), o.ctypes.data_as(C.POINTER(C.c_uint32)), 1, 1)
+        q = O.sort_lex(inds, order)
+        xi, xv = x.arrays()
+        assert np.array_equal(xi, inds[:, q]) and np.array_equal(xv, vals[q]), order
+        assert x.sortorder == order
+        x.free()
+    print("nnz %d  %d HiCOO blocks  bit-exact HiCOO + 3 lexicographic orders in %.1f s"
+          % (nnz, nb, time.time() - t0))
