@@ -81,6 +81,7 @@ def parse():
     p.add_argument("--skip-c1", action="store_true")
     p.add_argument("--skip-cpals", action="store_true")
     p.add_argument("--cpals-nnz", type=int, default=50_000_000)
+    p.add_argument("--skip-ref-gpu", action="store_true")
     return p.parse_args()
 
 
@@ -794,6 +795,41 @@ def cpu_leg(t, mats, reps):
             "seconds_per_step": secs, "nnz_per_s": 3 * t.nnz / secs, "atomic": atomic}
 
 
+def reference_gpu_leg(sess, reps=2):
+    """The reference's own best CUDA MTTKRP on the same tensor: sptCudaMTTKRPOneKernel
+    with impl_num 15 (mttkrp_cuda_onekernel.cu:41-427; kernel
+    spt_MTTKRPKernelRankSplitNnz3DOneKernel, mttkrp_cuda_kernels.cu:544-603,
+    one atomicAdd per nonzero and column), built for sm_103a.  Per mode one
+    warm-up call, then `reps` calls: the kernel time as the reference prints
+    it (CPU timer around the launch and the synchronisation) and the time of
+    the whole call (uploads of the tensor and factors, cudaMalloc/cudaFree,
+    the kernel and the copy back, all from pageable memory)."""
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            return None
+    except Exception:
+        return None
+    kern, call = [], []
+    for m in range(3):
+        if sess.cuda_mttkrp(m) is None:
+            return None
+        ks, cs = [], []
+        for _ in range(reps):
+            c, k = sess.cuda_mttkrp(m)
+            cs.append(c)
+            if k is not None:
+                ks.append(k)
+        kern.append(float(np.median(ks)) if ks else None)
+        call.append(float(np.median(cs)))
+    ab = algo_bytes(sess.ndims, sess.nnz, RANK)
+    return {"function": "sptCudaMTTKRPOneKernel impl 15 (spt_MTTKRPKernelRankSplitNnz3DOneKernel), sm_103a",
+            "kernel_ms_by_mode": [round(k * 1e3, 3) if k is not None else None for k in kern],
+            "kernel_gbs": round(3 * ab / sum(kern) / 1e9, 1) if all(k for k in kern) else None,
+            "call_ms_by_mode": [round(c * 1e3, 2) for c in call],
+            "call_gbs": round(3 * ab / sum(call) / 1e9, 2), "reps": reps}
+
+
 def run_reference(args, world, rank):
     """--impl reference: the reference's own sptOmpMTTKRP_Reduce
     (mttkrp_omp.c:401-563) with every host thread on the full workload tensor,
@@ -842,6 +878,7 @@ def run_reference(args, world, rank):
         step()
     secs = (time.perf_counter() - t0) / K
     gbs = 3 * algo_bytes(DIMS, nnz, RANK) / secs / 1e9
+    ref_gpu = reference_gpu_leg(sess) if kind == "reference" and not args.skip_ref_gpu else None
     sample = ("the full %d-nnz workload tensor, 3 modes per step, sptOmpMTTKRP_Reduce with %d threads, "
               "%d timed steps after %d warm-up steps" % (nnz, threads, K, W))
     line = {
@@ -855,6 +892,7 @@ def run_reference(args, world, rank):
         "setup_s": {"generate": round(gen_s, 2)},
         "tensor_source": ("library generator linked into the reference build (reference containers)"
                           if kind == "reference" else "libParTI.so generator (reference not built)"),
+        "reference_gpu": ref_gpu,
     }
     print(json.dumps(line), flush=True)
 

@@ -174,6 +174,8 @@ def ref():
         L.ref_session_ndims.argtypes = [C.c_void_p, u32p]
         L.ref_session_mttkrp.restype = C.c_double
         L.ref_session_mttkrp.argtypes = [C.c_void_p, C.c_int, C.c_uint32, f32p]
+        L.ref_session_cuda_mttkrp.restype = C.c_double
+        L.ref_session_cuda_mttkrp.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, f32p]
         L.ref_session_cpd.restype = C.c_double
         L.ref_session_cpd.argtypes = [C.c_void_p, C.c_uint32, C.c_int, f32p, f64p]
         L.ref_omp_cpd.restype = C.c_double
@@ -689,6 +691,30 @@ class quiet_stdout:
         return False
 
 
+class capture_stdout:
+    """Collects what the C library writes to stdout during a call (the
+    reference prints its own phase timings) into .text."""
+
+    def __enter__(self):
+        import sys
+        import tempfile
+        sys.stdout.flush()
+        self._f = tempfile.TemporaryFile(mode="w+b")
+        self._saved = os.dup(1)
+        os.dup2(self._f.fileno(), 1)
+        self.text = ""
+        return self
+
+    def __exit__(self, *exc):
+        C.CDLL(None).fflush(None)
+        os.dup2(self._saved, 1)
+        os.close(self._saved)
+        self._f.seek(0)
+        self.text = self._f.read().decode(errors="replace")
+        self._f.close()
+        return False
+
+
 class RefSession:
     """The reference's own CPU MTTKRP / CP-ALS on a tensor held in the
     reference's containers (ref_harness.c, ref_session_*): the tensor is made
@@ -719,6 +745,21 @@ class RefSession:
         if t < 0:
             raise RuntimeError("reference MTTKRP failed")
         return t
+
+    def cuda_mttkrp(self, mode, impl=15, out=None):
+        """The reference's sptCudaMTTKRPOneKernel: (call seconds, kernel
+        seconds as the reference itself prints them), or None when the
+        reference was built without CUDA."""
+        p = out.ctypes.data_as(f32p) if out is not None else None
+        with capture_stdout() as cap:
+            t = ref().ref_session_cuda_mttkrp(self.h, mode, impl, p)
+        if t == -2.0:
+            return None
+        if t < 0:
+            raise RuntimeError("reference sptCudaMTTKRPOneKernel failed:\n" + cap.text[-2000:])
+        import re
+        m = re.search(r"^\[CUDA SpTns MTTKRP\]: ([0-9.eE+-]+) s$", cap.text, re.M)
+        return t, (float(m.group(1)) if m else None)
 
     def cpd(self, niters, use_reduce=1):
         """OmpCpdAlsStep from the session's factors: (seconds, corrected fit, lambda)."""

@@ -535,6 +535,32 @@ double ref_session_mttkrp(ref_session *s, int which, uint32_t mode, float *out) 
     return r ? -1.0 : dt;
 }
 
+/* The reference's own CUDA MTTKRP, sptCudaMTTKRPOneKernel with impl_num =
+ * impl (mttkrp_cuda_onekernel.cu:41-427; 15 is its rank-split kernel,
+ * spt_MTTKRPKernelRankSplitNnz3DOneKernel, mttkrp_cuda_kernels.cu:544-603):
+ * every call copies the tensor and factors to the GPU, runs one kernel with
+ * one atomicAdd per (nonzero, column) and copies the result back; it prints
+ * its own phase times ("[CUDA SpTns MTTKRP]: <s> s" is the kernel).  Returns
+ * the seconds of the whole call, negative when it fails or when the library
+ * was built without CUDA. */
+double ref_session_cuda_mttkrp(ref_session *s, uint32_t mode, uint32_t impl, float *out) {
+#ifdef REF_HAVE_CUDA
+    const uint32_t N = s->X.nmodes;
+    sptIndex order[8];
+    order[0] = mode;
+    for (uint32_t i = 1; i < N; ++i) order[i] = (mode + i) % N;
+    s->U[N]->nrows = s->X.ndims[mode];
+    const double t0 = now_s();
+    const int r = sptCudaMTTKRPOneKernel(&s->X, s->U, order, mode, impl);
+    const double dt = now_s() - t0;
+    if (out) memcpy(out, s->U[N]->values, (size_t)s->X.ndims[mode] * s->U[N]->stride * sizeof(float));
+    return r ? -1.0 : dt;
+#else
+    (void)s, (void)mode, (void)impl, (void)out;
+    return -2.0;
+#endif
+}
+
 /* The reference's sptOmpCpdAls loop, OmpCpdAlsStep (cpd_omp.c:32-157), run
  * from the session's factors as the initial guess (cpd_omp.c:166-228 only
  * adds sptRandomizeMatrix initialisation and the allocations); the factors
