@@ -414,6 +414,23 @@ def serve_leg(args):
         diffs.append(max(float(np.abs(served["fits"][i] - plain["fits"][i]).max()),
                          float(np.abs(batched["fits"][i] - plain["fits"][i]).max())))
     dfit = max(diffs) if diffs else None
+    # the requests left out: the reference's own CP-ALS loop (CpdAlsStep's
+    # steps through its exported pieces, corrected fit per iteration) from
+    # the same initial factors, judged by the same rule
+    ref_div = {}
+    try:
+        import oracle as O
+        if O.ref_loadable():
+            for i in div:
+                r = reqs[i]
+                init = [m.array()[:d, : r["rank"]].copy() for m, d in zip(request_init(r), r["dims"])]
+                inds, vals = tensors[i].arrays()
+                with O.quiet_stdout():
+                    tr = O.ref_cpd_trace(r["dims"], inds, vals, r["rank"], SERVE_ITERS, init)
+                ref_div[i] = {"reference_fits": [float(x) for x in tr["fits"]],
+                              "reference_diverges": bool(diverged(np.asarray(tr["fits"])))}
+    except Exception as e:   # informational only
+        ref_div = {"error": str(e)[:200]}
 
     def pct(a, q):
         return round(float(np.percentile(a, q)) * 1e3, 2)
@@ -444,8 +461,10 @@ def serve_leg(args):
         "batched_over_plain": round(batched["solves_per_s"] / plain["solves_per_s"], 2),
         "fit_match": {"compared": sample, "well_posed": len(diffs), "max_diff_vs_plain": dfit, "tolerance": 1e-4,
                       "within_tolerance": int(sum(d <= 1e-4 for d in diffs)),
-                      "diverged": [{"request": i, "dims": reqs[i]["dims"], "nnz": int(tensors[i].nnz),
-                                    "rank": reqs[i]["rank"]} for i in div]},
+                      "diverged": [dict({"request": i, "dims": reqs[i]["dims"], "nnz": int(tensors[i].nnz),
+                                         "rank": reqs[i]["rank"], "plain_fits": [float(x) for x in plain["fits"][i]]},
+                                        **(ref_div.get(i, {}) if isinstance(ref_div, dict) else {}))
+                                   for i in div]},
         "generate_s": round(gen_s, 1),
     }
 
