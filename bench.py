@@ -269,9 +269,10 @@ def run_served(reqs, tensors, inits, outs, poisson, keep_fits):
     span = time.monotonic() - t0 - (reqs[0]["arrival"] if poisson else 0.0)
     launches = S.launch_count() - n0
     units = {g: srv.unit_length(g) for g in range(4)}
+    persistent = srv.persistent()
     srv.free()
     return {"solves_per_s": n / span, "makespan_s": span, "lat": lat, "fits": fits, "steps": steps,
-            "launches": int(launches), "unit_lengths": units,
+            "launches": int(launches), "unit_lengths": units, "persistent": persistent,
             "host_s": {"submit": round(t_sub, 3), "step": round(t_step, 3), "poll": round(t_poll, 3)}}
 
 
@@ -389,6 +390,13 @@ def serve_leg(args):
     run_served(warm, wt, [request_init(r) for r in warm], [[S.Matrix(d, r["rank"]) for d in r["dims"]] for r in warm],
                poisson=False, keep_fits=0)
     batched = run_served(reqs, tensors, inits, outs, poisson=False, keep_fits=sample)
+    # the same batched run with each ALS step as one persistent cooperative
+    # kernel instead of the kernel sequence (SPTGB_STEP=persistent)
+    os.environ["SPTGB_STEP"] = "persistent"
+    try:
+        pers = run_served(reqs, tensors, inits, outs, poisson=False, keep_fits=sample)
+    finally:
+        os.environ.pop("SPTGB_STEP", None)
     served = run_served(reqs, tensors, inits, outs, poisson=True, keep_fits=sample)
     # the same arrivals as the plain run: the stream's first `sample`
     # requests, so that served and plain latencies cover one population
@@ -414,6 +422,7 @@ def serve_leg(args):
         diffs.append(max(float(np.abs(served["fits"][i] - plain["fits"][i]).max()),
                          float(np.abs(batched["fits"][i] - plain["fits"][i]).max())))
     dfit = max(diffs) if diffs else None
+    pdiff = [float(np.abs(pers["fits"][i] - batched["fits"][i]).max()) for i in range(sample) if i not in div]
     # the requests left out: the reference's own CP-ALS loop (CpdAlsStep's
     # steps through its exported pieces, corrected fit per iteration) from
     # the same initial factors, judged by the same rule
@@ -442,10 +451,17 @@ def serve_leg(args):
         "served": {"solves_per_s": round(served["solves_per_s"], 1), "p50_ms": pct(served["lat"], 50),
                    "p99_ms": pct(served["lat"], 99), "makespan_s": round(served["makespan_s"], 3),
                    "steps": served["steps"], "gpu_launches": served["launches"],
-                   "unit_lengths": served["unit_lengths"], "host_s": served["host_s"]},
+                   "unit_lengths": served["unit_lengths"], "persistent_step": served["persistent"],
+                   "host_s": served["host_s"]},
         "batched": {"solves_per_s": round(batched["solves_per_s"], 1), "p50_ms": pct(batched["lat"], 50),
                     "p99_ms": pct(batched["lat"], 99), "makespan_s": round(batched["makespan_s"], 3),
-                    "steps": batched["steps"], "gpu_launches": batched["launches"], "host_s": batched["host_s"]},
+                    "steps": batched["steps"], "gpu_launches": batched["launches"],
+                    "persistent_step": batched["persistent"], "host_s": batched["host_s"]},
+        "batched_persistent_step": {
+            "solves_per_s": round(pers["solves_per_s"], 1), "makespan_s": round(pers["makespan_s"], 3),
+            "steps": pers["steps"], "gpu_launches": pers["launches"], "persistent_step": pers["persistent"],
+            "max_fit_diff_vs_batched": max(pdiff) if pdiff else None,
+            "what": "the batched run with each ALS step as one persistent cooperative kernel"},
         "plain": {"solves_per_s": round(plain["solves_per_s"], 1), "p50_ms": pct(plain["lat"], 50),
                   "p99_ms": pct(plain["lat"], 99), "makespan_s": round(plain["makespan_s"], 3),
                   "sample": "first %d requests of the same stream at their arrival times, one at a time "

@@ -163,6 +163,17 @@ int  sptgbServerDrain(sptgbServer *s);
 size_t sptgbServerBytesInUse(const sptgbServer *s);
 /* Unit length (nonzeros) the autotuner chose for rank group g (W = 2<<g). */
 uint32_t sptgbServerUnitLength(const sptgbServer *s, int group);
+/* 1 when each step runs as one persistent cooperative kernel (opt-in with
+ * SPTGB_STEP=persistent when the device and the capture allow cooperative
+ * launches), 0 when it runs as the kernel sequence (the default); meaningful
+ * after the first step. */
+int sptgbServerPersistent(const sptgbServer *s);
+/* Diagnostic of the persistent step's bounded grid barrier: a 4-block
+ * cooperative kernel passes two barrier rounds and, with missing != 0, a third
+ * that waits for a fifth block; every wait there gives up after 2^14 polls, so
+ * the kernel returns with *err = 1 instead of hanging.  *rounds counts the
+ * rounds completed, summed over blocks (8 in both cases). */
+int sptgbGridBarrierSelfTest(int missing, int *err, unsigned int *rounds);
 void sptgbServerFree(sptgbServer *s);
 
 /* ------------------------------------------------ without device allocation --

@@ -233,6 +233,8 @@ def _declare(L):
         "sptgbServerCompleted": (C.c_uint32, [C.c_void_p, u64p, C.c_uint32]),
         "sptgbServerBytesInUse": (C.c_size_t, [C.c_void_p]),
         "sptgbServerUnitLength": (C.c_uint32, [C.c_void_p, C.c_int]),
+        "sptgbServerPersistent": (C.c_int, [C.c_void_p]),
+        "sptgbGridBarrierSelfTest": (C.c_int, [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_uint)]),
         "sptgbServerFree": (None, [C.c_void_p]),
     }
     for name, (res, args) in sig.items():
@@ -631,6 +633,10 @@ class Server:
 
     def unit_length(self, group):
         return int(lib().sptgbServerUnitLength(self.h, group))
+
+    def persistent(self):
+        """True when each step runs as one persistent cooperative kernel."""
+        return bool(lib().sptgbServerPersistent(self.h))
 
     def free(self):
         if self.h:

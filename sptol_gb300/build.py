@@ -33,6 +33,7 @@ def _cuda_home():
 
 def _headers():
     hs = glob.glob(os.path.join(CSRC, "**", "*.h"), recursive=True)
+    hs += glob.glob(os.path.join(CSRC, "**", "*.cuh"), recursive=True)
     hs += glob.glob(os.path.join(ROOT, "include", "*.h"))
     return hs
 

@@ -9,6 +9,16 @@
 #include <math.h>
 #include "../sptgb_internal.h"
 
+// Pointer qualifier of the bodies' operands.  A unit whose kernels only read
+// data written by earlier launches keeps __restrict__ (const operands may then
+// take the read-only load path); the persistent batched step (batch_step.cu),
+// whose phases read what earlier phases of the same launch wrote, defines it
+// empty before including this file.  Each .cu is its own device module (no
+// relocatable device code), so the two forms never meet.
+#ifndef SPTGB_RESTRICT
+#define SPTGB_RESTRICT __restrict__
+#endif
+
 namespace sptgb_dense {
 
 
@@ -31,7 +41,7 @@ __device__ __forceinline__ void pair_of(int idx, int rank, int *p, int *q) {
 }
 
 // Per-block partial of A^T A over a grid-stride set of row tiles.
-__device__ __forceinline__ void gram_partial_body(const float *__restrict__ A, uint32_t nrows, int rank, int stride, double *__restrict__ part, unsigned bid, unsigned nbk) {
+__device__ __forceinline__ void gram_partial_body(const float *SPTGB_RESTRICT A, uint32_t nrows, int rank, int stride, double *SPTGB_RESTRICT part, unsigned bid, unsigned nbk) {
     __shared__ double tile[TR][RMAX + 1];
     __shared__ unsigned char pp_s[PMAX], qq_s[PMAX];
     const int P = rank * (rank + 1) / 2;
@@ -73,7 +83,7 @@ __device__ __forceinline__ void gram_partial_body(const float *__restrict__ A, u
 
 // Sums the per-block pair partials (fixed order) into a full symmetric
 // rank x rank matrix G (row-major, leading dimension rank).
-__device__ __forceinline__ void gram_reduce_body(const double *__restrict__ part, int nblk, int rank, double *__restrict__ G) {
+__device__ __forceinline__ void gram_reduce_body(const double *SPTGB_RESTRICT part, int nblk, int rank, double *SPTGB_RESTRICT G) {
     const int P = rank * (rank + 1) / 2;
     for (int i = threadIdx.x; i < P; i += blockDim.x) {
         double s = 0.0;
@@ -115,8 +125,8 @@ __device__ __forceinline__ void split_inverse(double *S, int RR) {
     }
 }
 
-__device__ __forceinline__ void solve_prepare_body(GramPtrs grams, int nmodes, int mode, int rank, double *__restrict__ S,
-                int *__restrict__ status) {
+__device__ __forceinline__ void solve_prepare_body(GramPtrs grams, int nmodes, int mode, int rank, double *SPTGB_RESTRICT S,
+                int *SPTGB_RESTRICT status) {
     extern __shared__ double sm[];
     double *H = sm;                       // [rank][rank+1]
     double *L = sm + RMAX * (RMAX + 1);   // [rank][rank+1]
@@ -355,9 +365,9 @@ constexpr int LDR = TR + 2;     // row length of the transposed X tile
 // r0 + j * rstep, j < NOUT; the k sum runs over pairs (k, k+1) in the two
 // lanes, which are added at the end.
 template <int NOUT>
-__device__ __forceinline__ void solve_tile_cols(const float *__restrict__ Mt, const float *__restrict__ StH,
-                                                const float *__restrict__ StN, const float *__restrict__ StL,
-                                                float *__restrict__ XT, float *__restrict__ XN, float *__restrict__ X,
+__device__ __forceinline__ void solve_tile_cols(const float *SPTGB_RESTRICT Mt, const float *SPTGB_RESTRICT StH,
+                                                const float *SPTGB_RESTRICT StN, const float *SPTGB_RESTRICT StL,
+                                                float *SPTGB_RESTRICT XT, float *SPTGB_RESTRICT XN, float *SPTGB_RESTRICT X,
                                                 uint64_t t0, uint32_t nrows, int rank2, int stride, int c0, int r0,
                                                 int rstep) {
     float2 hi[NOUT], lo[NOUT];
@@ -391,8 +401,8 @@ __device__ __forceinline__ void solve_tile_cols(const float *__restrict__ Mt, co
 // X^T X (over the FP32 values written) and the column maxima.  Each output
 // element and each Gram entry is accumulated in double-float (packed FP32x2)
 // and rounded once: outputs to FP32, Gram partials to FP64.
-__device__ __forceinline__ void solve_rows_body(const float *__restrict__ M, float *__restrict__ X, uint32_t nrows, int rank, int stride,
-             const double *__restrict__ S, double *__restrict__ gpart, double *__restrict__ mpart, unsigned bid, unsigned nbk) {
+__device__ __forceinline__ void solve_rows_body(const float *SPTGB_RESTRICT M, float *SPTGB_RESTRICT X, uint32_t nrows, int rank, int stride,
+             const double *SPTGB_RESTRICT S, double *SPTGB_RESTRICT gpart, double *SPTGB_RESTRICT mpart, unsigned bid, unsigned nbk) {
     extern __shared__ float smf[];
     float *StH = smf;                       // [RMAX][LDK]: S^T hi, k-major per column
     float *StN = StH + RMAX * LDK;          // -hi
@@ -500,9 +510,9 @@ __device__ __forceinline__ void solve_rows_body(const float *__restrict__ M, flo
 }
 
 // Reduces the solve statistics, forms lambda and the normalised Gram.
-__device__ __forceinline__ void lambda_body(const double *__restrict__ gpart, const double *__restrict__ mpart, int nblk, int rank,
-                         int use_2norm, double *__restrict__ G, float *__restrict__ lambda_f32,
-                         double *__restrict__ colmax_out) {
+__device__ __forceinline__ void lambda_body(const double *SPTGB_RESTRICT gpart, const double *SPTGB_RESTRICT mpart, int nblk, int rank,
+                         int use_2norm, double *SPTGB_RESTRICT G, float *SPTGB_RESTRICT lambda_f32,
+                         double *SPTGB_RESTRICT colmax_out) {
     __shared__ double lam[RMAX];
     const int P = rank * (rank + 1) / 2;
     for (int i = threadIdx.x; i < P; i += blockDim.x) {
@@ -551,8 +561,8 @@ __device__ __forceinline__ void lambda_body(const double *__restrict__ gpart, co
 // X[i, j] /= lambda[j] for j < rank (padding columns untouched), one float4
 // of a row per thread: rows are stride floats, so float4 e of the matrix is
 // row e / (stride/4), columns 4 * (e % (stride/4)) + 0..3.
-__device__ __forceinline__ void scale_cols_body(float *__restrict__ X, uint32_t nrows, int rank, int stride,
-                             const float *__restrict__ lambda, unsigned bid, unsigned nbk) {
+__device__ __forceinline__ void scale_cols_body(float *SPTGB_RESTRICT X, uint32_t nrows, int rank, int stride,
+                             const float *SPTGB_RESTRICT lambda, unsigned bid, unsigned nbk) {
     const uint32_t c4n = (uint32_t)stride / 4;
     const uint64_t total = (uint64_t)nrows * c4n;
     float4 *X4 = reinterpret_cast<float4 *>(X);
@@ -570,8 +580,8 @@ __device__ __forceinline__ void scale_cols_body(float *__restrict__ X, uint32_t 
 }
 
 // Per-block partials of sum_i A[i,r] * M[i,r].
-__device__ __forceinline__ void inner_partial_body(const float *__restrict__ A, const float *__restrict__ M, uint32_t nrows, int rank, int stride,
-                double *__restrict__ part, unsigned bid, unsigned nbk) {
+__device__ __forceinline__ void inner_partial_body(const float *SPTGB_RESTRICT A, const float *SPTGB_RESTRICT M, uint32_t nrows, int rank, int stride,
+                double *SPTGB_RESTRICT part, unsigned bid, unsigned nbk) {
     __shared__ double red[DT];
     // thread handles column c = tid % rank for rows strided by DT / rank
     const int per = DT / rank;
@@ -591,8 +601,8 @@ __device__ __forceinline__ void inner_partial_body(const float *__restrict__ A, 
     }
 }
 
-__device__ __forceinline__ void fit_final_body(const double *__restrict__ part, int nblk, int rank, const float *__restrict__ lambda,
-                            GramPtrs gp, int nmodes, const double *__restrict__ normX2, double *__restrict__ fit) {
+__device__ __forceinline__ void fit_final_body(const double *SPTGB_RESTRICT part, int nblk, int rank, const float *SPTGB_RESTRICT lambda,
+                            GramPtrs gp, int nmodes, const double *SPTGB_RESTRICT normX2, double *SPTGB_RESTRICT fit) {
     __shared__ double red[DT];
     __shared__ double inner_s;
     double inner = 0.0;
@@ -629,7 +639,7 @@ __device__ __forceinline__ void fit_final_body(const double *__restrict__ part, 
     }
 }
 
-__device__ __forceinline__ void sumsq_partial_body(const float *__restrict__ v, uint64_t n, double *part, unsigned bid, unsigned nbk) {
+__device__ __forceinline__ void sumsq_partial_body(const float *SPTGB_RESTRICT v, uint64_t n, double *part, unsigned bid, unsigned nbk) {
     __shared__ double red[DT];
     double s = 0.0;
     // vals[n] * vals[n] rounded in FP32 and summed in FP64, as the reference's
@@ -656,7 +666,7 @@ __device__ __forceinline__ void sum_final_body(const double *part, int nblk, dou
 }
 
 // Column sums of squares (FP64) per block.
-__device__ __forceinline__ void colsq_partial_body(const float *__restrict__ A, uint32_t nrows, int rank, int stride, double *__restrict__ part, unsigned bid, unsigned nbk) {
+__device__ __forceinline__ void colsq_partial_body(const float *SPTGB_RESTRICT A, uint32_t nrows, int rank, int stride, double *SPTGB_RESTRICT part, unsigned bid, unsigned nbk) {
     __shared__ double red[DT];
     const int per = DT / rank;
     const int c = threadIdx.x % rank;
@@ -686,7 +696,7 @@ __device__ __forceinline__ void colnorm_final_body(const double *part, int nblk,
     }
 }
 
-__device__ __forceinline__ void f32_to_bf16_body(const float *__restrict__ in, uint16_t *__restrict__ out, uint64_t n, unsigned bid, unsigned nbk) {
+__device__ __forceinline__ void f32_to_bf16_body(const float *SPTGB_RESTRICT in, uint16_t *SPTGB_RESTRICT out, uint64_t n, unsigned bid, unsigned nbk) {
     for (uint64_t i = bid * (uint64_t)blockDim.x + threadIdx.x; i < n;
          i += (uint64_t)nbk * blockDim.x) {
         // round to nearest even

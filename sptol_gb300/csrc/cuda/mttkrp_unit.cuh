@@ -33,8 +33,12 @@ __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
     return *reinterpret_cast<float2 *>(&rd);
 }
 
-template <bool BF16>
+// COH: the rows may have been written earlier in the same kernel (the
+// persistent batched step), so they are read through the coherent path
+// instead of the read-only one.
+template <bool BF16, bool COH = false>
 __device__ __forceinline__ float4 gather_row(const char *base, uint32_t row, uint32_t row_bytes) {
+    if (!BF16 && COH) return __ldca(reinterpret_cast<const float4 *>(base + (size_t)row * row_bytes));
     if (!BF16) return __ldg(reinterpret_cast<const float4 *>(base + (size_t)row * row_bytes));
     const uint2 u = __ldg(reinterpret_cast<const uint2 *>(base + (size_t)row * row_bytes));
     return make_float4(__uint_as_float(u.x << 16), __uint_as_float(u.x & 0xffff0000u), __uint_as_float(u.y << 16),
@@ -50,7 +54,7 @@ __device__ __forceinline__ void put_row(float *out, uint32_t row, uint32_t strid
 }
 
 // F[i]: factor base already offset by this lane's columns (bytes).
-template <bool BF16, bool FULL, int NF, int BATCH = 4>
+template <bool BF16, bool FULL, int NF, int BATCH = 4, bool COH = false>
 __device__ __forceinline__ void unit(const uint4 *__restrict__ rec, const float *__restrict__ vals,
                                      const char *const *F, uint32_t row_bytes, float *__restrict__ out, uint64_t nnz,
                                      uint64_t start, uint32_t len, uint32_t stride, uint32_t rank, int sl) {
@@ -74,9 +78,9 @@ __device__ __forceinline__ void unit(const uint4 *__restrict__ rec, const float 
         put_row(out, cur, stride, sl, v, shared);
     };
     auto gather = [&](const uint4 &q, float4 *f) {
-        f[0] = col_ok ? gather_row<BF16>(F[0], q.y, row_bytes) : make_float4(0.f, 0.f, 0.f, 0.f);
-        f[1] = col_ok ? gather_row<BF16>(F[1], q.z, row_bytes) : make_float4(0.f, 0.f, 0.f, 0.f);
-        if (NF == 3) f[2] = col_ok ? gather_row<BF16>(F[2], q.w, row_bytes) : make_float4(0.f, 0.f, 0.f, 0.f);
+        f[0] = col_ok ? gather_row<BF16, COH>(F[0], q.y, row_bytes) : make_float4(0.f, 0.f, 0.f, 0.f);
+        f[1] = col_ok ? gather_row<BF16, COH>(F[1], q.z, row_bytes) : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (NF == 3) f[2] = col_ok ? gather_row<BF16, COH>(F[2], q.w, row_bytes) : make_float4(0.f, 0.f, 0.f, 0.f);
     };
     auto consume = [&](const uint4 &q, float v, const float4 *f) {
         if (q.x != cur) {

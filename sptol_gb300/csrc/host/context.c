@@ -139,6 +139,7 @@ cudaStream_t sptgb_stream(void) { return g_stream; }
 cudaStream_t sptgb_copy_stream(void) { return g_copy_stream; }
 
 void sptgb_count_launch(unsigned n) { atomic_fetch_add(&g_launches, (uint64_t)n); }
+void sptgb_uncount_launch(uint64_t n) { atomic_fetch_sub(&g_launches, n); }
 
 int sptgb_dbuf_reserve(sptgb_dbuf *b, size_t bytes) {
     if (bytes <= b->cap && b->ptr) return 0;

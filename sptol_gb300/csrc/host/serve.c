@@ -87,6 +87,9 @@ struct sptgbServer {
     cudaStream_t as;             /* admission: uploads, checks, sorts of new slots, overlapping the step on cs */
     cudaGraphExec_t gexec;
     int have_graph;
+    int persistent;              /* the step graph holds one persistent kernel (1) or the kernel sequence (0) */
+    uint32_t graph_kernels;      /* kernels in the step graph */
+    sptgb_grid_bar *bar;         /* its grid barrier (device) */
     int changed;
     uint32_t nactive;
     /* admission group */
@@ -536,6 +539,11 @@ static int retire(sptgbServer *s, uint32_t R) {
             SPTGB_CUDA(cudaMemcpyAsync(j->fits, d->fits, (size_t)j->niters * 8, cudaMemcpyDeviceToHost, s->cs), module);
     }
     SPTGB_CUDA(cudaStreamSynchronize(s->cs), module);
+    if (s->persistent) {
+        sptgb_grid_bar hb;   /* a grid barrier of the persistent step whose bounded wait ran out */
+        SPTGB_CUDA(cudaMemcpy(&hb, s->bar, sizeof hb, cudaMemcpyDeviceToHost), module);
+        if (hb.err) SPTGB_CUDA(cudaErrorLaunchTimeout, module);
+    }
     const double t = now_s();
     for (uint32_t r = 0; r < R; ++r) {
         job_t *j = &s->jobs[s->slot_job[s->ret[r]]];
@@ -608,17 +616,41 @@ static int capture(sptgbServer *s) {
     for (int g = 0; g < 4; ++g) s->L.ul[g] = s->ul[g];
     s->L.fit = wl(s, NL_FIT);
     s->L.fit_one = wl(s, NL_FITONE);
-    cudaGraph_t graph;
-    SPTGB_CUDA(cudaStreamBeginCapture(s->cs, cudaStreamCaptureModeThreadLocal), module);
-    const cudaError_t e = sptgb_batch_step(s->ds, &s->L, s->cs);
-    const cudaError_t e2 = cudaStreamEndCapture(s->cs, &graph);
-    SPTGB_CUDA(e, module);
-    SPTGB_CUDA(e2, module);
-    const cudaError_t e3 = cudaGraphInstantiate(&s->gexec, graph, 0);
-    cudaGraphDestroy(graph);
-    SPTGB_CUDA(e3, module);
-    s->have_graph = 1;
-    return 0;
+    /* One ALS iteration of every admitted job: by default the sequence of
+     * kernels (one per phase and lane group); SPTGB_STEP=persistent captures
+     * one persistent cooperative kernel (sptgb_batch_step_persistent) as the
+     * graph's only node instead, and falls back to the sequence on a device
+     * without cooperative launch or a capture that refuses the node.  The
+     * sequence is the default because it is faster on GB300: its MTTKRP
+     * kernels run with the whole L1 (the fused kernel carries the solve's
+     * shared memory in every phase) and admission kernels overlap it. */
+    const char *mode = getenv("SPTGB_STEP");
+    int persistent = mode && mode[0] == 'p';
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        cudaGraph_t graph = NULL;
+        SPTGB_CUDA(cudaStreamBeginCapture(s->cs, cudaStreamCaptureModeThreadLocal), module);
+        const uint64_t c0 = sptgbLaunchCount();
+        const cudaError_t e = persistent ? sptgb_batch_step_persistent(s->ds, &s->L, s->bar, s->cs)
+                                         : sptgb_batch_step(s->ds, &s->L, s->cs);
+        const uint64_t nk = sptgbLaunchCount() - c0;
+        sptgb_uncount_launch(nk);
+        const cudaError_t e2 = cudaStreamEndCapture(s->cs, &graph);
+        cudaError_t e3 = cudaErrorUnknown;
+        if (e == cudaSuccess && e2 == cudaSuccess) e3 = cudaGraphInstantiate(&s->gexec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (e == cudaSuccess && e2 == cudaSuccess && e3 == cudaSuccess) {
+            s->have_graph = 1;
+            s->persistent = persistent;
+            s->graph_kernels = (uint32_t)nk;
+            return 0;
+        }
+        cudaGetLastError();
+        if (!persistent) {
+            SPTGB_CUDA(e != cudaSuccess ? e : (e2 != cudaSuccess ? e2 : e3), module);
+        }
+        persistent = 0;   /* retry with the kernel sequence */
+    }
+    return SPTERR_CUDA_ERROR;
 }
 
 /* ------------------------------------------------------------- API -- */
@@ -633,6 +665,8 @@ int sptgbServerCreate(sptgbServer **out, size_t hbm_budget_bytes, uint32_t max_s
     int r = 0;
     cudaError_t e = cudaMalloc((void **)&s->arena, s->budget);
     if (e == cudaSuccess) e = cudaMalloc((void **)&s->ds, (size_t)s->cap * sizeof(sptgb_slot));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&s->bar, sizeof(sptgb_grid_bar));
+    if (e == cudaSuccess) e = cudaMemset(s->bar, 0, sizeof(sptgb_grid_bar));
     if (e == cudaSuccess) e = cudaMalloc((void **)&s->d_counts, NLISTS * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMalloc((void **)&s->d_ids, (size_t)NLISTS * s->cap * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMalloc((void **)&s->d_pre, (size_t)NLISTS * (s->cap + 1) * sizeof(uint64_t));
@@ -740,6 +774,7 @@ int sptgbServerStep(sptgbServer *s, uint32_t *active, uint32_t *queued) {
         if (!s->have_graph) SPTGB_CHECK(capture(s), module);
         if (s->trace) t0 = now_s();
         SPTGB_CUDA(cudaGraphLaunch(s->gexec, s->cs), module);
+        sptgb_count_launch(s->graph_kernels);
         if (s->trace) {
             SPTGB_CUDA(cudaStreamSynchronize(s->cs), module);
             s->t_step += now_s() - t0;
@@ -834,6 +869,14 @@ int sptgbServerDrain(sptgbServer *s) {
 size_t sptgbServerBytesInUse(const sptgbServer *s) { return s->used; }
 
 uint32_t sptgbServerUnitLength(const sptgbServer *s, int group) { return group >= 0 && group < 4 ? s->ul[group] : 0; }
+int sptgbServerPersistent(const sptgbServer *s) { return s->persistent; }
+
+int sptgbGridBarrierSelfTest(int missing, int *err, unsigned int *rounds) {
+    const char *module = "GPU barrier self-test";
+    SPTGB_CHECK(sptgb_ctx(), module);
+    SPTGB_CUDA(sptgb_grid_barrier_selftest(missing, err, rounds), module);
+    return 0;
+}
 
 void sptgbServerFree(sptgbServer *s) {
     if (!s) return;
@@ -847,6 +890,7 @@ void sptgbServerFree(sptgbServer *s) {
     if (s->have_graph) cudaGraphExecDestroy(s->gexec);
     if (s->arena) cudaFree(s->arena);
     if (s->ds) cudaFree(s->ds);
+    if (s->bar) cudaFree(s->bar);
     if (s->d_counts) cudaFree(s->d_counts);
     if (s->d_ids) cudaFree(s->d_ids);
     if (s->d_pre) cudaFree(s->d_pre);

@@ -25,6 +25,9 @@ cudaStream_t sptgb_stream(void);
 int          sptgb_sm_count(void);        /* SMs of the library's device */
 cudaStream_t sptgb_copy_stream(void);
 void         sptgb_count_launch(unsigned n);
+/* Kernels enqueued while a stream is captured run only when the graph is
+ * launched: the capture takes its count back, each graph launch adds it. */
+void         sptgb_uncount_launch(uint64_t n);
 
 /* Records the error in the thread-local last-error slot and prints it like
  * the reference's spt_ComplainError (src/error/error.c:33-60). */
@@ -304,6 +307,18 @@ typedef struct {
     sptgb_wlist zr[4], one[4], dn[4], fit, fit_one;
 } sptgb_step_lists;
 cudaError_t sptgb_batch_step(const sptgb_slot *slots, const sptgb_step_lists *L, cudaStream_t s);
+/* The same ALS iteration as ONE cooperative launch of a persistent kernel,
+ * its phases separated by a grid barrier on *bar (zeroed once, device
+ * memory; err set when a bounded barrier wait ran out).  cudaErrorNotSupported
+ * when the device cannot launch cooperatively. */
+typedef struct { unsigned int count, gen; int err, pad; } sptgb_grid_bar;
+cudaError_t sptgb_batch_step_persistent(const sptgb_slot *slots, const sptgb_step_lists *L, sptgb_grid_bar *bar,
+                                        cudaStream_t s);
+/* The grid barrier of the persistent step on a 4-block grid: every round
+ * completes (missing = 0) or the last round waits for one block too many and
+ * every wait gives up (missing = 1); *err = the barrier's error word after the
+ * launch, *rounds = rounds completed summed over blocks. */
+cudaError_t sptgb_grid_barrier_selftest(int missing, int *err, unsigned int *rounds);
 /* The MTTKRP launch of mode m, lane group g alone (for timing). */
 cudaError_t sptgb_batch_mttkrp(const sptgb_slot *slots, const sptgb_wlist *w, int mode, int group, uint32_t ul,
                                cudaStream_t s);

@@ -8,8 +8,14 @@
   summation order at unit boundaries, which depends on the autotuned unit
   length, and the order of the boundary atomics);
 - admission never exceeds the HBM budget, queued jobs start when space frees,
-  and a job larger than the whole budget fails alone.
+  and a job larger than the whole budget fails alone;
+- the persistent cooperative step (SPTGB_STEP=persistent, one launch per
+  step) gives the default kernel sequence's results on the same jobs.
 """
+import ctypes as C
+import os
+import time
+
 import numpy as np
 import pytest
 
@@ -86,6 +92,56 @@ def test_batched_jobs_match_plain_path():
     assert srv.bytes_in_use() == 0
     for g in range(4):
         assert srv.unit_length(g) in (64, 128, 256, 512)
+    assert not srv.persistent()
+
+
+def _run_mix(step_kind, niters=5):
+    old = os.environ.get("SPTGB_STEP")
+    if step_kind:
+        os.environ["SPTGB_STEP"] = step_kind
+    else:
+        os.environ.pop("SPTGB_STEP", None)
+    try:
+        tensors = [make_tensor(500 + i, d, n) for i, (d, n, r) in enumerate(JOBS)]
+        inits = [init_for(d, r, 600 + i) for i, (d, n, r) in enumerate(JOBS)]
+        srv = S.Server(4 << 30, 64)
+        n0 = S.launch_count()
+        tickets = [srv.submit(t, r, niters + (i % 3), ini)
+                   for i, (t, (d, n, r), ini) in enumerate(zip(tensors, JOBS, inits))]
+        steps = 0
+        while True:
+            a, q = srv.step()
+            if a == 0 and q == 0:
+                break
+            steps += 1
+        out = [srv.result(k) for k in tickets]
+        launches = S.launch_count() - n0
+        kind = srv.persistent()
+        srv.free()
+        return out, kind, launches, steps
+    finally:
+        if old is None:
+            os.environ.pop("SPTGB_STEP", None)
+        else:
+            os.environ["SPTGB_STEP"] = old
+
+
+def test_persistent_step_matches_kernel_sequence():
+    """Same jobs, same initial factors, staggered iteration counts: the
+    one-launch persistent step and the ~38-launch kernel sequence agree to
+    the FP32 atomic-order tolerance, and the persistent step launches far
+    fewer kernels."""
+    pers, kind_p, launches_p, steps_p = _run_mix("persistent")
+    seq, kind_s, launches_s, steps_s = _run_mix(None)
+    assert kind_p and not kind_s
+    for (f1, l1, fit1), (f2, l2, fit2), (d, n, r) in zip(pers, seq, JOBS):
+        assert fit1.shape == fit2.shape
+        assert np.abs(fit1 - fit2).max() <= MIX_FIT_TOL, (d, r, fit1, fit2)
+        for a, b in zip(f1, f2):
+            assert rel_fro(a, b) <= MIX_FAC_TOL, (d, r)
+        assert rel_fro(l1, l2) <= MIX_FAC_TOL
+    assert steps_p == steps_s
+    assert launches_s - launches_p >= 20 * steps_p
 
 
 def test_same_result_alone_and_in_mix():
@@ -182,3 +238,23 @@ def test_single_slot_server_serialises():
         facs, lam, fits = srv.result(k)
         pf, plam, pfits, it = S.cpd_als(t, r, niters, 0.0, ini)
         assert np.abs(fits - pfits).max() <= FIT_TOL
+
+
+def test_grid_barrier_wait_is_bounded():
+    """The persistent step's grid barrier: complete rounds pass with no error;
+    a round that waits for a block the grid does not have gives up after its
+    bounded wait with the error word set, the kernel returns, and the context
+    stays usable."""
+    L = S.lib()
+    err, rounds = C.c_int(-1), C.c_uint(0)
+    assert L.sptgbGridBarrierSelfTest(0, C.byref(err), C.byref(rounds)) == 0
+    assert err.value == 0 and rounds.value == 8
+    t0 = time.monotonic()
+    assert L.sptgbGridBarrierSelfTest(1, C.byref(err), C.byref(rounds)) == 0
+    assert err.value == 1 and rounds.value == 8
+    assert time.monotonic() - t0 < 30.0
+    t = make_tensor(9, [50, 40, 30], 2000)
+    srv = S.Server(1 << 28, 2)
+    k = srv.submit(t, 8, 2, init_for([50, 40, 30], 8, 10))
+    srv.drain()
+    assert np.all(np.isfinite(srv.result(k)[2]))
