@@ -168,6 +168,14 @@ uint32_t sptgbServerUnitLength(const sptgbServer *s, int group);
  * launches), 0 when it runs as the kernel sequence (the default); meaningful
  * after the first step. */
 int sptgbServerPersistent(const sptgbServer *s);
+/* The MTTKRP schedule the autotuner chose for rank group `group` (0..3: rank
+ * <= 8, 16, 32, 64): unit length in nonzeros, deep (1) or shallow (0) record
+ * batches, blocks per SM the kernel's registers are sized for (2 or 3; the
+ * persistent step always runs 2), and *from_cache = 1 when the choice came
+ * from an earlier server of this process, 0 when it was timed, -1 when the
+ * group had no jobs at tuning time.  Meaningful after the first step. */
+int sptgbServerSchedule(const sptgbServer *s, int group, uint32_t *unit_len, uint32_t *deep, uint32_t *blocks_per_sm,
+                        int *from_cache);
 /* Diagnostic of the persistent step's bounded grid barrier: a 4-block
  * cooperative kernel passes two barrier rounds and, with missing != 0, a third
  * that waits for a fifth block; every wait there gives up after 2^14 polls, so

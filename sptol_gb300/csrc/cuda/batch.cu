@@ -35,10 +35,12 @@ using namespace sptgb_batch;
 
 // The step's kernels: each phase as its own launch ...
 __global__ void k_b_zero(const sptgb_slot *__restrict__ slots, sptgb_wlist w, int mode) { ph_zero(slots, w, mode); }
-template <int W>
-__global__ void __launch_bounds__(BT, 2) k_b_mttkrp(const sptgb_slot *__restrict__ slots, sptgb_wlist w, int mode,
-                                                   uint32_t ul) {
-    ph_mttkrp<W, false>(slots, w, mode, ul);
+// MINB: resident blocks per SM the registers are sized for (2: 128
+// registers a thread, 3: 80).
+template <int W, bool DEEP, int MINB>
+__global__ void __launch_bounds__(BT, MINB) k_b_mttkrp(const sptgb_slot *__restrict__ slots, sptgb_wlist w, int mode,
+                                                      uint32_t ul) {
+    ph_mttkrp<W, false, DEEP>(slots, w, mode, ul);
 }
 __global__ void __launch_bounds__(DT) k_b_prepare(const sptgb_slot *__restrict__ slots, sptgb_wlist w, int mode) {
     ph_prepare(slots, w, mode);
@@ -208,7 +210,21 @@ unsigned grid_for(uint64_t n, unsigned cap) {
 }
 
 int g_nsm = 0;
-int g_mt_blocks[4];
+int g_mt_blocks[4][2][2];   // [group][deep][occupancy 2 / 3]: grid of each MTTKRP kernel
+
+template <int W, bool DEEP, int MINB>
+void size_mttkrp(int g) {
+    int per = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_b_mttkrp<W, DEEP, MINB>, BT, 0);
+    g_mt_blocks[g][DEEP][MINB - 2] = (per < 1 ? 1 : per) * g_nsm;
+}
+template <int W>
+void size_group(int g) {
+    size_mttkrp<W, false, 2>(g);
+    size_mttkrp<W, true, 2>(g);
+    size_mttkrp<W, false, 3>(g);
+    size_mttkrp<W, true, 3>(g);
+}
 
 int nsm() {
     if (!g_nsm) {
@@ -217,26 +233,33 @@ int nsm() {
         cudaDeviceGetAttribute(&g_nsm, cudaDevAttrMultiProcessorCount, dev);
         cudaFuncSetAttribute(k_b_prepare, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PREP_SMEM);
         cudaFuncSetAttribute(k_b_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SOLVE_SMEM);
-        int per = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_b_mttkrp<2>, BT, 0);
-        g_mt_blocks[0] = (per < 1 ? 1 : per) * g_nsm;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_b_mttkrp<4>, BT, 0);
-        g_mt_blocks[1] = (per < 1 ? 1 : per) * g_nsm;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_b_mttkrp<8>, BT, 0);
-        g_mt_blocks[2] = (per < 1 ? 1 : per) * g_nsm;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_b_mttkrp<16>, BT, 0);
-        g_mt_blocks[3] = (per < 1 ? 1 : per) * g_nsm;
+        size_group<2>(0);
+        size_group<4>(1);
+        size_group<8>(2);
+        size_group<16>(3);
     }
     return g_nsm;
 }
 
+template <int W>
+void launch_group(const sptgb_slot *slots, const sptgb_wlist &w, int mode, int g, uint32_t ul, uint32_t sched,
+                  cudaStream_t s) {
+    const bool deep = sched & 1u, occ3 = sched & 2u;
+    const int blocks = g_mt_blocks[g][deep][occ3];
+    if (deep && occ3) k_b_mttkrp<W, true, 3><<<blocks, BT, 0, s>>>(slots, w, mode, ul);
+    else if (deep) k_b_mttkrp<W, true, 2><<<blocks, BT, 0, s>>>(slots, w, mode, ul);
+    else if (occ3) k_b_mttkrp<W, false, 3><<<blocks, BT, 0, s>>>(slots, w, mode, ul);
+    else k_b_mttkrp<W, false, 2><<<blocks, BT, 0, s>>>(slots, w, mode, ul);
+}
+
+// sched bit 0: deep record batches, bit 1: the 3-blocks-per-SM build
 cudaError_t mttkrp_group(const sptgb_slot *slots, const sptgb_wlist &w, int mode, int group, uint32_t ul,
-                         cudaStream_t s) {
+                         uint32_t sched, cudaStream_t s) {
     switch (group) {
-        case 0: k_b_mttkrp<2><<<g_mt_blocks[0], BT, 0, s>>>(slots, w, mode, ul); break;
-        case 1: k_b_mttkrp<4><<<g_mt_blocks[1], BT, 0, s>>>(slots, w, mode, ul); break;
-        case 2: k_b_mttkrp<8><<<g_mt_blocks[2], BT, 0, s>>>(slots, w, mode, ul); break;
-        default: k_b_mttkrp<16><<<g_mt_blocks[3], BT, 0, s>>>(slots, w, mode, ul); break;
+        case 0: launch_group<2>(slots, w, mode, 0, ul, sched, s); break;
+        case 1: launch_group<4>(slots, w, mode, 1, ul, sched, s); break;
+        case 2: launch_group<8>(slots, w, mode, 2, ul, sched, s); break;
+        default: launch_group<16>(slots, w, mode, 3, ul, sched, s); break;
     }
     sptgb_count_launch(1);
     return cudaGetLastError();
@@ -250,9 +273,9 @@ extern "C" uint32_t sptgb_batch_zero_rows(void) { return ZERO_ROWS; }
 extern "C" uint32_t sptgb_batch_max_blocks(void) { return NBLK; }
 
 extern "C" cudaError_t sptgb_batch_mttkrp(const sptgb_slot *slots, const sptgb_wlist *w, int mode, int group,
-                                          uint32_t ul, cudaStream_t s) {
+                                          uint32_t ul, uint32_t sched, cudaStream_t s) {
     nsm();
-    return mttkrp_group(slots, *w, mode, group, ul, s);
+    return mttkrp_group(slots, *w, mode, group, ul, sched, s);
 }
 
 extern "C" cudaError_t sptgb_batch_step(const sptgb_slot *slots, const sptgb_step_lists *L, cudaStream_t s) {
@@ -261,7 +284,7 @@ extern "C" cudaError_t sptgb_batch_step(const sptgb_slot *slots, const sptgb_ste
         k_b_zero<<<n * 8, BT, 0, s>>>(slots, L->zr[m], m);
         sptgb_count_launch(1);
         for (int g = 0; g < 4; ++g) {
-            cudaError_t e = mttkrp_group(slots, L->mt[m][g], m, g, L->ul[g], s);
+            cudaError_t e = mttkrp_group(slots, L->mt[m][g], m, g, L->ul[g], L->sched[g], s);
             if (e != cudaSuccess) return e;
         }
         k_b_prepare<<<n * 2, DT, PREP_SMEM, s>>>(slots, L->one[m], m);

@@ -48,7 +48,9 @@ __device__ __forceinline__ void ph_zero(const sptgb_slot *__restrict__ slots, co
     }
 }
 
-template <int W, bool COH>
+// DEEP: records software-pipelined in batches of 4 (order 3) / 2 (order 4),
+// else 2 / 1; the batch depth changes the loads in flight, not the arithmetic.
+template <int W, bool COH, bool DEEP>
 __device__ __forceinline__ void ph_mttkrp(const sptgb_slot *__restrict__ slots, const sptgb_wlist &w, int mode,
                                           uint32_t ul) {
     const uint32_t cnt = *w.count;
@@ -71,17 +73,17 @@ __device__ __forceinline__ void ph_mttkrp(const sptgb_slot *__restrict__ slots, 
         const uint32_t rb = s.stride * 4;
         if (s.nmodes == 3) {
             if (s.stride == 4u * W)
-                sptgb_mttkrp::unit<false, true, 2, 4, COH>(rec, nullptr, F, rb, s.M, s.nnz, start, len, s.stride, s.rank,
+                sptgb_mttkrp::unit<false, true, 2, DEEP ? 4 : 2, COH>(rec, nullptr, F, rb, s.M, s.nnz, start, len, s.stride, s.rank,
                                                           sl);
             else
-                sptgb_mttkrp::unit<false, false, 2, 4, COH>(rec, nullptr, F, rb, s.M, s.nnz, start, len, s.stride, s.rank,
+                sptgb_mttkrp::unit<false, false, 2, DEEP ? 4 : 2, COH>(rec, nullptr, F, rb, s.M, s.nnz, start, len, s.stride, s.rank,
                                                            sl);
         } else {
             if (s.stride == 4u * W)
-                sptgb_mttkrp::unit<false, true, 3, 2, COH>(rec, s.val4[mode], F, rb, s.M, s.nnz, start, len, s.stride,
+                sptgb_mttkrp::unit<false, true, 3, DEEP ? 2 : 1, COH>(rec, s.val4[mode], F, rb, s.M, s.nnz, start, len, s.stride,
                                                         s.rank, sl);
             else
-                sptgb_mttkrp::unit<false, false, 3, 2, COH>(rec, s.val4[mode], F, rb, s.M, s.nnz, start, len, s.stride,
+                sptgb_mttkrp::unit<false, false, 3, DEEP ? 2 : 1, COH>(rec, s.val4[mode], F, rb, s.M, s.nnz, start, len, s.stride,
                                                          s.rank, sl);
         }
     }
@@ -108,8 +110,8 @@ __device__ __forceinline__ void ph_solve(const sptgb_slot *__restrict__ slots, c
         const uint32_t b = (uint32_t)(g - w.pre[e]);
         const uint32_t nb = (uint32_t)(w.pre[e + 1] - w.pre[e]);
         const size_t P = (size_t)s.rank * (s.rank + 1) / 2;
-        solve_rows_body(s.M, s.fac[mode], s.ndims[mode], (int)s.rank, (int)s.stride, s.S, s.ws, s.ws + NBLK * P, b,
-                        nb);
+        solve_rows_body(s.M, s.fac[mode], s.ndims[mode], (int)s.rank, (int)s.stride, s.S, s.status + mode, s.ws,
+                        s.ws + NBLK * P, b, nb);
         __syncthreads();
     }
 }

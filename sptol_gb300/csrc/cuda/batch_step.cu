@@ -82,9 +82,15 @@ __device__ __forceinline__ bool grid_sync(sptgb_grid_bar *bar, uint32_t arrivals
 // The phases as separate functions: each gets its own register allocation
 // instead of the union of all of them.
 __device__ __noinline__ void pz(const sptgb_slot *sl, const sptgb_wlist w, int m) { ph_zero(sl, w, m); }
-template <int W>
+template <int W, bool DEEP>
 __device__ __noinline__ void pm(const sptgb_slot *sl, const sptgb_wlist w, int m, uint32_t ul) {
-    ph_mttkrp<W, true>(sl, w, m, ul);
+    ph_mttkrp<W, true, DEEP>(sl, w, m, ul);
+}
+template <int W>
+__device__ __forceinline__ void pm_sched(const sptgb_slot *sl, const sptgb_wlist &w, int m, uint32_t ul,
+                                         uint32_t sched) {
+    if (sched & 1u) pm<W, true>(sl, w, m, ul);
+    else pm<W, false>(sl, w, m, ul);
 }
 __device__ __noinline__ void pp(const sptgb_slot *sl, const sptgb_wlist w, int m) { ph_prepare(sl, w, m); }
 __device__ __noinline__ void ps(const sptgb_slot *sl, const sptgb_wlist w, int m) { ph_solve(sl, w, m); }
@@ -103,10 +109,10 @@ __global__ void __launch_bounds__(BT, 2) k_b_step(const sptgb_slot *__restrict__
     for (int m = 0; m < 4; ++m) {
         pz(slots, L.zr[m], m);
         if (!grid_sync(bar)) return;
-        pm<2>(slots, L.mt[m][0], m, L.ul[0]);
-        pm<4>(slots, L.mt[m][1], m, L.ul[1]);
-        pm<8>(slots, L.mt[m][2], m, L.ul[2]);
-        pm<16>(slots, L.mt[m][3], m, L.ul[3]);
+        pm_sched<2>(slots, L.mt[m][0], m, L.ul[0], L.sched[0]);
+        pm_sched<4>(slots, L.mt[m][1], m, L.ul[1], L.sched[1]);
+        pm_sched<8>(slots, L.mt[m][2], m, L.ul[2], L.sched[2]);
+        pm_sched<16>(slots, L.mt[m][3], m, L.ul[3], L.sched[3]);
         if (!grid_sync(bar)) return;
         pp(slots, L.one[m], m);
         if (!grid_sync(bar)) return;

@@ -28,7 +28,7 @@ __global__ void k_gram_reduce(const double *__restrict__ part, int nblk, int ran
 __global__ void __launch_bounds__(DT) k_solve_prepare(GramPtrs grams, int nmodes, int mode, int rank, double *__restrict__ S,
                 int *__restrict__ status) { solve_prepare_body(grams, nmodes, mode, rank, S, status); }
 __global__ void __launch_bounds__(DT, 2) k_solve_rows(const float *__restrict__ M, float *__restrict__ X, uint32_t nrows, int rank, int stride,
-             const double *__restrict__ S, double *__restrict__ gpart, double *__restrict__ mpart) { solve_rows_body(M, X, nrows, rank, stride, S, gpart, mpart, blockIdx.x, gridDim.x); }
+             const double *__restrict__ S, const int *__restrict__ sstatus, double *__restrict__ gpart, double *__restrict__ mpart) { solve_rows_body(M, X, nrows, rank, stride, S, sstatus, gpart, mpart, blockIdx.x, gridDim.x); }
 __global__ void k_lambda(const double *__restrict__ gpart, const double *__restrict__ mpart, int nblk, int rank,
                          int use_2norm, double *__restrict__ G, float *__restrict__ lambda_f32,
                          double *__restrict__ colmax_out) { lambda_body(gpart, mpart, nblk, rank, use_2norm, G, lambda_f32, colmax_out); }
@@ -78,7 +78,7 @@ extern "C" cudaError_t sptgb_solve_prepare(const double *const *grams, int nmode
 }
 
 extern "C" cudaError_t sptgb_solve_rows(const float *M, float *X, uint32_t nrows, int rank, int stride,
-                                        const double *Hinv, double *ws, cudaStream_t s) {
+                                        const double *Hinv, const int *status, double *ws, cudaStream_t s) {
     if (rank < 1 || rank > RMAX) return cudaErrorInvalidValue;
     static int configured = 0;
     if (!configured) {
@@ -87,7 +87,7 @@ extern "C" cudaError_t sptgb_solve_rows(const float *M, float *X, uint32_t nrows
     }
     const int nb = nblocks_for_rows(nrows);
     const size_t P = (size_t)rank * (rank + 1) / 2;
-    k_solve_rows<<<nb, DT, SOLVE_SMEM, s>>>(M, X, nrows, rank, stride, Hinv, ws, ws + NBLK * P);
+    k_solve_rows<<<nb, DT, SOLVE_SMEM, s>>>(M, X, nrows, rank, stride, Hinv, status, ws, ws + NBLK * P);
     sptgb_count_launch(1);
     return cudaGetLastError();
 }

@@ -125,6 +125,39 @@ __device__ __forceinline__ void split_inverse(double *S, int RR) {
     }
 }
 
+// Status word of a prepared solve: bits 0-7 the factorisation (0 Cholesky,
+// 1 LU, 2 LU with a zero pivot), bits 8 and up the exponent e >= 0 of the
+// power of two the inverse was divided by.  An ill-conditioned H has an
+// inverse far larger than its rows' solutions; the FP32 words of the
+// double-float solve (and the FP32 products of the new Gram) would overflow
+// on it, so an inverse whose largest entry exceeds 2^32 is scaled by 2^-e
+// (exact) and the solve scales its results back by 2^e in the precision each
+// is kept in.
+constexpr double INV_SCALE_ABOVE = 4294967296.0;   // 2^32
+__device__ __forceinline__ int inverse_exponent(int status) { return status >> 8; }
+
+__device__ __forceinline__ void finish_inverse(double *S, int RR, int *status, int kind) {
+    __shared__ double red[DT / 32];
+    __shared__ int e_s;
+    __syncthreads();
+    double m = 0.0;
+    for (int i = threadIdx.x; i < RR; i += DT) m = fmax(m, fabs(S[i]));
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < DT / 32; ++w) t = fmax(t, red[w]);
+        e_s = (t > INV_SCALE_ABOVE && t <= 1.7e308) ? ilogb(t) : 0;
+        *status = kind | (e_s << 8);
+    }
+    __syncthreads();
+    const int e = e_s;
+    if (e)
+        for (int i = threadIdx.x; i < RR; i += DT) S[i] = ldexp(S[i], -e);
+    split_inverse(S, RR);
+}
+
 __device__ __forceinline__ void solve_prepare_body(GramPtrs grams, int nmodes, int mode, int rank, double *SPTGB_RESTRICT S,
                 int *SPTGB_RESTRICT status) {
     extern __shared__ double sm[];
@@ -187,8 +220,7 @@ __device__ __forceinline__ void solve_prepare_body(GramPtrs grams, int nmodes, i
             for (int k = k0; k < rank; ++k) s += H[k * ld + p] * H[k * ld + q];
             S[e] = s;
         }
-        if (tid == 0) *status = 0;
-        split_inverse(S, RR);
+        finish_inverse(S, RR, status, 0);
         return;
     }
 
@@ -253,8 +285,7 @@ __device__ __forceinline__ void solve_prepare_body(GramPtrs grams, int nmodes, i
         }
         for (int i = 0; i < rank; ++i) S[j * rank + i] = x[i];
     }
-    if (tid == 0) *status = singular ? 2 : 1;
-    split_inverse(S, RR);
+    finish_inverse(S, RR, status, singular ? 2 : 1);
 }
 
 // X[i, :] = M[i, :] * S (S = (H^{-1})^T, so row i of X solves H x = m_i).
@@ -369,7 +400,7 @@ __device__ __forceinline__ void solve_tile_cols(const float *SPTGB_RESTRICT Mt, 
                                                 const float *SPTGB_RESTRICT StN, const float *SPTGB_RESTRICT StL,
                                                 float *SPTGB_RESTRICT XT, float *SPTGB_RESTRICT XN, float *SPTGB_RESTRICT X,
                                                 uint64_t t0, uint32_t nrows, int rank2, int stride, int c0, int r0,
-                                                int rstep) {
+                                                int rstep, int sexp) {
     float2 hi[NOUT], lo[NOUT];
 #pragma unroll
     for (int j = 0; j < NOUT; ++j) hi[j] = lo[j] = make_float2(0.f, 0.f);
@@ -390,9 +421,9 @@ __device__ __forceinline__ void solve_tile_cols(const float *SPTGB_RESTRICT Mt, 
         const int r = r0 + j * rstep;
         const uint64_t row = t0 + r;
         const float xf = row < nrows ? __fadd_rn(h, l) : 0.f;
-        XT[c0 * LDR + r] = xf;
+        XT[c0 * LDR + r] = xf;   // the Gram and the column maxima use the scaled values
         XN[c0 * LDR + r] = -xf;
-        if (row < nrows) X[row * stride + c0] = xf;
+        if (row < nrows) X[row * stride + c0] = sexp ? scalbnf(xf, sexp) : xf;
     }
 }
 
@@ -402,7 +433,9 @@ __device__ __forceinline__ void solve_tile_cols(const float *SPTGB_RESTRICT Mt, 
 // element and each Gram entry is accumulated in double-float (packed FP32x2)
 // and rounded once: outputs to FP32, Gram partials to FP64.
 __device__ __forceinline__ void solve_rows_body(const float *SPTGB_RESTRICT M, float *SPTGB_RESTRICT X, uint32_t nrows, int rank, int stride,
-             const double *SPTGB_RESTRICT S, double *SPTGB_RESTRICT gpart, double *SPTGB_RESTRICT mpart, unsigned bid, unsigned nbk) {
+             const double *SPTGB_RESTRICT S, const int *SPTGB_RESTRICT sstatus, double *SPTGB_RESTRICT gpart,
+             double *SPTGB_RESTRICT mpart, unsigned bid, unsigned nbk) {
+    const int sexp = inverse_exponent(*sstatus);
     extern __shared__ float smf[];
     float *StH = smf;                       // [RMAX][LDK]: S^T hi, k-major per column
     float *StN = StH + RMAX * LDK;          // -hi
@@ -468,15 +501,16 @@ __device__ __forceinline__ void solve_rows_body(const float *SPTGB_RESTRICT M, f
         if (fixed_col) {
             if (r0 < TR) {
                 switch (nout) {
-                    case 8: solve_tile_cols<8>(Mt, StH, StN, StL, XT, XN, X, t0, nrows, rank2, stride, c0, r0, rstep); break;
-                    case 4: solve_tile_cols<4>(Mt, StH, StN, StL, XT, XN, X, t0, nrows, rank2, stride, c0, r0, rstep); break;
-                    case 2: solve_tile_cols<2>(Mt, StH, StN, StL, XT, XN, X, t0, nrows, rank2, stride, c0, r0, rstep); break;
-                    default: solve_tile_cols<1>(Mt, StH, StN, StL, XT, XN, X, t0, nrows, rank2, stride, c0, r0, rstep); break;
+                    case 8: solve_tile_cols<8>(Mt, StH, StN, StL, XT, XN, X, t0, nrows, rank2, stride, c0, r0, rstep, sexp); break;
+                    case 4: solve_tile_cols<4>(Mt, StH, StN, StL, XT, XN, X, t0, nrows, rank2, stride, c0, r0, rstep, sexp); break;
+                    case 2: solve_tile_cols<2>(Mt, StH, StN, StL, XT, XN, X, t0, nrows, rank2, stride, c0, r0, rstep, sexp); break;
+                    default: solve_tile_cols<1>(Mt, StH, StN, StL, XT, XN, X, t0, nrows, rank2, stride, c0, r0, rstep, sexp); break;
                 }
             }
         } else {
             for (int e = threadIdx.x; e < TR * rank; e += DT)
-                solve_tile_cols<1>(Mt, StH, StN, StL, XT, XN, X, t0, nrows, rank2, stride, e % rank, e / rank, 0);
+                solve_tile_cols<1>(Mt, StH, StN, StL, XT, XN, X, t0, nrows, rank2, stride, e % rank, e / rank, 0,
+                                   sexp);
         }
         __syncthreads();
         // Gram partial: this thread's pairs over row pairs (r, r+1)
@@ -503,10 +537,10 @@ __device__ __forceinline__ void solve_rows_body(const float *SPTGB_RESTRICT M, f
         if (i < P) {
             float h, l;
             df2::fold(ghi[k], glo[k], h, l);
-            gpart[(uint64_t)bid * P + i] = (double)h + (double)l;
+            gpart[(uint64_t)bid * P + i] = ldexp((double)h + (double)l, 2 * sexp);
         }
     }
-    if (threadIdx.x < rank) mpart[(uint64_t)bid * rank + threadIdx.x] = (double)cmax;
+    if (threadIdx.x < rank) mpart[(uint64_t)bid * rank + threadIdx.x] = ldexp((double)cmax, sexp);
 }
 
 // Reduces the solve statistics, forms lambda and the normalised Gram.

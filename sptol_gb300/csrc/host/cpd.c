@@ -119,7 +119,7 @@ static int cpd_run(int N, const sptIndex *ndims, const float *vals, uint64_t nnz
             r = mttkrp(ctx, (sptIndex)m, order, (const float *const *)b.fac, rank, (sptIndex)stride, b.M, s);
             if (r) goto done;
             CUDA_OR_FAIL(sptgb_solve_prepare(gptr, N, m, (int)rank, b.S, b.status + m, s));
-            CUDA_OR_FAIL(sptgb_solve_rows(b.M, b.fac[m], ndims[m], (int)rank, stride, b.S, b.ws, s));
+            CUDA_OR_FAIL(sptgb_solve_rows(b.M, b.fac[m], ndims[m], (int)rank, stride, b.S, b.status + m, b.ws, s));
             CUDA_OR_FAIL(sptgb_normalize(b.fac[m], ndims[m], (int)rank, stride, b.gram[m], it == 0 ? 1 : 0,
                                          b.lambda, b.ws, s));
         }
@@ -133,7 +133,7 @@ static int cpd_run(int N, const sptIndex *ndims, const float *vals, uint64_t nnz
         done_iters = it + 1;
         if (!sptgb_quiet()) {
             for (int m = 0; m < N; ++m)
-                if (hstatus[m]) printf("Gram matrix is not SPD. Trying `gesv`.\n");
+                if (hstatus[m] & 0xff) printf("Gram matrix is not SPD. Trying `gesv`.\n");
             printf("  its = %u ( %.3lf s ) fit = %0.5f  delta = %+0.4e\n", it + 1, now_s() - t0, fit, fit - oldfit);
         }
         if (it > 0 && fabs(fit - oldfit) < tol) break;

@@ -153,7 +153,7 @@ int sptMatrixSolveNormals(sptIndex const mode, sptIndex const nmodes, sptMatrix 
         if (nrows) {
             CK(cudaMemcpyAsync(dM, rhs->values, (size_t)nrows * stride * sizeof(float), cudaMemcpyHostToDevice, s));
             CK(cudaMemcpyAsync(dX, dM, (size_t)nrows * stride * sizeof(float), cudaMemcpyDeviceToDevice, s));
-            CK(sptgb_solve_rows(dM, dX, nrows, (int)rank, (int)stride, Hinv, ws, s));
+            CK(sptgb_solve_rows(dM, dX, nrows, (int)rank, (int)stride, Hinv, status, ws, s));
             CK(cudaMemcpyAsync(rhs->values, dX, (size_t)nrows * stride * sizeof(float), cudaMemcpyDeviceToHost, s));
         }
         CK(cudaStreamSynchronize(s));

@@ -21,9 +21,14 @@
  * in the slot's status words), so membership changes never touch a running
  * job's state.
  *
- * The first capture times the MTTKRP of each rank group with unit lengths of
- * 64..512 nonzeros on the admitted jobs and keeps the fastest (the autotuner);
- * the chosen lengths are fixed in the captured graph.
+ * The first time a rank group has admitted jobs, before their first
+ * iteration, the autotuner picks the group's MTTKRP schedule: unit length
+ * (64..512 nonzeros), record batch depth and the register budget (2 or 3
+ * blocks per SM), timed on the admitted jobs of the group; the
+ * choice is cached per process by (rank group, dominant order, nonzeros per
+ * job rounded to a power of two), so a later server with jobs of the same
+ * kind reuses it without timing.  The schedules are launch parameters of the
+ * captured graph, which is captured again when a group gets its schedule.
  *
  * Staging buffers of an admission group (coordinates, values, sort keys and
  * permutations, about 40 bytes per nonzero) are outside the budget; a group
@@ -31,6 +36,7 @@
  */
 #define _GNU_SOURCE
 #include <math.h>
+#include <pthread.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -82,7 +88,8 @@ struct sptgbServer {
     uint64_t *d_pre, *h_pre;
     sptgb_step_lists L;
     uint32_t ul[4];
-    int tuned;
+    uint32_t sched[4];           /* MTTKRP schedule bits per rank group (sptgb_step_lists.sched) */
+    int tuned_from_cache[4];     /* 1: the group's schedule came from the process cache, 0: timed, -1: no jobs */
     cudaStream_t cs;
     cudaStream_t as;             /* admission: uploads, checks, sorts of new slots, overlapping the step on cs */
     cudaGraphExec_t gexec;
@@ -561,43 +568,92 @@ static int retire(sptgbServer *s, uint32_t R) {
 }
 
 /* ------------------------------------------------------ autotuning -- */
-static int autotune(sptgbServer *s) {
-    static const uint32_t cand[4] = {64, 128, 256, 512};
+/* Schedules tuned in this process: [rank group][order 3 / 4][log2 of the
+ * mean nonzeros per job]. */
+#define TUNE_BUCKETS 40
+typedef struct {
+    uint32_t ul, sched;
+    int valid;
+} tune_entry;
+static tune_entry g_tune[4][2][TUNE_BUCKETS];
+static pthread_mutex_t g_tune_lock = PTHREAD_MUTEX_INITIALIZER;
+
+/* Tunes every rank group that has admitted jobs and no schedule yet (a
+ * group is tuned once, before the first iteration of its first jobs);
+ * *ntuned = groups given a schedule by this call. */
+static int autotune(sptgbServer *s, int *ntuned) {
+    static const uint32_t cand_ul[4] = {64, 128, 256, 512};
     const char *module = "GPU server tune";
+    *ntuned = 0;
+    uint64_t nnz3[4] = {0, 0, 0, 0}, nnz4[4] = {0, 0, 0, 0}, jobs[4] = {0, 0, 0, 0};
+    for (uint32_t i = 0; i < s->cap; ++i)
+        if (s->slot_job[i] >= 0 && s->hs[i].nnz) {
+            const int g = group_of(s->hs[i].stride);
+            ++jobs[g];
+            if (s->hs[i].nmodes == 3) nnz3[g] += s->hs[i].nnz;
+            else nnz4[g] += s->hs[i].nnz;
+        }
+    int todo = 0;
+    for (int g = 0; g < 4; ++g) todo |= jobs[g] && s->tuned_from_cache[g] < 0;
+    if (!todo) return 0;
     cudaEvent_t e0, e1;
     SPTGB_CUDA(cudaEventCreate(&e0), module);
     SPTGB_CUDA(cudaEventCreate(&e1), module);
     for (int g = 0; g < 4; ++g) {
+        if (!jobs[g] || s->tuned_from_cache[g] >= 0) continue;
+        ++*ntuned;
+        const int ord = nnz4[g] > nnz3[g];
+        int bucket = 0;
+        for (uint64_t mean = (nnz3[g] + nnz4[g]) / jobs[g]; mean > 1 && bucket < TUNE_BUCKETS - 1; mean >>= 1)
+            ++bucket;
+        pthread_mutex_lock(&g_tune_lock);
+        const tune_entry hit = g_tune[g][ord][bucket];
+        pthread_mutex_unlock(&g_tune_lock);
+        if (hit.valid) {
+            s->ul[g] = hit.ul;
+            s->sched[g] = hit.sched;
+            s->tuned_from_cache[g] = 1;
+            continue;
+        }
         float best = 1e30f;
-        uint32_t best_ul = s->ul[g];
-        int present = 0;
-        for (uint32_t i = 0; i < s->cap && !present; ++i)
-            if (s->slot_job[i] >= 0 && group_of(s->hs[i].stride) == g && s->hs[i].nnz) present = 1;
-        if (!present) continue;
+        uint32_t best_ul = s->ul[g], best_sched = s->sched[g];
         for (int c = 0; c < 4; ++c) {
-            s->ul[g] = cand[c];
+            s->ul[g] = cand_ul[c];
             step_lists_build(s);
             SPTGB_CHECK(lists_upload(s, 0, NL_STEP, s->cs), module);
             const sptgb_wlist w = wl(s, NL_MT + g);
-            float ms = 0.f, tot = 0.f;
-            for (int rep = 0; rep < 3; ++rep) {
-                SPTGB_CUDA(cudaEventRecord(e0, s->cs), module);
-                SPTGB_CUDA(sptgb_batch_mttkrp(s->ds, &w, 0, g, cand[c], s->cs), module);
-                SPTGB_CUDA(cudaEventRecord(e1, s->cs), module);
-                SPTGB_CUDA(cudaEventSynchronize(e1), module);
-                SPTGB_CUDA(cudaEventElapsedTime(&ms, e0, e1), module);
-                if (rep) tot += ms;
-            }
-            if (tot < best) {
-                best = tot;
-                best_ul = cand[c];
+            for (uint32_t sc = 0; sc < 4; ++sc) {
+                float ms = 0.f, tot = 0.f;
+                for (int rep = 0; rep < 3; ++rep) {
+                    SPTGB_CUDA(cudaEventRecord(e0, s->cs), module);
+                    SPTGB_CUDA(sptgb_batch_mttkrp(s->ds, &w, 0, g, cand_ul[c], sc, s->cs), module);
+                    SPTGB_CUDA(cudaEventRecord(e1, s->cs), module);
+                    SPTGB_CUDA(cudaEventSynchronize(e1), module);
+                    SPTGB_CUDA(cudaEventElapsedTime(&ms, e0, e1), module);
+                    if (rep) tot += ms;
+                }
+                if (tot < best) {
+                    best = tot;
+                    best_ul = cand_ul[c];
+                    best_sched = sc;
+                }
             }
         }
         s->ul[g] = best_ul;
+        s->sched[g] = best_sched;
+        s->tuned_from_cache[g] = 0;
+        pthread_mutex_lock(&g_tune_lock);
+        g_tune[g][ord][bucket] = (tune_entry){best_ul, best_sched, 1};
+        pthread_mutex_unlock(&g_tune_lock);
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    s->tuned = 1;
+    if (s->trace)
+        for (int g = 0; g < 4; ++g)
+            if (jobs[g] && s->tuned_from_cache[g] >= 0)
+                fprintf(stderr, "[sptgb server] rank <= %d: MTTKRP unit %u, %s record batches, %d blocks/SM (%s)\n",
+                        8 << g, s->ul[g], (s->sched[g] & 1u) ? "deep" : "shallow", (s->sched[g] & 2u) ? 3 : 2,
+                        s->tuned_from_cache[g] ? "cached" : "timed");
     return 0;
 }
 
@@ -613,7 +669,10 @@ static int capture(sptgbServer *s) {
         s->L.one[m] = wl(s, NL_ONE + m);
         s->L.dn[m] = wl(s, NL_DN + m);
     }
-    for (int g = 0; g < 4; ++g) s->L.ul[g] = s->ul[g];
+    for (int g = 0; g < 4; ++g) {
+        s->L.ul[g] = s->ul[g];
+        s->L.sched[g] = s->sched[g];
+    }
     s->L.fit = wl(s, NL_FIT);
     s->L.fit_one = wl(s, NL_FITONE);
     /* One ALS iteration of every admitted job: by default the sequence of
@@ -700,7 +759,11 @@ int sptgbServerCreate(sptgbServer **out, size_t hbm_budget_bytes, uint32_t max_s
     s->freel[0].off = 0;
     s->freel[0].len = s->budget;
     s->nfree = 1;
-    for (int g = 0; g < 4; ++g) s->ul[g] = 256;
+    for (int g = 0; g < 4; ++g) {
+        s->ul[g] = 256;
+        s->sched[g] = 1;   /* deep batches, 2 blocks per SM until tuned */
+        s->tuned_from_cache[g] = -1;
+    }
     s->changed = 1;
     const char *tr = getenv("SPTGB_TRACE");
     s->trace = tr && tr[0] && tr[0] != '0';
@@ -762,9 +825,14 @@ int sptgbServerStep(sptgbServer *s, uint32_t *active, uint32_t *queued) {
      *    the host and the copy engines while the graph runs */
     uint32_t R = 0;
     if (s->nactive > 0) {
-        if (!s->tuned) {
-            SPTGB_CHECK(autotune(s), module);
+        int ntuned = 0;
+        SPTGB_CHECK(autotune(s, &ntuned), module);
+        if (ntuned) {
             s->changed = 1;
+            if (s->have_graph) {   /* the schedules are launch parameters of the captured step */
+                cudaGraphExecDestroy(s->gexec);
+                s->have_graph = 0;
+            }
         }
         if (s->changed) {
             step_lists_build(s);
@@ -870,6 +938,16 @@ size_t sptgbServerBytesInUse(const sptgbServer *s) { return s->used; }
 
 uint32_t sptgbServerUnitLength(const sptgbServer *s, int group) { return group >= 0 && group < 4 ? s->ul[group] : 0; }
 int sptgbServerPersistent(const sptgbServer *s) { return s->persistent; }
+
+int sptgbServerSchedule(const sptgbServer *s, int group, uint32_t *unit_len, uint32_t *deep, uint32_t *blocks_per_sm,
+                        int *from_cache) {
+    if (group < 0 || group > 3) return SPTERR_VALUE_ERROR;
+    *unit_len = s->ul[group];
+    *deep = s->sched[group] & 1u;
+    *blocks_per_sm = (s->sched[group] & 2u) ? 3u : 2u;
+    *from_cache = s->tuned_from_cache[group];
+    return 0;
+}
 
 int sptgbGridBarrierSelfTest(int missing, int *err, unsigned int *rounds) {
     const char *module = "GPU barrier self-test";

@@ -213,14 +213,17 @@ cudaError_t sptgb_gram(const float *A, uint32_t nrows, int rank, int stride, dou
 /* Builds H = Hadamard of grams[m] for m != mode (grams: host array of
  * device pointers), factorises it (Cholesky, or LU with partial pivoting
  * when H is not SPD) and writes S = (H^{-1})^T to Hinv.
- * status (device int): 0 Cholesky, 1 LU fallback, 2 singular. */
+ * status (device int): bits 0-7 = 0 Cholesky, 1 LU fallback, 2 singular;
+ * bits 8 and up = e, the inverse stored divided by 2^e (e > 0 only when its
+ * largest entry exceeds 2^32). */
 cudaError_t sptgb_solve_prepare(const double *const *grams, int nmodes, int mode, int rank,
                                 double *Hinv, int *status, cudaStream_t s);
 /* X[i,:] solves H x = M[i,:] for i < nrows (FP64 arithmetic, FP32
- * storage) given S = (H^{-1})^T; leaves per-block partials of X^T X and of
- * the column maxima in ws for sptgb_normalize.  X must not alias M. */
+ * storage) given S = (H^{-1})^T and the status word sptgb_solve_prepare
+ * wrote with it (its scale exponent); leaves per-block partials of X^T X and
+ * of the column maxima in ws for sptgb_normalize.  X must not alias M. */
 cudaError_t sptgb_solve_rows(const float *M, float *X, uint32_t nrows, int rank, int stride,
-                             const double *S, double *ws, cudaStream_t s);
+                             const double *S, const int *status, double *ws, cudaStream_t s);
 /* lambda from those partials (2-norm when use_2norm, else the column maximum
  * clamped to >= 1, matrix.c:390-554), X's columns divided by lambda, and
  * gram = the Gram matrix of the normalised X. */
@@ -303,7 +306,9 @@ typedef struct {
  * the fit's slots in the same order, one item each. */
 typedef struct {
     sptgb_wlist mt[4][4];
-    uint32_t ul[4];
+    uint32_t ul[4];     /* MTTKRP unit length per lane group */
+    uint32_t sched[4];  /* MTTKRP schedule per lane group: bit 0 deep record batches, bit 1 the
+                           3-blocks-per-SM build (the persistent step honours bit 0 only) */
     sptgb_wlist zr[4], one[4], dn[4], fit, fit_one;
 } sptgb_step_lists;
 cudaError_t sptgb_batch_step(const sptgb_slot *slots, const sptgb_step_lists *L, cudaStream_t s);
@@ -321,7 +326,7 @@ cudaError_t sptgb_batch_step_persistent(const sptgb_slot *slots, const sptgb_ste
 cudaError_t sptgb_grid_barrier_selftest(int missing, int *err, unsigned int *rounds);
 /* The MTTKRP launch of mode m, lane group g alone (for timing). */
 cudaError_t sptgb_batch_mttkrp(const sptgb_slot *slots, const sptgb_wlist *w, int mode, int group, uint32_t ul,
-                               cudaStream_t s);
+                               uint32_t sched, cudaStream_t s);
 /* Grid sizes the step uses, so that hosts size their prefix lists. */
 uint32_t sptgb_batch_rows_per_block(void);
 uint32_t sptgb_batch_fit_rows_per_block(void);

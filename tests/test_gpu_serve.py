@@ -92,7 +92,30 @@ def test_batched_jobs_match_plain_path():
     assert srv.bytes_in_use() == 0
     for g in range(4):
         assert srv.unit_length(g) in (64, 128, 256, 512)
+        sch = srv.schedule(g)
+        assert sch["unit"] == srv.unit_length(g)
+        assert sch["blocks_per_sm"] in (2, 3) and sch["batches"] in ("deep", "shallow")
+        assert sch["source"] in ("timed", "cached")   # every rank group has jobs in JOBS
     assert not srv.persistent()
+
+
+def test_tuned_schedules_are_reused():
+    """A second server given jobs of the same kinds takes every rank group's
+    MTTKRP schedule from the process cache instead of timing again."""
+    tensors = [make_tensor(700 + i, d, n) for i, (d, n, r) in enumerate(JOBS)]
+    inits = [init_for(d, r, 800 + i) for i, (d, n, r) in enumerate(JOBS)]
+    first = S.Server(4 << 30, 64)
+    for t, (d, n, r), ini in zip(tensors, JOBS, inits):
+        first.submit(t, r, 2, ini)
+    first.drain()
+    second = S.Server(4 << 30, 64)
+    for t, (d, n, r), ini in zip(tensors, JOBS, inits):
+        second.submit(t, r, 2, ini)
+    second.drain()
+    for g in range(4):
+        a, b = first.schedule(g), second.schedule(g)
+        assert b["source"] == "cached", (g, a, b)
+        assert (a["unit"], a["batches"], a["blocks_per_sm"]) == (b["unit"], b["batches"], b["blocks_per_sm"])
 
 
 def _run_mix(step_kind, niters=5):
@@ -258,3 +281,21 @@ def test_grid_barrier_wait_is_bounded():
     k = srv.submit(t, 8, 2, init_for([50, 40, 30], 8, 10))
     srv.drain()
     assert np.all(np.isfinite(srv.result(k)[2]))
+
+
+def test_rank_group_tuned_when_it_first_gets_jobs():
+    """Jobs of a new rank group arriving after the first step get a tuned
+    schedule of their own before their first iteration."""
+    srv = S.Server(4 << 30, 16)
+    t8 = make_tensor(901, [300, 200, 100], 5000)
+    k8 = srv.submit(t8, 8, 6, init_for([300, 200, 100], 8, 902))
+    srv.step()
+    srv.step()
+    assert srv.schedule(0)["source"] in ("timed", "cached")
+    assert srv.schedule(3)["source"] == "no jobs"
+    t64 = make_tensor(903, [200, 100, 70, 64], 8000)
+    k64 = srv.submit(t64, 64, 3, init_for([200, 100, 70, 64], 64, 904))
+    srv.drain()
+    assert srv.schedule(3)["source"] in ("timed", "cached")
+    for k in (k8, k64):
+        assert np.all(np.isfinite(srv.result(k)[2]))
