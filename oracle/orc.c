@@ -666,9 +666,12 @@ static int solve_rows_f64(double *H, int R, double *X, uint64_t nrows, int ld) {
         free(L);
         return 0;
     }
-    /* LU with partial pivoting of H, solve H x = m per row. */
+    /* LU with partial pivoting of H, solve H x = m per row.  An exactly zero
+     * pivot leaves the rows unsolved, as sgesv_ returns with info > 0 and the
+     * right-hand sides untouched (matrix_solver.c:66-80). */
     int *piv = (int *)malloc(R * sizeof(int));
     memcpy(L, H, (size_t)R * R * sizeof(double));
+    int zero_pivot = 0;
     for (int k = 0; k < R; ++k) {
         int p = k;
         for (int i = k + 1; i < R; ++i)
@@ -685,6 +688,13 @@ static int solve_rows_f64(double *H, int R, double *X, uint64_t nrows, int ld) {
                 L[i * R + k] /= L[k * R + k];
                 for (int j = k + 1; j < R; ++j) L[i * R + j] -= L[i * R + k] * L[k * R + j];
             }
+        else
+            zero_pivot = 1;
+    }
+    if (zero_pivot) {
+        free(piv);
+        free(L);
+        return 2;
     }
 #pragma omp parallel for schedule(static) num_threads(orc_threads)
     for (uint64_t i = 0; i < nrows; ++i) {

@@ -262,6 +262,14 @@ __device__ __forceinline__ void solve_prepare_body(GramPtrs grams, int nmodes, i
         }
         __syncthreads();
     }
+    // An exactly zero pivot: LAPACK's sgesv (the reference's fallback,
+    // matrix_solver.c:66-80) stops after the factorisation and leaves the
+    // right-hand sides unsolved, so the rows stay the MTTKRP output: S = I.
+    if (singular) {
+        for (int e = tid; e < RR; e += DT) S[e] = (e / rank == e % rank) ? 1.0 : 0.0;
+        finish_inverse(S, RR, status, 2);
+        return;
+    }
     // Inverse column by column: solve L U x = P e_j.  S = (H^{-1})^T, so
     // row j of S is column j of the inverse.
     for (int j = tid; j < rank; j += DT) {
@@ -285,7 +293,7 @@ __device__ __forceinline__ void solve_prepare_body(GramPtrs grams, int nmodes, i
         }
         for (int i = 0; i < rank; ++i) S[j * rank + i] = x[i];
     }
-    finish_inverse(S, RR, status, singular ? 2 : 1);
+    finish_inverse(S, RR, status, 1);
 }
 
 // X[i, :] = M[i, :] * S (S = (H^{-1})^T, so row i of X solves H x = m_i).

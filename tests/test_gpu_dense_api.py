@@ -62,6 +62,23 @@ def test_solve_normals(N, rank, mode):
     assert rel_fro(mats[N].array()[:rank, :rank], H) <= 1e-6
 
 
+@pytest.mark.parametrize("N,rank,mode,zero_col", [(3, 16, 1, 5), (4, 32, 3, 0)])
+def test_solve_normals_exactly_singular_leaves_rows(N, rank, mode, zero_col):
+    """Exactly singular Hadamard (a zero row and column in one Gram): the
+    rows come back unsolved, bit for bit, as the reference's sgesv_ fallback
+    leaves them (pinned in tests/test_oracle_dense.py)."""
+    rng = np.random.default_rng(11 + rank)
+    gs = _grams(rng, N, rank)
+    k = (mode + 1) % N
+    gs[k][zero_col, :] = 0.0
+    gs[k][:, zero_col] = 0.0
+    mats = [S.Matrix.from_array(g) for g in gs] + [S.Matrix(rank, rank)]
+    rhs_a = rng.uniform(-1, 1, (300, rank)).astype(np.float32)
+    rhs = S.Matrix.from_array(rhs_a)
+    assert S.lib().sptMatrixSolveNormals(mode, N, _arr(mats), C.byref(rhs.s)) == 0
+    assert np.array_equal(rhs.array()[:300, :rank], rhs_a)
+
+
 def test_norms_and_final_lambda():
     rng = np.random.default_rng(3)
     rank = 20

@@ -88,3 +88,20 @@ def test_solve_normals_formula(N, rank, mode):
     X = np.linalg.solve(H, rhs.astype(np.float64).T).T
     err = np.linalg.norm(got - X) / np.linalg.norm(X)
     assert err <= 1e-5, err
+
+
+@pytest.mark.parametrize("N,rank,mode,zero_col", [(3, 16, 1, 5), (4, 32, 3, 0)])
+def test_solve_normals_exactly_singular_leaves_rows(N, rank, mode, zero_col):
+    """A Gram with a zero row and column (a factor column that is all zero)
+    makes the Hadamard exactly singular: the reference's spotrf_ fails, its
+    sgesv_ fallback meets an exactly zero pivot and returns with the
+    right-hand sides untouched, so sptMatrixSolveNormals leaves the rows as
+    they came in.  The device solve and the oracle restate that."""
+    rng = np.random.default_rng(11 + rank)
+    gs = _grams(rng, N, rank)
+    k = (mode + 1) % N
+    gs[k][zero_col, :] = 0.0
+    gs[k][:, zero_col] = 0.0
+    rhs = rng.uniform(-1, 1, (300, rank)).astype(np.float32)
+    got = O.ref_solve_normals(gs, mode, rhs)
+    assert np.array_equal(got, rhs)
