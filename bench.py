@@ -268,11 +268,11 @@ def run_served(reqs, tensors, inits, outs, poisson, keep_fits):
         t_poll += time.monotonic() - a2
     span = time.monotonic() - t0 - (reqs[0]["arrival"] if poisson else 0.0)
     launches = S.launch_count() - n0
-    units = {g: srv.unit_length(g) for g in range(4)}
+    units = {g: srv.schedule(g) for g in range(4)}
     persistent = srv.persistent()
     srv.free()
     return {"solves_per_s": n / span, "makespan_s": span, "lat": lat, "fits": fits, "steps": steps,
-            "launches": int(launches), "unit_lengths": units, "persistent": persistent,
+            "launches": int(launches), "schedules": units, "persistent": persistent,
             "host_s": {"submit": round(t_sub, 3), "step": round(t_step, 3), "poll": round(t_poll, 3)}}
 
 
@@ -451,11 +451,13 @@ def serve_leg(args):
         "served": {"solves_per_s": round(served["solves_per_s"], 1), "p50_ms": pct(served["lat"], 50),
                    "p99_ms": pct(served["lat"], 99), "makespan_s": round(served["makespan_s"], 3),
                    "steps": served["steps"], "gpu_launches": served["launches"],
-                   "unit_lengths": served["unit_lengths"], "persistent_step": served["persistent"],
+                   "mttkrp_schedule_by_rank": {"<=%d" % (8 << g): v for g, v in served["schedules"].items()},
+                   "persistent_step": served["persistent"],
                    "host_s": served["host_s"]},
         "batched": {"solves_per_s": round(batched["solves_per_s"], 1), "p50_ms": pct(batched["lat"], 50),
                     "p99_ms": pct(batched["lat"], 99), "makespan_s": round(batched["makespan_s"], 3),
                     "steps": batched["steps"], "gpu_launches": batched["launches"],
+                    "mttkrp_schedule_by_rank": {"<=%d" % (8 << g): v for g, v in batched["schedules"].items()},
                     "persistent_step": batched["persistent"], "host_s": batched["host_s"]},
         "batched_persistent_step": {
             "solves_per_s": round(pers["solves_per_s"], 1), "makespan_s": round(pers["makespan_s"], 3),

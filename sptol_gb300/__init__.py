@@ -234,6 +234,7 @@ def _declare(L):
         "sptgbServerBytesInUse": (C.c_size_t, [C.c_void_p]),
         "sptgbServerUnitLength": (C.c_uint32, [C.c_void_p, C.c_int]),
         "sptgbServerPersistent": (C.c_int, [C.c_void_p]),
+        "sptgbServerSchedule": (C.c_int, [C.c_void_p, C.c_int, u32p, u32p, u32p, C.POINTER(C.c_int)]),
         "sptgbGridBarrierSelfTest": (C.c_int, [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_uint)]),
         "sptgbServerFree": (None, [C.c_void_p]),
     }
@@ -633,6 +634,15 @@ class Server:
 
     def unit_length(self, group):
         return int(lib().sptgbServerUnitLength(self.h, group))
+
+    def schedule(self, group):
+        """The tuned MTTKRP schedule of a rank group: dict of unit length,
+        record batch depth, blocks per SM and where it came from."""
+        ul, deep, bps, src = C.c_uint32(), C.c_uint32(), C.c_uint32(), C.c_int()
+        _check(lib().sptgbServerSchedule(self.h, group, C.byref(ul), C.byref(deep), C.byref(bps), C.byref(src)),
+               "sptgbServerSchedule")
+        return {"unit": int(ul.value), "batches": "deep" if deep.value else "shallow",
+                "blocks_per_sm": int(bps.value), "source": {1: "cached", 0: "timed", -1: "no jobs"}[src.value]}
 
     def persistent(self):
         """True when each step runs as one persistent cooperative kernel."""

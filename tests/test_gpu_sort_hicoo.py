@@ -190,6 +190,23 @@ def test_hicoo_window_kernel_3d_every_worker_width(rank):
         assert rel_fro(out, ref) <= 1e-5, (mode, rel_fro(out, ref))
 
 
+@pytest.mark.parametrize("sb", [4, 8])
+def test_hicoo_window_kernel_3d_block_sizes(sb):
+    """Order 3 with 16- and 256-row windows: the heavy windows' row counting
+    sort covers every window size the format allows (2^sb <= 256)."""
+    t = _skewed3(500_000, 23)
+    ndims = t.ndims
+    h = S.HiCOO(t, sb, 17)
+    i2, v2 = t.arrays()
+    rank = 32
+    mats = S.new_factors(ndims, rank, seed=10)
+    facs = [m.array()[: ndims[k]].copy() for k, m in enumerate(mats[:3])]
+    for mode in range(3):
+        out = S.mttkrp_hicoo(h, mats, mode)
+        ref = O.mttkrp(ndims, i2, v2, facs, rank, mode, precision="f64")
+        assert rel_fro(out, ref) <= 1e-5, (mode, rel_fro(out, ref))
+
+
 def test_hicoo_empty_blocks_in_a_caller_hicoo():
     """A caller's HiCOO may hold empty blocks (repeated bptr entries), alone,
     in a run of 100, inside windows and as windows of their own; the result is
