@@ -107,6 +107,8 @@ static int cpd_run(int N, const sptIndex *ndims, const float *vals, uint64_t nnz
     for (int m = 0; m < N; ++m)
         CUDA_OR_FAIL(sptgb_gram(b.fac[m], ndims[m], (int)rank, stride, b.gram[m], b.ws, s));
 
+    double t_prev = sptgb_wall();
+    SPTGB_TRACE_POINT("cpd setup", s, t_prev);
     double oldfit = 0.0;
     const double *gptr[SPTGB_MAX_MODES];
     for (int m = 0; m < N; ++m) gptr[m] = b.gram[m];
@@ -140,6 +142,7 @@ static int cpd_run(int N, const sptIndex *ndims, const float *vals, uint64_t nnz
         oldfit = fit;
     }
 
+    SPTGB_TRACE_POINT("cpd iters", s, t_prev);
     /* GetFinalLambda: lambda *= column 2-norms of every factor, factors
      * normalised by them (matrix.c:557-573). */
     for (int m = 0; m < N; ++m)
@@ -153,6 +156,7 @@ static int cpd_run(int N, const sptIndex *ndims, const float *vals, uint64_t nnz
     if (fits)
         for (sptIndex it = 0; it < niters; ++it) fits[it] = it < done_iters ? hfits[it] : NAN;
     if (iters_done) *iters_done = done_iters;
+    SPTGB_TRACE_POINT("cpd d2h", s, t_prev);
 
 done:
     free_buffers(&b);
@@ -190,12 +194,17 @@ int sptgbCpdAls(sptSparseTensor const *X, sptIndex rank, sptIndex niters, double
     }
     SPTGB_CHECK(sptgb_ctx(), module);
     const cudaStream_t s = sptgb_stream();
+    double t_prev = sptgb_wall();
     sptgbCoo *t = NULL;
     int r = sptgbCooCreate(&t, X, (void *)s);
+    SPTGB_TRACE_POINT("cpd upload", s, t_prev);
     for (int m = 0; m < N && !r; ++m) r = sptgbCooPrepareMode(t, (sptIndex)m, (void *)s);
+    SPTGB_TRACE_POINT("cpd sorts", s, t_prev);
     if (!r) r = cpd_run(N, X->ndims, t->vals, t->nnz, coo_mttkrp, t, rank, stride, hfac, niters, tol, lambda, fits,
                         iters_done, s);
+    SPTGB_TRACE_POINT("cpd loop", s, t_prev);
     if (t) sptgbCooFree(t);
+    SPTGB_TRACE_POINT("cpd free", s, t_prev);
     return r;
 }
 
