@@ -20,6 +20,7 @@
 #include <stdio.h>
 #include <stdint.h>
 #include <inttypes.h>
+#include <math.h>      /* the reference's header includes it; its callers use pow() */
 #include <stdbool.h>
 
 #ifdef __cplusplus
@@ -58,6 +59,13 @@ typedef unsigned __int128 sptMortonIndex;
 #define PARTI_PRI_BLOCKNNZ_INDEX PARTI_PRI_BLOCK_INDEX
 #define PARTI_SCN_BLOCKNNZ_INDEX PARTI_SCN_BLOCK_INDEX
 #define PARTI_PRI_NNZ_INDEX PRIu64
+/* Tuning constants of the reference's CPU schedules (macros.h:23-28); its
+ * HiCOO callers print them and pick a reduction schedule with them. */
+#define NUM_CORES 32
+#define L1_SIZE 32000
+#define PAR_DEGREE_REDUCE 20
+#define PAR_MAX_DEGREE 100
+#define PAR_MIN_DEGREE 4
 #define PARTI_SCN_NNZ_INDEX SCNu64
 
 /* --------------------------------------------------------------- errors --
@@ -297,6 +305,10 @@ int  sptSparseTensorToHiCOO(sptSparseTensorHiCOO *hitsr, sptNnzIndex *max_nnzb, 
                             const sptElementIndex sb_bits, const sptElementIndex sk_bits, int const tk);
 int  sptSetKernelPointers(sptNnzIndexVector *kptr, sptSparseTensor *tsr, const sptElementIndex sk_bits);
 double sptSparseTensorFrobeniusNormSquaredHiCOO(sptSparseTensorHiCOO const *const hitsr);
+/* The HiCOO summary the reference prints (hicoo/status.c:28-118): sizes,
+ * storage, schedule per mode, block-size statistics and the suggested
+ * parameters, in the same lines. */
+void sptSparseTensorStatusHiCOO(sptSparseTensorHiCOO *hitsr, FILE *fp);
 
 /* --------------------------------------------------------------- MTTKRP --
  * mats[0..nmodes-1] are the factor matrices, mats[nmodes] receives the

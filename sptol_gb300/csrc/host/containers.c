@@ -217,6 +217,76 @@ void sptSparseTensorStatus(sptSparseTensor *tsr, FILE *fp) {
     free(b);
 }
 
+static int cmp_nnz(const void *a, const void *b) {
+    const sptNnzIndex x = *(const sptNnzIndex *)a, y = *(const sptNnzIndex *)b;
+    return x < y ? -1 : x > y;
+}
+
+/* hicoo/status.c:28-118: the same lines, in the same format.  Block sizes
+ * are bptr differences; the median is element (nb + 1) / 2 - 1 of the sorted
+ * sizes, the geometric mean the product over blocks, in block order, of
+ * (nnzb / sb)^(1 / nb).  A tensor without blocks prints zero statistics. */
+void sptSparseTensorStatusHiCOO(sptSparseTensorHiCOO *hitsr, FILE *fp) {
+    const sptIndex N = hitsr->nmodes;
+    fprintf(fp, "HiCOO Sparse Tensor information ---------\n");
+    fprintf(fp, "DIMS=%" PARTI_PRI_INDEX, hitsr->ndims[0]);
+    for (sptIndex m = 1; m < N; ++m) fprintf(fp, "x%" PARTI_PRI_INDEX, hitsr->ndims[m]);
+    fprintf(fp, " NNZ=%" PARTI_PRI_NNZ_INDEX "\n", hitsr->nnz);
+    const sptIndex sb = (sptIndex)1 << hitsr->sb_bits, sk = (sptIndex)1 << hitsr->sk_bits;
+    fprintf(fp, "sb=%" PARTI_PRI_INDEX " sk=%" PARTI_PRI_INDEX "\n", sb, sk);
+    const sptNnzIndex nb = hitsr->bptr.len ? hitsr->bptr.len - 1 : 0;
+    fprintf(fp, "nb=%" PARTI_PRI_NNZ_INDEX " nk=%" PARTI_PRI_NNZ_INDEX " nc=%" PARTI_PRI_NNZ_INDEX "\n", nb,
+            hitsr->kptr.len ? hitsr->kptr.len - 1 : 0, hitsr->cptr.len ? hitsr->cptr.len - 1 : 0);
+    sptNnzIndex bytes = hitsr->nnz * (sizeof(sptValue) + N * sizeof(sptElementIndex));
+    bytes += (sptNnzIndex)hitsr->binds[0].len * N * sizeof(sptBlockIndex);
+    bytes += (hitsr->bptr.len + hitsr->kptr.len + hitsr->cptr.len) * sizeof(sptNnzIndex);
+    for (sptIndex m = 0; m < N; ++m) {
+        const sptIndex kdim = (hitsr->ndims[m] + sk - 1) / sk;
+        for (sptIndex i = 0; i < kdim; ++i) bytes += (sptNnzIndex)hitsr->kschr[m][i].len * sizeof(sptIndex);
+        bytes += kdim * sizeof(sptIndexVector *);
+    }
+    bytes += N * sizeof(sptIndexVector **) + N * sizeof(sptIndex);
+    char *b = sptBytesString(bytes);
+    fprintf(fp, "HiCOO-STORAGE=%s\n", b ? b : "?");
+    free(b);
+    fprintf(fp, "SCHEDULE INFO [KERNEL]: \n");
+    for (sptIndex m = 0; m < N; ++m)
+        fprintf(fp, "SCHEDULE MODE %" PARTI_PRI_INDEX " : %" PARTI_PRI_INDEX " x %" PARTI_PRI_INDEX "\n", m,
+                (hitsr->ndims[m] + sk - 1) / sk, hitsr->nkiters[m]);
+    sptNnzIndex mx = 0, mn = 0, sum = 0, med = 0;
+    double geo = 1.0;
+    fprintf(fp, "block nnzs:\n");
+    if (nb) {
+        sptNnzIndex *sz = (sptNnzIndex *)malloc(nb * sizeof *sz);
+        mx = mn = hitsr->bptr.data[1] - hitsr->bptr.data[0];
+        for (sptNnzIndex i = 0; i < nb; ++i) {
+            const sptNnzIndex n = hitsr->bptr.data[i + 1] - hitsr->bptr.data[i];
+            if (n > mx) mx = n;
+            if (n < mn) mn = n;
+            sum += n;
+            geo *= pow((double)n / sb, 1.0 / nb);
+            if (sz) sz[i] = n;
+        }
+        if (sz) {
+            qsort(sz, nb, sizeof *sz, cmp_nnz);
+            med = sz[(nb + 1) / 2 - 1];
+            free(sz);
+        }
+    }
+    const sptNnzIndex aver = nb ? sum / nb : 0;
+    fprintf(fp, "Nnzb: Max=%lu, Min=%lu, Aver=%lu\n", (unsigned long)mx, (unsigned long)mn, (unsigned long)aver);
+    fprintf(fp, "cb: Max=%.3lf, Min=%.3lf, Aver=%.3lf\n", (double)mx / sb, (double)mn / sb, (double)aver / sb);
+    fprintf(fp, "median cb: %.3lf, geometric mean cb: %.3lf\n", (double)med / sb, geo);
+    fprintf(fp, "alpha_b: %lf\n", hitsr->nnz ? (double)nb / hitsr->nnz : 0.0);
+    fprintf(fp, "\nParameter configuration --------\n");
+    fprintf(fp, "Suggest B (sb) <= %.2lf / R. For cache efficiency\n", (double)L1_SIZE / N / sizeof(sptValue));
+    fprintf(fp, "Suggest alpha_b in (0,1], small is better. For tensor storage\n");
+    fprintf(fp, "Suggest cb > 1, large is better. For MTTKRP performance\n");
+    fprintf(fp, "Suggest num_tasks should in [%d, %d] PAR_DEGREE: [%d, %d]. For parallel efficiency\n",
+            PAR_MIN_DEGREE * NUM_CORES, PAR_MAX_DEGREE * NUM_CORES, PAR_MIN_DEGREE, PAR_MAX_DEGREE);
+    fprintf(fp, "\n\n");
+}
+
 /* sort.c:371-380: for every position z, srand(z + 1), one rand() scaled to a
  * position, and a swap of the two nonzeros (all modes and the value); the C
  * library's rand() makes it the reference's permutation on the same libc. */

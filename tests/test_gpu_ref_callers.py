@@ -11,10 +11,20 @@ separate programs:
                       -u 1) or sptOmpMTTKRP (-d -1 -u 0), each result written
                       by sptDumpMatrix (examples/mttkrp.c:142-291);
   examples/cpd.c      sptCpdAls (-d -2) / sptOmpCpdAls (-d -1) and
-                      sptDumpKruskalTensor (examples/cpd.c:107-140).
+                      sptDumpKruskalTensor (examples/cpd.c:107-140);
+  tests/test_ttm.c    sptSparseTensorMulMatrix of a 2x2x2 tensor, converted
+                      and dumped, checked by the program itself against its
+                      expected text (tests/test_ttm.c:45-106);
+  examples/convert_hicoo.c  sptLoadSparseTensor, sptSparseTensorToHiCOO,
+                      sptSparseTensorStatusHiCOO, sptDumpSparseTensorHiCOO
+                      (examples/convert_hicoo.c:79-92);
+  examples/loadstore.c  sptLoadSparseTensor then sptDumpSparseTensor
+                      (examples/loadstore.c:22-42).
 
 Their printed results are checked against the oracle run from the same
-initial factors: this library's sptRandomizeMatrix draws the k-th matrix of a
+initial factors, or, for the converters, against the same program built
+on the reference library (oracle/_ref/libparti_ref.so) and run on the same
+input: this library's sptRandomizeMatrix draws the k-th matrix of a
 process from a seeded stream (SPTGB_SEED), restated here in numpy and pinned
 to the library by a CPU test.  The reference sources come from the staged copy
 (oracle/_ref/tree, `make -C oracle stage`); without it these tests skip."""
@@ -31,7 +41,9 @@ import oracle as O
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 TREE = O.REF_TREE
 LIBDIR = os.path.join(ROOT, "sptol_gb300", "lib")
-CALLERS = {"test_cpd": "tests/test_cpd.c", "mttkrp": "examples/mttkrp.c", "cpd": "examples/cpd.c"}
+CALLERS = {"test_cpd": "tests/test_cpd.c", "mttkrp": "examples/mttkrp.c", "cpd": "examples/cpd.c",
+           "test_ttm": "tests/test_ttm.c", "convert_hicoo": "examples/convert_hicoo.c",
+           "loadstore": "examples/loadstore.c"}
 have_tree = pytest.mark.skipif(not all(os.path.exists(os.path.join(TREE, p)) for p in CALLERS.values()),
                                reason="reference sources not staged (make -C oracle stage)")
 GAMMA = 0x9E3779B97F4A7C15
@@ -80,11 +92,22 @@ def test_seeded_matrix_restatement_matches_library():
             os.remove(path)
 
 
-def _compile(name, outdir):
-    exe = os.path.join(outdir, name)
-    cmd = ["gcc", "-O2", "-std=gnu99", "-fopenmp", "-D_GNU_SOURCE", "-DPARTI_USE_OPENMP",
-           "-I", os.path.join(ROOT, "include"), "-o", exe, os.path.join(TREE, CALLERS[name]),
-           "-L", LIBDIR, "-lParTI", "-Wl,-rpath," + LIBDIR, "-lm"]
+def _compile(name, outdir, on_reference=False):
+    """The caller against include/ParTI.h and libParTI.so, or (on_reference)
+    against the reference's own headers and its library built from the staged
+    sources."""
+    if on_reference:
+        exe = os.path.join(outdir, name + "_ref")
+        refdir = os.path.dirname(O.REF_PATH)
+        cmd = ["gcc", "-O2", "-std=gnu99", "-fopenmp", "-D_GNU_SOURCE", "-DPARTI_USE_OPENMP",
+               "-DPARTI_INDEX_TYPEWIDTH=32", "-DPARTI_VALUE_TYPEWIDTH=32", "-DPARTI_ELEMENT_INDEX_TYPEWIDTH=8",
+               "-I", os.path.join(TREE, "include"), "-o", exe, os.path.join(TREE, CALLERS[name]),
+               "-L", refdir, "-lparti_ref", "-Wl,-rpath," + refdir, "-lm"]
+    else:
+        exe = os.path.join(outdir, name)
+        cmd = ["gcc", "-O2", "-std=gnu99", "-fopenmp", "-D_GNU_SOURCE", "-DPARTI_USE_OPENMP",
+               "-I", os.path.join(ROOT, "include"), "-o", exe, os.path.join(TREE, CALLERS[name]),
+               "-L", LIBDIR, "-lParTI", "-Wl,-rpath," + LIBDIR, "-lm"]
     subprocess.run(cmd, check=True, capture_output=True, text=True)
     return exe
 
@@ -201,3 +224,67 @@ def test_reference_cpd_example(tmp_path, flags):
     init = [seeded_matrix(seed, m, ndims[m], rank) for m in range(3)]
     _, _, ofits, oit = O.cpd_als(ndims, inds, vals_read, rank, 5, 1e-5, init)
     assert abs(fit - ofits[oit - 1]) <= 1e-4, (fit, ofits[:oit])
+
+
+have_ref_lib = pytest.mark.skipif(not os.path.exists(O.REF_PATH), reason="reference library not built (oracle.build())")
+
+
+@pytest.mark.gpu
+@have_tree
+def test_reference_test_ttm_program(tmp_path):
+    """tests/test_ttm.c unmodified: the TTM of its 2x2x2 tensor, converted to
+    a sparse tensor and dumped, must equal the text the program expects; it
+    exits 1 on any difference."""
+    exe = _compile("test_ttm", str(tmp_path))
+    p = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert p.returncode == 0, (p.stdout[-2000:], p.stderr[-2000:])
+
+
+def _status_lines(text):
+    keep = ("DIMS=", "sb=", "nb=", "HiCOO-STORAGE=", "SCHEDULE MODE", "Nnzb:", "cb:", "median cb:", "alpha_b:",
+            "Suggest", "COO-STORAGE=", "Average slice length")
+    return [l.rstrip() for l in text.splitlines() if l.startswith(keep)]
+
+
+@pytest.mark.gpu
+@have_tree
+@have_ref_lib
+@pytest.mark.parametrize("bits", [(3, 5), (7, 17)], ids=["sb3_sk5", "sb7_sk17"])
+def test_reference_convert_hicoo_example_matches_reference(tmp_path, bits):
+    """examples/convert_hicoo.c unmodified, built on this library and on the
+    reference, same input: the dumped HiCOO files are byte-identical and the
+    COO and HiCOO status lines it prints are the same."""
+    ndims = [300, 200, 90]
+    inds, vals = _small_tensor(12, ndims, 20000)
+    tns = str(tmp_path / "x.tns")
+    _write_tns(tns, ndims, inds, vals)
+    outs = {}
+    for ref in (False, True):
+        exe = _compile("convert_hicoo", str(tmp_path), on_reference=ref)
+        dump = str(tmp_path / ("ref.txt" if ref else "ours.txt"))
+        stdout = _run([exe, "-i", tns, "-o", dump, "-b", str(bits[0]), "-k", str(bits[1])], 1)
+        outs[ref] = (open(dump, "rb").read(), _status_lines(stdout))
+    assert outs[False][0] == outs[True][0]
+    assert outs[False][1] == outs[True][1] and len(outs[True][1]) >= 10
+
+
+@pytest.mark.gpu
+@have_tree
+@have_ref_lib
+def test_reference_loadstore_example_matches_reference(tmp_path):
+    """examples/loadstore.c unmodified, built on this library and on the
+    reference: the same text file (with a zero value and a duplicated
+    coordinate) is read and written back byte-identically."""
+    ndims = [50, 40, 30]
+    inds, vals = _small_tensor(13, ndims, 3000)
+    vals[17] = 0.0
+    inds[:, 25] = inds[:, 24]
+    tns = str(tmp_path / "x.tns")
+    _write_tns(tns, ndims, inds, vals)
+    outs = []
+    for ref in (False, True):
+        exe = _compile("loadstore", str(tmp_path), on_reference=ref)
+        out = str(tmp_path / ("ref.tns" if ref else "ours.tns"))
+        _run([exe, tns, out], 1)
+        outs.append(open(out, "rb").read())
+    assert outs[0] == outs[1] and len(outs[0]) > 1000
