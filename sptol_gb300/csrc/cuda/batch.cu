@@ -267,7 +267,7 @@ cudaError_t mttkrp_group(const sptgb_slot *slots, const sptgb_wlist &w, int mode
 
 }  // namespace
 
-extern "C" uint32_t sptgb_batch_rows_per_block(void) { return TR; }
+extern "C" uint32_t sptgb_batch_solve_tile_rows(uint32_t rank) { return (uint32_t)solve_tile_rows((int)rank); }
 extern "C" uint32_t sptgb_batch_fit_rows_per_block(void) { return FIT_ROWS; }
 extern "C" uint32_t sptgb_batch_zero_rows(void) { return ZERO_ROWS; }
 extern "C" uint32_t sptgb_batch_max_blocks(void) { return NBLK; }

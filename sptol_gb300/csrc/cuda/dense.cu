@@ -85,7 +85,7 @@ extern "C" cudaError_t sptgb_solve_rows(const float *M, float *X, uint32_t nrows
         cudaFuncSetAttribute(k_solve_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SOLVE_SMEM);
         configured = 1;
     }
-    const int nb = nblocks_for_rows(nrows);
+    const int nb = nblocks_for_solve(nrows, rank);
     const size_t P = (size_t)rank * (rank + 1) / 2;
     k_solve_rows<<<nb, DT, SOLVE_SMEM, s>>>(M, X, nrows, rank, stride, Hinv, status, ws, ws + NBLK * P);
     sptgb_count_launch(1);
@@ -95,7 +95,7 @@ extern "C" cudaError_t sptgb_solve_rows(const float *M, float *X, uint32_t nrows
 // Consumes the partials left in ws by sptgb_solve_rows (same nrows).
 extern "C" cudaError_t sptgb_normalize(float *X, uint32_t nrows, int rank, int stride, double *gram,
                                           int use_2norm, float *lambda_f32, const double *ws, cudaStream_t s) {
-    const int nb = nblocks_for_rows(nrows);
+    const int nb = nblocks_for_solve(nrows, rank);
     const size_t P = (size_t)rank * (rank + 1) / 2;
     k_lambda<<<1, DT, 0, s>>>(ws, ws + NBLK * P, nb, rank, use_2norm, gram, lambda_f32, nullptr);
     uint64_t total = (uint64_t)nrows * rank;

@@ -397,8 +397,17 @@ __device__ __forceinline__ void fold(float2 hi, float2 lo, float &h, float &l) {
 }
 }  // namespace df2
 
-constexpr int LDK = RMAX + 2;   // row length of the k-major tiles (even: 8-byte pairs)
-constexpr int LDR = TR + 2;     // row length of the transposed X tile
+constexpr int LDK = RMAX + 2;   // row length of the k-major tiles at rank RMAX (even: 8-byte pairs)
+constexpr int LDR = TR + 2;     // row length of the transposed X tile at rank RMAX
+
+// Rows per tile of the row solve: 32 x (64 / the rank's power-of-two class),
+// so that a tile holds about 2,048 outputs (8 per thread) at every rank and
+// the per-tile barriers and Gram loop are paid per 2,048 outputs, not per 256
+// at rank 8.  The shared-memory layout ([rank][rank2 + 2] for S, [2][tiles]
+// of M, [rank][rows + 2] for X) stays within the rank-64 layout.
+__host__ __device__ inline int solve_tile_rows(int rank) {
+    return rank <= 8 ? 256 : rank <= 16 ? 128 : rank <= 32 ? 64 : 32;
+}
 
 // One tile of X = M * S for a thread that owns column c0 of rows
 // r0 + j * rstep, j < NOUT; the k sum runs over pairs (k, k+1) in the two
@@ -408,11 +417,11 @@ __device__ __forceinline__ void solve_tile_cols(const float *SPTGB_RESTRICT Mt, 
                                                 const float *SPTGB_RESTRICT StN, const float *SPTGB_RESTRICT StL,
                                                 float *SPTGB_RESTRICT XT, float *SPTGB_RESTRICT XN, float *SPTGB_RESTRICT X,
                                                 uint64_t t0, uint32_t nrows, int rank2, int stride, int c0, int r0,
-                                                int rstep, int sexp) {
+                                                int rstep, int sexp, int ldk, int ldr) {
     float2 hi[NOUT], lo[NOUT];
 #pragma unroll
     for (int j = 0; j < NOUT; ++j) hi[j] = lo[j] = make_float2(0.f, 0.f);
-    const float *sh_p = StH + c0 * LDK, *sn_p = StN + c0 * LDK, *sl_p = StL + c0 * LDK;
+    const float *sh_p = StH + c0 * ldk, *sn_p = StN + c0 * ldk, *sl_p = StL + c0 * ldk;
 #pragma unroll 2
     for (int k = 0; k < rank2; k += 2) {
         const float2 sh = *reinterpret_cast<const float2 *>(sh_p + k);
@@ -420,7 +429,7 @@ __device__ __forceinline__ void solve_tile_cols(const float *SPTGB_RESTRICT Mt, 
         const float2 sl = *reinterpret_cast<const float2 *>(sl_p + k);
 #pragma unroll
         for (int j = 0; j < NOUT; ++j)
-            df2::fma_acc(hi[j], lo[j], *reinterpret_cast<const float2 *>(Mt + (r0 + j * rstep) * LDK + k), sh, sn, sl);
+            df2::fma_acc(hi[j], lo[j], *reinterpret_cast<const float2 *>(Mt + (r0 + j * rstep) * ldk + k), sh, sn, sl);
     }
 #pragma unroll
     for (int j = 0; j < NOUT; ++j) {
@@ -429,8 +438,8 @@ __device__ __forceinline__ void solve_tile_cols(const float *SPTGB_RESTRICT Mt, 
         const int r = r0 + j * rstep;
         const uint64_t row = t0 + r;
         const float xf = row < nrows ? __fadd_rn(h, l) : 0.f;
-        XT[c0 * LDR + r] = xf;   // the Gram and the column maxima use the scaled values
-        XN[c0 * LDR + r] = -xf;
+        XT[c0 * ldr + r] = xf;   // the Gram and the column maxima use the scaled values
+        XN[c0 * ldr + r] = -xf;
         if (row < nrows) X[row * stride + c0] = sexp ? scalbnf(xf, sexp) : xf;
     }
 }
@@ -439,46 +448,53 @@ __device__ __forceinline__ void solve_tile_cols(const float *SPTGB_RESTRICT Mt, 
 // solve_prepare_body, as hi and lo FP32 arrays), plus this block's partial of
 // X^T X (over the FP32 values written) and the column maxima.  Each output
 // element and each Gram entry is accumulated in double-float (packed FP32x2)
-// and rounded once: outputs to FP32, Gram partials to FP64.
-__device__ __forceinline__ void solve_rows_body(const float *SPTGB_RESTRICT M, float *SPTGB_RESTRICT X, uint32_t nrows, int rank, int stride,
+// and rounded once: outputs to FP32, Gram partials to FP64.  TRC: rows per
+// tile (solve_tile_rows of the rank), fixed per instantiation with the
+// layout of its rank class RC = 64 * 32 / TRC.
+template <int TRC>
+__device__ __forceinline__ void solve_rows_tiles(const float *SPTGB_RESTRICT M, float *SPTGB_RESTRICT X, uint32_t nrows, int rank, int stride,
              const double *SPTGB_RESTRICT S, const int *SPTGB_RESTRICT sstatus, double *SPTGB_RESTRICT gpart,
              double *SPTGB_RESTRICT mpart, unsigned bid, unsigned nbk) {
+    constexpr int RC = RMAX * TR / TRC;     // largest rank of the class
+    constexpr int tr = TRC;                 // rows per tile
+    constexpr int ldk = RC + 2;             // row length of the k-major tiles (even: 8-byte pairs)
+    constexpr int ldr = TRC + 2;            // row length of the transposed X tile
     const int sexp = inverse_exponent(*sstatus);
-    extern __shared__ float smf[];
-    float *StH = smf;                       // [RMAX][LDK]: S^T hi, k-major per column
-    float *StN = StH + RMAX * LDK;          // -hi
-    float *StL = StN + RMAX * LDK;          // lo
-    float *Mt2 = StL + RMAX * LDK;          // [2][TR][LDK]: row tiles of M, double-buffered
-    float *XT = Mt2 + 2 * TR * LDK;         // [RMAX][LDR]: tile of X, transposed
-    float *XN = XT + RMAX * LDR;            // -XT
-    __shared__ unsigned char pp_s[PMAX], qq_s[PMAX];
     const int P = rank * (rank + 1) / 2;
     const int RR = rank * rank;
     const int rank2 = (rank + 1) & ~1;
+    extern __shared__ float smf[];
+    float *StH = smf;                       // [RC][ldk]: S^T hi, k-major per column
+    float *StN = StH + RC * ldk;            // -hi
+    float *StL = StN + RC * ldk;            // lo
+    float *Mt2 = StL + RC * ldk;            // [2][tr][ldk]: row tiles of M, double-buffered
+    float *XT = Mt2 + 2 * tr * ldk;         // [RC][ldr]: tile of X, transposed
+    float *XN = XT + RC * ldr;              // -XT
+    __shared__ unsigned char pp_s[PMAX], qq_s[PMAX];
     // TR x rank2 floats of M from row t0 into dst as 8-byte cp.async chunks,
     // one commit group; rows past nrows and columns past rank read as zero
     // (source size 0 or 4 of the 8 bytes)
     auto load_tile = [&](float *dst, uint64_t t0) {
         const int half = rank2 / 2;
-        for (int e = threadIdx.x; e < TR * half; e += DT) {
+        for (int e = threadIdx.x; e < tr * half; e += DT) {
             const int r = e / half, c = 2 * (e % half);
             const uint64_t row = t0 + r;
             const unsigned bytes = row < nrows ? (c + 1 < rank ? 8u : (c < rank ? 4u : 0u)) : 0u;
             const float *src = bytes ? M + row * stride + c : M;
-            const unsigned dst_s = (unsigned)__cvta_generic_to_shared(dst + r * LDK + c);
+            const unsigned dst_s = (unsigned)__cvta_generic_to_shared(dst + r * ldk + c);
             asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(dst_s), "l"(src), "r"(bytes) : "memory");
         }
         asm volatile("cp.async.commit_group;" ::: "memory");
     };
     int cur = 0;
-    if ((uint64_t)bid * TR < nrows) load_tile(Mt2, (uint64_t)bid * TR);
+    if ((uint64_t)bid * tr < nrows) load_tile(Mt2, (uint64_t)bid * tr);
     const float *Sf = reinterpret_cast<const float *>(S);
     for (int e = threadIdx.x; e < rank * rank2; e += DT) {
         const int c = e / rank2, k = e % rank2;   // S[k][c]
         const float h = k < rank ? Sf[k * rank + c] : 0.f;
-        StH[c * LDK + k] = h;
-        StN[c * LDK + k] = -h;
-        StL[c * LDK + k] = k < rank ? Sf[RR + k * rank + c] : 0.f;
+        StH[c * ldk + k] = h;
+        StN[c * ldk + k] = -h;
+        StL[c * ldk + k] = k < rank ? Sf[RR + k * rank + c] : 0.f;
     }
     for (int i = threadIdx.x; i < P; i += DT) {
         int p, q;
@@ -493,13 +509,13 @@ __device__ __forceinline__ void solve_rows_body(const float *SPTGB_RESTRICT M, f
     // with rank | DT a thread keeps one column c0 and rows r0 + j * (DT / rank)
     const bool fixed_col = (DT % rank) == 0;
     const int c0 = threadIdx.x % rank, r0 = threadIdx.x / rank, rstep = DT / rank;
-    const int nout = (TR * rank + DT - 1) / DT;   // 1, 2, 4 or 8 when fixed_col
-    for (uint64_t t0 = (uint64_t)bid * TR; t0 < nrows; t0 += (uint64_t)nbk * TR) {
+    const int nout = (tr * rank + DT - 1) / DT;   // 1, 2, 4 or 8 when fixed_col
+    for (uint64_t t0 = (uint64_t)bid * tr; t0 < nrows; t0 += (uint64_t)nbk * tr) {
         // the next tile streams into the other buffer while this one is used;
         // that buffer was last read before the previous iteration's barrier
-        const float *Mt = Mt2 + cur * TR * LDK;
-        if (t0 + (uint64_t)nbk * TR < nrows) {
-            load_tile(Mt2 + (cur ^ 1) * TR * LDK, t0 + (uint64_t)nbk * TR);
+        const float *Mt = Mt2 + cur * tr * ldk;
+        if (t0 + (uint64_t)nbk * tr < nrows) {
+            load_tile(Mt2 + (cur ^ 1) * tr * ldk, t0 + (uint64_t)nbk * tr);
             asm volatile("cp.async.wait_group 1;" ::: "memory");
         } else {
             asm volatile("cp.async.wait_group 0;" ::: "memory");
@@ -507,18 +523,18 @@ __device__ __forceinline__ void solve_rows_body(const float *SPTGB_RESTRICT M, f
         cur ^= 1;
         __syncthreads();
         if (fixed_col) {
-            if (r0 < TR) {
+            if (r0 < tr) {
                 switch (nout) {
-                    case 8: solve_tile_cols<8>(Mt, StH, StN, StL, XT, XN, X, t0, nrows, rank2, stride, c0, r0, rstep, sexp); break;
-                    case 4: solve_tile_cols<4>(Mt, StH, StN, StL, XT, XN, X, t0, nrows, rank2, stride, c0, r0, rstep, sexp); break;
-                    case 2: solve_tile_cols<2>(Mt, StH, StN, StL, XT, XN, X, t0, nrows, rank2, stride, c0, r0, rstep, sexp); break;
-                    default: solve_tile_cols<1>(Mt, StH, StN, StL, XT, XN, X, t0, nrows, rank2, stride, c0, r0, rstep, sexp); break;
+                    case 8: solve_tile_cols<8>(Mt, StH, StN, StL, XT, XN, X, t0, nrows, rank2, stride, c0, r0, rstep, sexp, ldk, ldr); break;
+                    case 4: solve_tile_cols<4>(Mt, StH, StN, StL, XT, XN, X, t0, nrows, rank2, stride, c0, r0, rstep, sexp, ldk, ldr); break;
+                    case 2: solve_tile_cols<2>(Mt, StH, StN, StL, XT, XN, X, t0, nrows, rank2, stride, c0, r0, rstep, sexp, ldk, ldr); break;
+                    default: solve_tile_cols<1>(Mt, StH, StN, StL, XT, XN, X, t0, nrows, rank2, stride, c0, r0, rstep, sexp, ldk, ldr); break;
                 }
             }
         } else {
-            for (int e = threadIdx.x; e < TR * rank; e += DT)
+            for (int e = threadIdx.x; e < tr * rank; e += DT)
                 solve_tile_cols<1>(Mt, StH, StN, StL, XT, XN, X, t0, nrows, rank2, stride, e % rank, e / rank, 0,
-                                   sexp);
+                                   sexp, ldk, ldr);
         }
         __syncthreads();
         // Gram partial: this thread's pairs over row pairs (r, r+1)
@@ -526,17 +542,17 @@ __device__ __forceinline__ void solve_rows_body(const float *SPTGB_RESTRICT M, f
         for (int k = 0; k < PPT; ++k) {
             const int i = threadIdx.x + k * DT;
             if (i < P) {
-                const float *xp = XT + pp_s[i] * LDR, *xq = XT + qq_s[i] * LDR, *nq = XN + qq_s[i] * LDR;
+                const float *xp = XT + pp_s[i] * ldr, *xq = XT + qq_s[i] * ldr, *nq = XN + qq_s[i] * ldr;
 #pragma unroll 4
-                for (int r = 0; r < TR; r += 2)
+                for (int r = 0; r < tr; r += 2)
                     df2::prod_acc(ghi[k], glo[k], *reinterpret_cast<const float2 *>(xp + r),
                                   *reinterpret_cast<const float2 *>(xq + r), *reinterpret_cast<const float2 *>(nq + r));
                 df2::renorm(ghi[k], glo[k]);
             }
         }
         if (threadIdx.x < rank) {
-            for (int r = 0; r < TR; ++r)
-                if (t0 + r < nrows && XT[threadIdx.x * LDR + r] > cmax) cmax = XT[threadIdx.x * LDR + r];
+            for (int r = 0; r < tr; ++r)
+                if (t0 + r < nrows && XT[threadIdx.x * ldr + r] > cmax) cmax = XT[threadIdx.x * ldr + r];
         }
     }
 #pragma unroll
@@ -549,6 +565,17 @@ __device__ __forceinline__ void solve_rows_body(const float *SPTGB_RESTRICT M, f
         }
     }
     if (threadIdx.x < rank) mpart[(uint64_t)bid * rank + threadIdx.x] = ldexp((double)cmax, sexp);
+}
+
+__device__ __forceinline__ void solve_rows_body(const float *SPTGB_RESTRICT M, float *SPTGB_RESTRICT X, uint32_t nrows, int rank, int stride,
+             const double *SPTGB_RESTRICT S, const int *SPTGB_RESTRICT sstatus, double *SPTGB_RESTRICT gpart,
+             double *SPTGB_RESTRICT mpart, unsigned bid, unsigned nbk) {
+    switch (solve_tile_rows(rank)) {
+        case 256: solve_rows_tiles<256>(M, X, nrows, rank, stride, S, sstatus, gpart, mpart, bid, nbk); break;
+        case 128: solve_rows_tiles<128>(M, X, nrows, rank, stride, S, sstatus, gpart, mpart, bid, nbk); break;
+        case 64: solve_rows_tiles<64>(M, X, nrows, rank, stride, S, sstatus, gpart, mpart, bid, nbk); break;
+        default: solve_rows_tiles<32>(M, X, nrows, rank, stride, S, sstatus, gpart, mpart, bid, nbk); break;
+    }
 }
 
 // Reduces the solve statistics, forms lambda and the normalised Gram.
@@ -750,6 +777,15 @@ __device__ __forceinline__ void f32_to_bf16_body(const float *SPTGB_RESTRICT in,
             out[i] = (uint16_t)(u >> 16);
         }
     }
+}
+
+// Blocks of the row solve for nrows rows (the partials sptgb_normalize reduces).
+__host__ __device__ inline int nblocks_for_solve(uint64_t nrows, int rank) {
+    const int tr = solve_tile_rows(rank);
+    uint64_t b = (nrows + tr - 1) / tr;
+    if (b > (uint64_t)NBLK) b = NBLK;
+    if (b < 1) b = 1;
+    return (int)b;
 }
 
 __host__ __device__ inline int nblocks_for_rows(uint64_t nrows) {

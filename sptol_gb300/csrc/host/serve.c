@@ -267,7 +267,7 @@ static uint64_t solve_items(uint64_t rows, uint32_t tr) { return clamp_blocks(ro
 
 static void step_lists_build(sptgbServer *s) {
     for (int l = 0; l < NL_STEP; ++l) list_clear(s, l);
-    const uint32_t tr = sptgb_batch_rows_per_block(), fr = sptgb_batch_fit_rows_per_block();
+    const uint32_t fr = sptgb_batch_fit_rows_per_block();
     const uint32_t zr = sptgb_batch_zero_rows();
     for (uint32_t i = 0; i < s->cap; ++i) {
         if (s->slot_job[i] < 0 || s->jobs[s->slot_job[i]].state != JOB_ACTIVE) continue;
@@ -277,7 +277,7 @@ static void step_lists_build(sptgbServer *s) {
             list_add(s, NL_MT + 4 * (int)m + g, i, (d->nnz + s->ul[g] - 1) / s->ul[g]);
             list_add(s, NL_ZR + (int)m, i, ((uint64_t)d->ndims[m] + zr - 1) / zr);
             list_add(s, NL_ONE + (int)m, i, 1);
-            list_add(s, NL_DN + (int)m, i, solve_items(d->ndims[m], tr));
+            list_add(s, NL_DN + (int)m, i, solve_items(d->ndims[m], sptgb_batch_solve_tile_rows(d->rank)));
         }
         list_add(s, NL_FIT, i, clamp_blocks(d->ndims[d->nmodes - 1], fr));
         list_add(s, NL_FITONE, i, 1);

@@ -328,7 +328,7 @@ cudaError_t sptgb_grid_barrier_selftest(int missing, int *err, unsigned int *rou
 cudaError_t sptgb_batch_mttkrp(const sptgb_slot *slots, const sptgb_wlist *w, int mode, int group, uint32_t ul,
                                uint32_t sched, cudaStream_t s);
 /* Grid sizes the step uses, so that hosts size their prefix lists. */
-uint32_t sptgb_batch_rows_per_block(void);
+uint32_t sptgb_batch_solve_tile_rows(uint32_t rank);   /* rows per row-solve tile at this rank */
 uint32_t sptgb_batch_fit_rows_per_block(void);
 uint32_t sptgb_batch_zero_rows(void);
 uint32_t sptgb_batch_max_blocks(void);

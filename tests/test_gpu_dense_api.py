@@ -43,8 +43,12 @@ def test_dot_mul_seq_triangle_bitexact(N, rank, mode):
     assert np.array_equal(mats[N].array()[:rank, :rank], exp)
 
 
-@pytest.mark.parametrize("N,rank,mode", [(3, 16, 1), (4, 32, 3)])
+@pytest.mark.parametrize("N,rank,mode", [(3, 16, 1), (4, 32, 3), (3, 5, 0), (3, 8, 2), (4, 12, 1), (3, 24, 1),
+                                         (3, 64, 2), (4, 48, 0)])
 def test_solve_normals(N, rank, mode):
+    """Every row-tile class of the solve (256 / 128 / 64 / 32 rows for ranks
+    <= 8 / 16 / 32 / 64), with ranks that divide the block (one column per
+    thread) and ranks that do not."""
     rng = np.random.default_rng(7 + rank)
     gs = _grams(rng, N, rank)
     mats = [S.Matrix.from_array(g) for g in gs] + [S.Matrix(rank, rank)]
