@@ -29,6 +29,43 @@
 
 #define TRACE(name) SPTGB_TRACE_POINT(name, s, t_prev)
 
+/* SPTGB_TRACE=2: one line per host-buffer call with the host times at which
+ * its synchronising points returned and the device times of its copy and
+ * compute milestones, from timing events; unlike SPTGB_TRACE=1 it adds no
+ * synchronisation, so the call overlaps its work as it does untraced. */
+enum { T2_START, T2_KEY, T2_FIRST_H2D, T2_ARRAYS, T2_FACTORS, T2_KERNELS, T2_D2H, T2_NEV };
+enum { T2H_START, T2H_KEY, T2H_CHUNKS, T2H_END, T2_NHOST };
+static cudaEvent_t t2_ev[T2_NEV];
+static double t2_host[T2_NHOST];
+static int t2_on(void) {
+    static int on = -1;
+    if (on < 0) {
+        const char *e = getenv("SPTGB_TRACE");
+        on = e && e[0] == '2';
+    }
+    return on;
+}
+static void t2_event(int i, cudaStream_t st) {
+    if (!t2_on()) return;
+    if (!t2_ev[i]) cudaEventCreate(&t2_ev[i]);
+    cudaEventRecord(t2_ev[i], st);
+}
+static void t2_mark(int i) {
+    if (t2_on()) t2_host[i] = sptgb_wall();
+}
+static void t2_print(sptIndex mode) {
+    if (!t2_on()) return;
+    float d[T2_NEV] = {0};
+    for (int i = 1; i < T2_NEV; ++i)
+        if (t2_ev[i] && cudaEventElapsedTime(&d[i], t2_ev[T2_START], t2_ev[i]) != cudaSuccess) d[i] = -1.f;
+    fprintf(stderr,
+            "[sptgb trace2] mode %u host: key %.2f chunks %.2f end %.2f ms | device: key %.2f first h2d %.2f "
+            "arrays %.2f factors %.2f kernels %.2f d2h %.2f ms\n",
+            (unsigned)mode, (t2_host[T2H_KEY] - t2_host[T2H_START]) * 1e3,
+            (t2_host[T2H_CHUNKS] - t2_host[T2H_START]) * 1e3, (t2_host[T2H_END] - t2_host[T2H_START]) * 1e3,
+            d[T2_KEY], d[T2_FIRST_H2D], d[T2_ARRAYS], d[T2_FACTORS], d[T2_KERNELS], d[T2_D2H]);
+}
+
 static int check_mats(sptIndex nmodes, const sptIndex *ndims, sptMatrix *mats[], sptIndex mode, const char *module) {
     if (nmodes < 2 || nmodes > SPTGB_MAX_MODES || mode >= nmodes) {
         spt_ComplainError(module, SPTERR_VALUE_ERROR, __FILE__, __LINE__, "unsupported order or mode");
@@ -127,6 +164,8 @@ static int mttkrp_host_locked(sptSparseTensor const *X, sptMatrix *mats[], sptIn
 
         /* 1. the output coordinates first: the range check, the sortedness
          *    check and the sort need only them. */
+        t2_mark(T2H_START);
+        t2_event(T2_START, s);
         SPTGB_CUDA(cudaMemcpyAsync(din[mode], X->inds[mode].data, n * sizeof(uint32_t), cudaMemcpyHostToDevice, s),
                    module);
         {
@@ -137,6 +176,7 @@ static int mttkrp_host_locked(sptSparseTensor const *X, sptMatrix *mats[], sptIn
             SPTGB_CUDA(cudaMemsetAsync(dflag + 2, 0, sizeof(unsigned int), s), module);
             SPTGB_CUDA(cudaMemcpyAsync(hflag, dflag, 2 * sizeof(unsigned int), cudaMemcpyDeviceToHost, s), module);
             SPTGB_CUDA(cudaEventRecord(g_ws.ev[0], s), module);
+            t2_event(T2_KEY, s);
         }
         /* 2. the other arrays and the factor matrices on the copy stream;
          *    the first one goes while the checks above run. */
@@ -156,8 +196,10 @@ static int mttkrp_host_locked(sptSparseTensor const *X, sptMatrix *mats[], sptIn
             if (bytes) src[nup] = mats[pm]->values, dst[nup] = g_ws.fac[pm].ptr, len[nup++] = bytes;
         }
         SPTGB_CUDA(cudaMemcpyAsync(dst[0], src[0], len[0], cudaMemcpyHostToDevice, cs), module);
+        t2_event(T2_FIRST_H2D, cs);
         cudaError_t e = cudaEventSynchronize(g_ws.ev[0]);
         if (e != cudaSuccess) return drain_copies(sptgb_cuda_fail(e, module, __FILE__, __LINE__));
+        t2_mark(T2H_KEY);
         TRACE("h2d key");
         if (hflag[0]) {
             spt_ComplainError(module, SPTERR_VALUE_ERROR, __FILE__, __LINE__,
@@ -184,6 +226,7 @@ static int mttkrp_host_locked(sptSparseTensor const *X, sptMatrix *mats[], sptIn
             if (e != cudaSuccess) return drain_copies(sptgb_cuda_fail(e, module, __FILE__, __LINE__));
         }
         e = cudaEventRecord(g_ws.ev[2], cs);
+        t2_event(T2_ARRAYS, cs);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(s, g_ws.ev[2], 0);
         if (e != cudaSuccess) return drain_copies(sptgb_cuda_fail(e, module, __FILE__, __LINE__));
 
@@ -220,6 +263,7 @@ static int mttkrp_host_locked(sptSparseTensor const *X, sptMatrix *mats[], sptIn
             if (e != cudaSuccess) return drain_copies(sptgb_cuda_fail(e, module, __FILE__, __LINE__));
         }
         e = cudaEventRecord(g_ws.ev[1], cs);
+        t2_event(T2_FACTORS, cs);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(s, g_ws.ev[1], 0);
         if (e != cudaSuccess) return drain_copies(sptgb_cuda_fail(e, module, __FILE__, __LINE__));
         TRACE("h2d rest");
@@ -258,6 +302,7 @@ static int mttkrp_host_locked(sptSparseTensor const *X, sptMatrix *mats[], sptIn
         const int nchunk = recs && tmpI && n >= CHUNKED_MIN_NNZ ? OUT_CHUNKS : 1;
         if (nchunk == 1) {
             SPTGB_CUDA(sptgb_mttkrp_coo(&a, s), module);
+            t2_event(T2_KERNELS, s);
             TRACE("kernel");
             if (recs)
                 SPTGB_CUDA(cudaMemcpyAsync(hflag + 2, dflag + 2, sizeof(unsigned int), cudaMemcpyDeviceToHost, s),
@@ -279,6 +324,7 @@ static int mttkrp_host_locked(sptSparseTensor const *X, sptMatrix *mats[], sptIn
                        module);
             SPTGB_CUDA(cudaMemsetAsync(g_ws.out.ptr, 0, (size_t)tmpI * stride * sizeof(float), s), module);
             SPTGB_CUDA(cudaStreamSynchronize(s), module);
+            t2_mark(T2H_CHUNKS);
             uint64_t ub[OUT_CHUNKS + 1];
             uint32_t last[OUT_CHUNKS];
             ub[0] = 0, last[0] = 0, ub[nchunk] = nunits;
@@ -295,6 +341,7 @@ static int mttkrp_host_locked(sptSparseTensor const *X, sptMatrix *mats[], sptIn
                 if (ub[c] < ub[c + 1]) SPTGB_CUDA(sptgb_mttkrp_coo(&a, s), module);
                 SPTGB_CUDA(cudaEventRecord(g_ws.cev[c], s), module);
             }
+            t2_event(T2_KERNELS, s);
             SPTGB_CUDA(cudaMemcpyAsync(hflag + 2, dflag + 2, sizeof(unsigned int), cudaMemcpyDeviceToHost, s),
                        module);
             uint32_t hi = tmpI;
@@ -310,6 +357,7 @@ static int mttkrp_host_locked(sptSparseTensor const *X, sptMatrix *mats[], sptIn
                 }
                 hi = lo;
             }
+            t2_event(T2_D2H, cs);
             SPTGB_CUDA(cudaStreamSynchronize(cs), module);
         }
     }
@@ -318,6 +366,10 @@ static int mttkrp_host_locked(sptSparseTensor const *X, sptMatrix *mats[], sptIn
                                    cudaMemcpyDeviceToHost, s),
                    module);
     SPTGB_CUDA(cudaStreamSynchronize(s), module);
+    if (n) {
+        t2_mark(T2H_END);
+        t2_print(mode);
+    }
     TRACE("d2h out");
     if (n && (N == 3 || N == 4) && g_ws.hflag[2]) {
         spt_ComplainError(module, SPTERR_VALUE_ERROR, __FILE__, __LINE__,
