@@ -152,17 +152,16 @@ int g_blocks = 0;   // resident blocks of k_b_step (0: not yet sized, <0: unsupp
 // cooperative launch that does not fit rather than running it.
 extern "C" cudaError_t sptgb_batch_step_persistent(const sptgb_slot *slots, const sptgb_step_lists *L,
                                                    sptgb_grid_bar *bar, cudaStream_t s) {
+    // sized once; two threads sizing it at the same time store the same value
     if (g_blocks == 0) {
-        int dev = 0, coop = 0, per = 0;
-        g_blocks = -1;
-        if (cudaGetDevice(&dev) != cudaSuccess) return cudaErrorNotSupported;
-        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
-        if (!coop) return cudaErrorNotSupported;
-        if (cudaFuncSetAttribute(k_b_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SOLVE_SMEM) != cudaSuccess)
-            return cudaErrorNotSupported;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_b_step, BT, SOLVE_SMEM) != cudaSuccess || per < 1)
-            return cudaErrorNotSupported;
-        g_blocks = (per < 2 ? per : 2) * sptgb_sm_count();
+        int dev = 0, coop = 0, per = 0, blocks = -1;
+        if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) ==
+                                                      cudaSuccess && coop &&
+            cudaFuncSetAttribute(k_b_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SOLVE_SMEM) ==
+                cudaSuccess &&
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_b_step, BT, SOLVE_SMEM) == cudaSuccess && per >= 1)
+            blocks = (per < 2 ? per : 2) * sptgb_sm_count();
+        g_blocks = blocks;
     }
     if (g_blocks < 0) return cudaErrorNotSupported;
     cudaLaunchConfig_t cfg = {};
