@@ -270,9 +270,10 @@ def run_served(reqs, tensors, inits, outs, poisson, keep_fits):
     launches = S.launch_count() - n0
     units = {g: srv.schedule(g) for g in range(4)}
     persistent = srv.persistent()
+    step_kernels = srv.step_kernels()
     srv.free()
     return {"solves_per_s": n / span, "makespan_s": span, "lat": lat, "fits": fits, "steps": steps,
-            "launches": int(launches), "schedules": units, "persistent": persistent,
+            "launches": int(launches), "schedules": units, "persistent": persistent, "step_kernels": step_kernels,
             "host_s": {"submit": round(t_sub, 3), "step": round(t_step, 3), "poll": round(t_poll, 3)}}
 
 
@@ -451,17 +452,21 @@ def serve_leg(args):
         "served": {"solves_per_s": round(served["solves_per_s"], 1), "p50_ms": pct(served["lat"], 50),
                    "p99_ms": pct(served["lat"], 99), "makespan_s": round(served["makespan_s"], 3),
                    "steps": served["steps"], "gpu_launches": served["launches"],
+                   "kernels_per_als_step": served["step_kernels"],
                    "mttkrp_schedule_by_rank": {"<=%d" % (8 << g): v for g, v in served["schedules"].items()},
                    "persistent_step": served["persistent"],
                    "host_s": served["host_s"]},
         "batched": {"solves_per_s": round(batched["solves_per_s"], 1), "p50_ms": pct(batched["lat"], 50),
                     "p99_ms": pct(batched["lat"], 99), "makespan_s": round(batched["makespan_s"], 3),
                     "steps": batched["steps"], "gpu_launches": batched["launches"],
+                    "kernels_per_als_step": batched["step_kernels"],
                     "mttkrp_schedule_by_rank": {"<=%d" % (8 << g): v for g, v in batched["schedules"].items()},
                     "persistent_step": batched["persistent"], "host_s": batched["host_s"]},
         "batched_persistent_step": {
             "solves_per_s": round(pers["solves_per_s"], 1), "makespan_s": round(pers["makespan_s"], 3),
             "steps": pers["steps"], "gpu_launches": pers["launches"], "persistent_step": pers["persistent"],
+            "kernels_per_als_step": pers["step_kernels"],
+            "launches_note": "gpu_launches also counts admission (sorts, packing, Grams) and retirement kernels",
             "max_fit_diff_vs_batched": max(pdiff) if pdiff else None,
             "what": "the batched run with each ALS step as one persistent cooperative kernel"},
         "plain": {"solves_per_s": round(plain["solves_per_s"], 1), "p50_ms": pct(plain["lat"], 50),

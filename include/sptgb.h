@@ -168,6 +168,10 @@ uint32_t sptgbServerUnitLength(const sptgbServer *s, int group);
  * launches), 0 when it runs as the kernel sequence (the default); meaningful
  * after the first step. */
 int sptgbServerPersistent(const sptgbServer *s);
+/* Kernels one ALS step launches (the nodes of the captured step graph: 1 for
+ * the persistent step, one per phase and lane group for the sequence); 0
+ * before the first step.  Admission and retirement kernels are not counted. */
+uint32_t sptgbServerStepKernels(const sptgbServer *s);
 /* The MTTKRP schedule the autotuner chose for rank group `group` (0..3: rank
  * <= 8, 16, 32, 64): unit length in nonzeros, deep (1) or shallow (0) record
  * batches, blocks per SM the kernel's registers are sized for (2 or 3; the

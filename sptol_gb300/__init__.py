@@ -234,6 +234,7 @@ def _declare(L):
         "sptgbServerBytesInUse": (C.c_size_t, [C.c_void_p]),
         "sptgbServerUnitLength": (C.c_uint32, [C.c_void_p, C.c_int]),
         "sptgbServerPersistent": (C.c_int, [C.c_void_p]),
+        "sptgbServerStepKernels": (C.c_uint32, [C.c_void_p]),
         "sptgbServerSchedule": (C.c_int, [C.c_void_p, C.c_int, u32p, u32p, u32p, C.POINTER(C.c_int)]),
         "sptgbGridBarrierSelfTest": (C.c_int, [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_uint)]),
         "sptgbServerFree": (None, [C.c_void_p]),
@@ -643,6 +644,10 @@ class Server:
                "sptgbServerSchedule")
         return {"unit": int(ul.value), "batches": "deep" if deep.value else "shallow",
                 "blocks_per_sm": int(bps.value), "source": {1: "cached", 0: "timed", -1: "no jobs"}[src.value]}
+
+    def step_kernels(self):
+        """Kernels one ALS step launches (0 before the first step)."""
+        return int(lib().sptgbServerStepKernels(self.h))
 
     def persistent(self):
         """True when each step runs as one persistent cooperative kernel."""

@@ -938,6 +938,7 @@ size_t sptgbServerBytesInUse(const sptgbServer *s) { return s->used; }
 
 uint32_t sptgbServerUnitLength(const sptgbServer *s, int group) { return group >= 0 && group < 4 ? s->ul[group] : 0; }
 int sptgbServerPersistent(const sptgbServer *s) { return s->persistent; }
+uint32_t sptgbServerStepKernels(const sptgbServer *s) { return s->have_graph ? s->graph_kernels : 0; }
 
 int sptgbServerSchedule(const sptgbServer *s, int group, uint32_t *unit_len, uint32_t *deep, uint32_t *blocks_per_sm,
                         int *from_cache) {

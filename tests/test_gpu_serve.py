@@ -140,6 +140,7 @@ def _run_mix(step_kind, niters=5):
         out = [srv.result(k) for k in tickets]
         launches = S.launch_count() - n0
         kind = srv.persistent()
+        assert srv.step_kernels() == (1 if kind else 38)
         srv.free()
         return out, kind, launches, steps
     finally:
