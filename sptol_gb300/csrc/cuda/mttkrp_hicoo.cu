@@ -249,8 +249,10 @@ struct Win2Ctx {
 
 // One worker's positions [r_beg, r_end) of the blocks [klo, khi) of the
 // schedule.  TILE: rows are window rows (row0 + r) summed in `tile`;
-// otherwise output rows, flushed with vector atomics.
-template <int W, bool TILE>
+// otherwise output rows, flushed with vector atomics.  FULL: the stride is
+// exactly 4W columns, so every lane holds real columns and the factor rows
+// are gathered without a select (an empty record carries rows 0, in range).
+template <int W, bool TILE, bool FULL>
 __device__ __forceinline__ void win2_range(const sptgb_hicoo_args &a, const Win2Ctx &x, uint4 *s_rec, float *tile,
                                            uint32_t row0, uint64_t klo, uint64_t khi, uint32_t r_beg,
                                            uint32_t r_end) {
@@ -258,7 +260,7 @@ __device__ __forceinline__ void win2_range(const sptgb_hicoo_args &a, const Win2
     uint32_t cur = NONE;
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     auto put = [&]() {
-        if (cur == NONE || !x.col_ok) return;
+        if (cur == NONE || (!FULL && !x.col_ok)) return;
         if (TILE) {
             // worker k adds its four columns starting at column k mod 4: at
             // each step the workers of a warp hit four different bank classes
@@ -348,11 +350,16 @@ __device__ __forceinline__ void win2_range(const sptgb_hicoo_args &a, const Win2
             for (int t = 0; t < EB; ++t) q4[t] = s_rec[x.wk * W + j0 + t];
 #pragma unroll
             for (int t = 0; t < EB; ++t) {
-                const bool use = q4[t].x != NONE && x.col_ok;
-                fa[t] = use ? __ldg(reinterpret_cast<const float4 *>(x.Fa + (size_t)q4[t].y * x.rb))
-                            : make_float4(0.f, 0.f, 0.f, 0.f);
-                fb[t] = use ? __ldg(reinterpret_cast<const float4 *>(x.Fb + (size_t)q4[t].z * x.rb))
-                            : make_float4(0.f, 0.f, 0.f, 0.f);
+                if (FULL) {
+                    fa[t] = __ldg(reinterpret_cast<const float4 *>(x.Fa + (size_t)q4[t].y * x.rb));
+                    fb[t] = __ldg(reinterpret_cast<const float4 *>(x.Fb + (size_t)q4[t].z * x.rb));
+                } else {
+                    const bool use = q4[t].x != NONE && x.col_ok;
+                    fa[t] = use ? __ldg(reinterpret_cast<const float4 *>(x.Fa + (size_t)q4[t].y * x.rb))
+                                : make_float4(0.f, 0.f, 0.f, 0.f);
+                    fb[t] = use ? __ldg(reinterpret_cast<const float4 *>(x.Fb + (size_t)q4[t].z * x.rb))
+                                : make_float4(0.f, 0.f, 0.f, 0.f);
+                }
             }
 #pragma unroll
             for (int t = 0; t < EB; ++t) {
@@ -374,7 +381,7 @@ __device__ __forceinline__ void win2_range(const sptgb_hicoo_args &a, const Win2
     put();
 }
 
-template <int W>
+template <int W, bool FULL>
 __global__ void __launch_bounds__(BLOCK, 5) k_hicoo_win2(sptgb_hicoo_args a, uint32_t chunk, uint32_t total) {
     extern __shared__ float tile[];   // [1 << sb][stride]
     constexpr int NWARP = BLOCK / 32;
@@ -443,7 +450,7 @@ __global__ void __launch_bounds__(BLOCK, 5) k_hicoo_win2(sptgb_hicoo_args a, uin
             const uint32_t s0 = q, s1 = hi < rend ? hi : rend;
             const uint32_t per = (s1 - s0 + NWC - 1) / NWC;
             const uint32_t r_beg = s0 + min(s1 - s0, gw * per);
-            win2_range<W, false>(a, x, s_rec[warp], tile, 0u, k0, kend, r_beg, min(s1, r_beg + per));
+            win2_range<W, false, FULL>(a, x, s_rec[warp], tile, 0u, k0, kend, r_beg, min(s1, r_beg + per));
             q = s1;
             w = wh;
             continue;
@@ -452,7 +459,7 @@ __global__ void __launch_bounds__(BLOCK, 5) k_hicoo_win2(sptgb_hicoo_args a, uin
         const uint32_t row0 = a.binds[mode][a.perm[k0]] << a.sb_bits;
         const uint32_t per = (s1 - s0 + NWC - 1) / NWC;
         const uint32_t r_beg = s0 + min(s1 - s0, gw * per);
-        win2_range<W, true>(a, x, s_rec[warp], tile, row0, k0, k1, r_beg, min(s1, r_beg + per));
+        win2_range<W, true, FULL>(a, x, s_rec[warp], tile, row0, k0, k1, r_beg, min(s1, r_beg + per));
         __syncthreads();
         // one write of the window: plain when this CTA covered all of it
         const bool owned = s0 == wbeg && s1 == wend;
@@ -485,8 +492,8 @@ __global__ void k_block_sizes(const uint32_t *__restrict__ perm, const uint64_t 
         sizes[k] = (uint32_t)(bptr[perm[k] + 1] - bptr[perm[k]]);
 }
 
-template <int W>
-cudaError_t launch_win2(const sptgb_hicoo_args &a, cudaStream_t s) {
+template <int W, bool FULL>
+cudaError_t launch_win2_k(const sptgb_hicoo_args &a, cudaStream_t s) {
     static int nsm = 0;
     const size_t smem = ((size_t)1 << a.sb_bits) * a.stride * sizeof(float);
     if (smem > 180 * 1024) return cudaErrorInvalidValue;
@@ -494,19 +501,24 @@ cudaError_t launch_win2(const sptgb_hicoo_args &a, cudaStream_t s) {
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        cudaFuncSetAttribute(k_hicoo_win2<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, 180 * 1024);
+        cudaFuncSetAttribute(k_hicoo_win2<W, FULL>, cudaFuncAttributeMaxDynamicSharedMemorySize, 180 * 1024);
     }
     int per = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_hicoo_win2<W>, BLOCK, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_hicoo_win2<W, FULL>, BLOCK, smem);
     if (per < 1) per = 1;
     if (a.nnz == 0 || a.nnz >= 0xffffffffull) return a.nnz ? cudaErrorInvalidValue : cudaSuccess;
     const uint32_t total = (uint32_t)a.nnz;
     const uint64_t grid = (uint64_t)nsm * per * 2;
     const uint32_t chunk = (uint32_t)((total + grid - 1) / grid);
     const uint32_t ngrid = (total + chunk - 1) / chunk;
-    k_hicoo_win2<W><<<ngrid, BLOCK, smem, s>>>(a, chunk, total);
+    k_hicoo_win2<W, FULL><<<ngrid, BLOCK, smem, s>>>(a, chunk, total);
     sptgb_count_launch(1);
     return cudaGetLastError();
+}
+
+template <int W>
+cudaError_t launch_win2(const sptgb_hicoo_args &a, cudaStream_t s) {
+    return a.stride == 4u * W ? launch_win2_k<W, true>(a, s) : launch_win2_k<W, false>(a, s);
 }
 
 template <int W, int NP>
