@@ -242,7 +242,8 @@ void sptSparseTensorStatusHiCOO(sptSparseTensorHiCOO *hitsr, FILE *fp) {
     bytes += (hitsr->bptr.len + hitsr->kptr.len + hitsr->cptr.len) * sizeof(sptNnzIndex);
     for (sptIndex m = 0; m < N; ++m) {
         const sptIndex kdim = (hitsr->ndims[m] + sk - 1) / sk;
-        for (sptIndex i = 0; i < kdim; ++i) bytes += (sptNnzIndex)hitsr->kschr[m][i].len * sizeof(sptIndex);
+        if (hitsr->kschr && hitsr->kschr[m])   /* absent before a conversion filled them */
+            for (sptIndex i = 0; i < kdim; ++i) bytes += (sptNnzIndex)hitsr->kschr[m][i].len * sizeof(sptIndex);
         bytes += kdim * sizeof(sptIndexVector *);
     }
     bytes += N * sizeof(sptIndexVector **) + N * sizeof(sptIndex);
@@ -252,7 +253,7 @@ void sptSparseTensorStatusHiCOO(sptSparseTensorHiCOO *hitsr, FILE *fp) {
     fprintf(fp, "SCHEDULE INFO [KERNEL]: \n");
     for (sptIndex m = 0; m < N; ++m)
         fprintf(fp, "SCHEDULE MODE %" PARTI_PRI_INDEX " : %" PARTI_PRI_INDEX " x %" PARTI_PRI_INDEX "\n", m,
-                (hitsr->ndims[m] + sk - 1) / sk, hitsr->nkiters[m]);
+                (hitsr->ndims[m] + sk - 1) / sk, hitsr->nkiters ? hitsr->nkiters[m] : 0);
     sptNnzIndex mx = 0, mn = 0, sum = 0, med = 0;
     double geo = 1.0;
     fprintf(fp, "block nnzs:\n");
