@@ -128,3 +128,44 @@ def test_dump_tensor_and_matrix_equal_the_reference_bytes(tmp_path, start):
                   L.sptDumpNnzIndexArray(nb.ctypes.data_as(S.u64p), len(nb), fp))
     O.ref_dump_arrays(ia, nb, ref_path)
     assert mine == open(ref_path).read()
+
+
+def test_hicoo_status_equals_the_reference(tmp_path):
+    """sptSparseTensorStatusHiCOO (hicoo/status.c:28-118) of one HiCOO
+    container printed by both libraries, line for line: sizes, storage,
+    schedule per mode, block-size statistics and the suggested parameters."""
+    O = _ref_or_skip()
+    R, L = O.ref(), S.lib()
+    H = C.POINTER(S.HiCOOS)
+    for lib in (R, L):
+        lib.sptNewSparseTensorHiCOO.argtypes = [H, C.c_uint32, S.u32p, C.c_uint64, C.c_uint8, C.c_uint8, C.c_uint8]
+        lib.sptSparseTensorStatusHiCOO.argtypes = [H, C.c_void_p]
+        lib.sptSparseTensorStatusHiCOO.restype = None
+    L.sptFreeSparseTensorHiCOO.argtypes = [H]
+    rng = np.random.default_rng(5)
+    ndims, nnz, sb, sk, sc = [300, 200, 100], 1000, 3, 6, 10
+    h = S.HiCOOS()
+    nd = (C.c_uint32 * 3)(*ndims)
+    assert L.sptNewSparseTensorHiCOO(C.byref(h), 3, nd, nnz, sb, sk, sc) == 0
+    sizes = []
+    while sum(sizes) < nnz:
+        sizes.append(int(min(rng.integers(1, 12), nnz - sum(sizes))))
+    pos = 0
+    assert L.sptAppendNnzIndexVector(C.byref(h.bptr), 0) == 0
+    for n in sizes:
+        pos += n
+        assert L.sptAppendNnzIndexVector(C.byref(h.bptr), pos) == 0
+    for m in range(3):
+        for _ in sizes:
+            assert L.sptAppendBlockIndexVector(C.byref(h.binds[m]), int(rng.integers(0, ndims[m] >> sb))) == 0
+        for i in range((ndims[m] + (1 << sk) - 1) >> sk):
+            for _ in range(int(rng.integers(0, 4))):
+                assert L.sptAppendIndexVector(C.byref(h.kschr[m][i]), int(rng.integers(0, 50))) == 0
+        h.nkiters[m] = int(rng.integers(1, 9))
+    for v in (0, 17, len(sizes)):
+        assert L.sptAppendNnzIndexVector(C.byref(h.kptr), v) == 0
+        assert L.sptAppendNnzIndexVector(C.byref(h.cptr), v) == 0
+    mine = _write(tmp_path, lambda fp: L.sptSparseTensorStatusHiCOO(C.byref(h), fp) or 0)
+    ref = _write(tmp_path, lambda fp: R.sptSparseTensorStatusHiCOO(C.byref(h), fp) or 0)
+    L.sptFreeSparseTensorHiCOO(C.byref(h))
+    assert mine == ref and "Nnzb: Max=" in mine
