@@ -230,7 +230,7 @@ __global__ void __launch_bounds__(BLOCK) k_hicoo_win(sptgb_hicoo_args a, uint32_
 //    decoded records {row, row of factor a, row of factor b, value} go through
 //    shared memory to the worker, which issues the factor-row gathers of a
 //    batch of them before using any.
-//  * Windows: only heavy windows (at least SPTGB_HICOO_HEAVY nonzeros, the
+//  * Windows: only heavy windows (at least heavy_nnz nonzeros, the
 //    hot rows of a power-law mode) are summed in the shared-memory tile and
 //    written once.  A run of consecutive light windows is one flat range: the
 //    running row sum of a worker goes to the output with a vector atomic when
@@ -240,7 +240,7 @@ struct Win2Ctx {
     const uint8_t *e_m, *e_a, *e_b;
     const uint32_t *b_m, *b_a, *b_b;
     const char *Fa, *Fb;
-    size_t rb;
+    uint32_t rb;      // bytes per factor row (stride * 4 <= 512)
     uint32_t lim_a, lim_b, rows_w, st;
     int sl, wk, c0;
     bool col_ok, m0, m1, m2, m3;
@@ -250,9 +250,11 @@ struct Win2Ctx {
 // One worker's positions [r_beg, r_end) of the blocks [klo, khi) of the
 // schedule.  TILE: rows are window rows (row0 + r) summed in `tile`;
 // otherwise output rows, flushed with vector atomics.  FULL: the stride is
-// exactly 4W columns, so every lane holds real columns and the factor rows
+// exactly 4W columns, so every lane holds stored columns and the factor rows
 // are gathered without a select (an empty record carries rows 0, in range).
-template <int W, bool TILE, bool FULL>
+// AC (with FULL): the rank equals the stride, so no column is padding and the
+// row flushes need no column masks.
+template <int W, bool TILE, bool FULL, bool AC>
 __device__ __forceinline__ void win2_range(const sptgb_hicoo_args &a, const Win2Ctx &x, uint4 *s_rec, float *tile,
                                            uint32_t row0, uint64_t klo, uint64_t khi, uint32_t r_beg,
                                            uint32_t r_end) {
@@ -271,20 +273,25 @@ __device__ __forceinline__ void win2_range(const sptgb_hicoo_args &a, const Win2
             if (x.wk & 1) v = make_float4(v.y, v.z, v.w, v.x);
             if (x.wk & 2) v = make_float4(v.z, v.w, v.x, v.y);
             const int r = x.wk & 3;
-            if (x.mrot & 1) atomicAdd(t + (r & 3), v.x);
-            if (x.mrot & 2) atomicAdd(t + ((r + 1) & 3), v.y);
-            if (x.mrot & 4) atomicAdd(t + ((r + 2) & 3), v.z);
-            if (x.mrot & 8) atomicAdd(t + ((r + 3) & 3), v.w);
+            if (AC || (x.mrot & 1)) atomicAdd(t + (r & 3), v.x);
+            if (AC || (x.mrot & 2)) atomicAdd(t + ((r + 1) & 3), v.y);
+            if (AC || (x.mrot & 4)) atomicAdd(t + ((r + 2) & 3), v.z);
+            if (AC || (x.mrot & 8)) atomicAdd(t + ((r + 3) & 3), v.w);
         } else {
-            const float4 v = make_float4(x.m0 ? acc.x : 0.f, x.m1 ? acc.y : 0.f, x.m2 ? acc.z : 0.f,
-                                         x.m3 ? acc.w : 0.f);
+            const float4 v = AC ? acc
+                                : make_float4(x.m0 ? acc.x : 0.f, x.m1 ? acc.y : 0.f, x.m2 ? acc.z : 0.f,
+                                              x.m3 ? acc.w : 0.f);
             atomicAdd(reinterpret_cast<float4 *>(a.out + (size_t)cur * x.st) + x.sl, v);
         }
     };
-    uint64_t kb = klo;
+    // block positions and element offsets fit in 32 bits: the launcher
+    // takes this kernel only for nb and nnz below 2^32 - 2^12, and bptr was
+    // checked to rise from 0 to nnz
+    const uint32_t khi32 = (uint32_t)khi;
+    uint32_t kb = (uint32_t)klo;
     uint32_t kst = 0;
     if (r_beg < r_end) {
-        kb = block_at(a.pnnz, klo, khi, r_beg);
+        kb = (uint32_t)block_at(a.pnnz, klo, khi, r_beg);
         kst = a.pnnz[kb];
     }
     const uint32_t rounds = __reduce_max_sync(0xffffffffu, (r_end - r_beg + W - 1) / W);
@@ -295,14 +302,14 @@ __device__ __forceinline__ void win2_range(const sptgb_hicoo_args &a, const Win2
         // the W boundaries the worker's lanes load; boundaries past khi read
         // as 0xffffffff, so the loop ends after at most (khi - kb) / W + 1
         // rounds (more than one only when blocks are empty)
-        uint64_t myk = kb;
+        uint32_t myk = kb;
         uint32_t mystart = kst;
         bool todo = valid;
-        uint64_t base = kb;
+        uint32_t base = kb;
         uint32_t bstart = kst;
         for (uint32_t guard = 0; guard < (1u << 26) && __any_sync(0xffffffffu, todo); ++guard) {
-            const uint64_t idx = base + 1 + x.sl;
-            const uint32_t bv = idx <= khi ? a.pnnz[idx] : 0xffffffffu;
+            const uint32_t idx = base + 1 + x.sl;
+            const uint32_t bv = idx <= khi32 ? a.pnnz[idx] : 0xffffffffu;
             uint32_t c = 0;
 #pragma unroll
             for (int step = W / 2; step >= 1; step >>= 1) {
@@ -323,7 +330,7 @@ __device__ __forceinline__ void win2_range(const sptgb_hicoo_args &a, const Win2
         uint4 r = make_uint4(NONE, 0u, 0u, 0u);
         if (valid && !todo) {
             const uint32_t b = a.perm[myk];
-            const uint64_t e = a.bptr[b] + (p - mystart);
+            const uint32_t e = (uint32_t)a.bptr[b] + (p - mystart);
             bool ok = e < a.nnz;
             if (ok) {
                 const uint32_t rl = x.e_m[e];
@@ -381,7 +388,7 @@ __device__ __forceinline__ void win2_range(const sptgb_hicoo_args &a, const Win2
     put();
 }
 
-template <int W, bool FULL>
+template <int W, bool FULL, bool AC>
 __global__ void __launch_bounds__(BLOCK, 5) k_hicoo_win2(sptgb_hicoo_args a, uint32_t chunk, uint32_t total) {
     extern __shared__ float tile[];   // [1 << sb][stride]
     constexpr int NWARP = BLOCK / 32;
@@ -416,7 +423,7 @@ __global__ void __launch_bounds__(BLOCK, 5) k_hicoo_win2(sptgb_hicoo_args a, uin
     x.lim_b = a.ndims[pb];
     x.Fa = reinterpret_cast<const char *>(a.fac[pa]) + (size_t)x.sl * 16;
     x.Fb = reinterpret_cast<const char *>(a.fac[pb]) + (size_t)x.sl * 16;
-    x.rb = (size_t)x.st * 4;
+    x.rb = x.st * 4u;
     const uint32_t st4 = x.st / 4;
     const uint32_t gw = (uint32_t)(warp * NWK + x.wk);
 
@@ -436,7 +443,7 @@ __global__ void __launch_bounds__(BLOCK, 5) k_hicoo_win2(sptgb_hicoo_args a, uin
     while (q < hi) {
         const uint64_t k0 = a.wst[w], k1 = a.wst[w + 1];
         const uint32_t wbeg = a.pnnz[k0], wend = a.pnnz[k1];
-        if (wend - wbeg < SPTGB_HICOO_HEAVY) {
+        if (wend - wbeg < a.heavy_nnz) {
             // a run of light windows, up to the next heavy one
             uint32_t hl = 0, hh = a.nheavy;   // first heavy window > w
             while (hl < hh) {
@@ -450,7 +457,7 @@ __global__ void __launch_bounds__(BLOCK, 5) k_hicoo_win2(sptgb_hicoo_args a, uin
             const uint32_t s0 = q, s1 = hi < rend ? hi : rend;
             const uint32_t per = (s1 - s0 + NWC - 1) / NWC;
             const uint32_t r_beg = s0 + min(s1 - s0, gw * per);
-            win2_range<W, false, FULL>(a, x, s_rec[warp], tile, 0u, k0, kend, r_beg, min(s1, r_beg + per));
+            win2_range<W, false, FULL, AC>(a, x, s_rec[warp], tile, 0u, k0, kend, r_beg, min(s1, r_beg + per));
             q = s1;
             w = wh;
             continue;
@@ -459,7 +466,7 @@ __global__ void __launch_bounds__(BLOCK, 5) k_hicoo_win2(sptgb_hicoo_args a, uin
         const uint32_t row0 = a.binds[mode][a.perm[k0]] << a.sb_bits;
         const uint32_t per = (s1 - s0 + NWC - 1) / NWC;
         const uint32_t r_beg = s0 + min(s1 - s0, gw * per);
-        win2_range<W, true, FULL>(a, x, s_rec[warp], tile, row0, k0, k1, r_beg, min(s1, r_beg + per));
+        win2_range<W, true, FULL, AC>(a, x, s_rec[warp], tile, row0, k0, k1, r_beg, min(s1, r_beg + per));
         __syncthreads();
         // one write of the window: plain when this CTA covered all of it
         const bool owned = s0 == wbeg && s1 == wend;
@@ -492,7 +499,7 @@ __global__ void k_block_sizes(const uint32_t *__restrict__ perm, const uint64_t 
         sizes[k] = (uint32_t)(bptr[perm[k] + 1] - bptr[perm[k]]);
 }
 
-template <int W, bool FULL>
+template <int W, bool FULL, bool AC>
 cudaError_t launch_win2_k(const sptgb_hicoo_args &a, cudaStream_t s) {
     static int nsm = 0;
     const size_t smem = ((size_t)1 << a.sb_bits) * a.stride * sizeof(float);
@@ -501,24 +508,25 @@ cudaError_t launch_win2_k(const sptgb_hicoo_args &a, cudaStream_t s) {
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        cudaFuncSetAttribute(k_hicoo_win2<W, FULL>, cudaFuncAttributeMaxDynamicSharedMemorySize, 180 * 1024);
+        cudaFuncSetAttribute(k_hicoo_win2<W, FULL, AC>, cudaFuncAttributeMaxDynamicSharedMemorySize, 180 * 1024);
     }
     int per = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_hicoo_win2<W, FULL>, BLOCK, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_hicoo_win2<W, FULL, AC>, BLOCK, smem);
     if (per < 1) per = 1;
     if (a.nnz == 0 || a.nnz >= 0xffffffffull) return a.nnz ? cudaErrorInvalidValue : cudaSuccess;
     const uint32_t total = (uint32_t)a.nnz;
     const uint64_t grid = (uint64_t)nsm * per * 2;
     const uint32_t chunk = (uint32_t)((total + grid - 1) / grid);
     const uint32_t ngrid = (total + chunk - 1) / chunk;
-    k_hicoo_win2<W, FULL><<<ngrid, BLOCK, smem, s>>>(a, chunk, total);
+    k_hicoo_win2<W, FULL, AC><<<ngrid, BLOCK, smem, s>>>(a, chunk, total);
     sptgb_count_launch(1);
     return cudaGetLastError();
 }
 
 template <int W>
 cudaError_t launch_win2(const sptgb_hicoo_args &a, cudaStream_t s) {
-    return a.stride == 4u * W ? launch_win2_k<W, true>(a, s) : launch_win2_k<W, false>(a, s);
+    if (a.stride != 4u * W) return launch_win2_k<W, false, false>(a, s);
+    return a.rank == a.stride ? launch_win2_k<W, true, true>(a, s) : launch_win2_k<W, true, false>(a, s);
 }
 
 template <int W, int NP>
@@ -587,7 +595,8 @@ extern "C" cudaError_t sptgb_mttkrp_hicoo(const sptgb_hicoo_args *a, cudaStream_
     cudaError_t e = cudaMemsetAsync(a->out, 0, (size_t)a->out_rows * a->stride * sizeof(float), s);
     if (e != cudaSuccess || a->nb == 0) return e;
     const uint32_t c4 = a->stride / 4;
-    if (a->perm && (a->nmodes == 3 || a->nmodes == 4)) {
+    // the window kernels count positions and blocks in 32 bits
+    if (a->perm && (a->nmodes == 3 || a->nmodes == 4) && a->nnz < 0xfffff000ull) {
         if (a->nmodes == 3) {
             if (c4 <= 2) return launch_win2<2>(*a, s);
             if (c4 <= 4) return launch_win2<4>(*a, s);
@@ -609,7 +618,7 @@ extern "C" cudaError_t sptgb_mttkrp_hicoo(const sptgb_hicoo_args *a, cudaStream_
 }
 
 extern "C" cudaError_t sptgb_hicoo_schedule(const uint32_t *binds_mode, const uint64_t *bptr, uint64_t nb,
-                                            int window_bits, const sptgb_hicoo_sched_scratch *w, uint32_t *perm,
+                                            int window_bits, uint32_t heavy_nnz, const sptgb_hicoo_sched_scratch *w, uint32_t *perm,
                                             uint32_t *pnnz, uint64_t *wst, uint32_t *nwin_out, uint64_t *heavy,
                                             uint32_t *nheavy_out, cudaStream_t s) {
     *nwin_out = 0;
@@ -647,7 +656,7 @@ extern "C" cudaError_t sptgb_hicoo_schedule(const uint32_t *binds_mode, const ui
     // the heavy windows, ascending
     uint64_t gw = (nwin + 255) / 256;
     if (gw > (uint64_t)sptgb_sm_count() * 16) gw = (uint64_t)sptgb_sm_count() * 16;
-    k_window_heavy<<<(unsigned)gw, 256, 0, s>>>(wst, pnnz, nwin, SPTGB_HICOO_HEAVY, w->flags);
+    k_window_heavy<<<(unsigned)gw, 256, 0, s>>>(wst, pnnz, nwin, heavy_nnz, w->flags);
     sptgb_count_launch(1);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = sptgb_exclusive_scan_u32(w->flags, w->pos, nwin, dn, w->stmp, s);

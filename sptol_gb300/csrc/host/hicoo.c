@@ -383,8 +383,9 @@ static int hicoo_mttkrp(sptSparseTensorHiCOO const *h, sptMatrix *mats[], sptInd
         const uint32_t maxb = h->ndims[mode] ? (h->ndims[mode] - 1) >> h->sb_bits : 0;
         uint32_t nwin = 0, nheavy = 0;
         uint64_t *wst = (uint64_t *)g_ws.misc[4].ptr;
-        C(sptgb_hicoo_schedule(a.binds[mode], a.bptr, nb, sptgb_bitwidth(maxb), &w, perm, pnnz, wst, &nwin,
-                               wst + nb + 1, &nheavy, s));
+        a.heavy_nnz = sptgb_hicoo_heavy_nnz(a.nnz);
+        C(sptgb_hicoo_schedule(a.binds[mode], a.bptr, nb, sptgb_bitwidth(maxb), a.heavy_nnz, &w, perm, pnnz, wst,
+                               &nwin, wst + nb + 1, &nheavy, s));
         a.perm = perm;
         a.pnnz = pnnz;
         a.wst = wst;
@@ -599,8 +600,9 @@ int sptgbHicooPrepareMode(sptgbHicoo *t, sptIndex mode, void *stream) {
         w.flags = (uint32_t *)g_ws.misc[2].ptr;
         w.pos = w.flags + nb;
         const uint32_t maxb = t->ndims[mode] ? (t->ndims[mode] - 1) >> t->sb_bits : 0;
-        e = sptgb_hicoo_schedule(t->binds[mode], t->bptr, nb, sptgb_bitwidth(maxb), &w, t->perm[mode], t->pnnz[mode],
-                                 t->wst[mode], &t->nwin[mode], t->wst[mode] + nb + 1, &t->nheavy[mode], s);
+        e = sptgb_hicoo_schedule(t->binds[mode], t->bptr, nb, sptgb_bitwidth(maxb), sptgb_hicoo_heavy_nnz(t->nnz), &w,
+                                 t->perm[mode], t->pnnz[mode], t->wst[mode], &t->nwin[mode], t->wst[mode] + nb + 1,
+                                 &t->nheavy[mode], s);
         if (e != cudaSuccess) r = sptgb_cuda_fail(e, module, __FILE__, __LINE__);
     }
     sptgb_unlock();
@@ -645,6 +647,7 @@ int sptgbHicooMTTKRP(sptgbHicoo *t, sptIndex mode, const sptIndex *mats_order, c
         a.nwin = t->nwin[mode];
         a.heavy = t->wst[mode] + t->nb + 1;
         a.nheavy = t->nheavy[mode];
+        a.heavy_nnz = sptgb_hicoo_heavy_nnz(t->nnz);
     }
     SPTGB_CUDA(sptgb_mttkrp_hicoo(&a, s), module);
     return 0;

@@ -171,8 +171,9 @@ typedef struct {
     const uint64_t *wst;                       /* [nwin+1] first position of each output window; wst[nwin] = nb */
     uint32_t        nwin;
     const uint64_t *heavy;                     /* [nheavy] ascending ids of the windows holding at least
-                                                  SPTGB_HICOO_HEAVY nonzeros (order 3) */
+                                                  heavy_nnz nonzeros (order 3) */
     uint32_t        nheavy;
+    uint32_t        heavy_nnz;                 /* sptgb_hicoo_heavy_nnz(nnz) */
     uint64_t        nnz;                       /* = bptr[nb]; below 2^32 for the window kernel */
 } sptgb_hicoo_args;
 cudaError_t sptgb_mttkrp_hicoo(const sptgb_hicoo_args *a, cudaStream_t s);
@@ -186,17 +187,29 @@ cudaError_t sptgb_hicoo_check_bptr(const uint64_t *bptr, uint64_t nb, uint64_t n
 /* Output-window schedule of one mode: blocks stably sorted by their block
  * index in `mode` (keys = binds_mode, window_bits significant bits), the
  * prefix of their sizes, the start of each run of equal keys (a window) and
- * the ascending list of windows with at least SPTGB_HICOO_HEAVY nonzeros
- * (heavy, [nb] capacity).  Scratch: keys/vals double buffers [nb] each, radix
- * tmp, flags/pos [nb], scan tmp.  *nwin_out and *nheavy_out are read back
- * (the stream is synchronised).  nnz < 2^32. */
-#define SPTGB_HICOO_HEAVY 8192u
+ * the ascending list of windows with at least heavy_nnz nonzeros (heavy, [nb]
+ * capacity).  Scratch: keys/vals double buffers [nb] each, radix tmp,
+ * flags/pos [nb], scan tmp.  *nwin_out and *nheavy_out are read back (the
+ * stream is synchronised).  nnz < 2^32. */
+#define SPTGB_HICOO_HEAVY_MIN 8192u
+#define SPTGB_HICOO_HEAVY_DIV 32u
+/* Order-3 window kernel: a window of 2^sb output rows holding at least this
+ * many nonzeros is summed in the shared-memory tile and written once; the
+ * rows of lighter windows go to the output with global vector atomics.  Only
+ * a window that holds a large share of the whole tensor (a power-law mode's
+ * head) puts enough atomics on a few rows to need the tile: on a 100M-nonzero
+ * tensor with two Zipf(1.2) modes the global atomics were faster for every
+ * window below a few million nonzeros. */
+static inline uint32_t sptgb_hicoo_heavy_nnz(uint64_t nnz) {
+    const uint64_t h = nnz / SPTGB_HICOO_HEAVY_DIV;
+    return h < SPTGB_HICOO_HEAVY_MIN ? SPTGB_HICOO_HEAVY_MIN : h > 0xffffffffull ? 0xffffffffu : (uint32_t)h;
+}
 typedef struct {
     uint32_t *keys[2], *vals[2], *flags, *pos;
     void *rtmp, *stmp;
 } sptgb_hicoo_sched_scratch;
 cudaError_t sptgb_hicoo_schedule(const uint32_t *binds_mode, const uint64_t *bptr, uint64_t nb, int window_bits,
-                                 const sptgb_hicoo_sched_scratch *w, uint32_t *perm, uint32_t *pnnz, uint64_t *wst,
+                                 uint32_t heavy_nnz, const sptgb_hicoo_sched_scratch *w, uint32_t *perm, uint32_t *pnnz, uint64_t *wst,
                                  uint32_t *nwin_out, uint64_t *heavy, uint32_t *nheavy_out, cudaStream_t s);
 
 /* ---------------------------------------------------- dense CP-ALS --
