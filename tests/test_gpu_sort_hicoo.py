@@ -192,8 +192,8 @@ def test_hicoo_window_kernel_3d_every_worker_width(rank):
 
 @pytest.mark.parametrize("sb", [4, 8])
 def test_hicoo_window_kernel_3d_block_sizes(sb):
-    """Order 3 with 16- and 256-row windows: the heavy windows' row counting
-    sort covers every window size the format allows (2^sb <= 256)."""
+    """Order 3 with 16- and 256-row windows: the heavy windows' shared-memory
+    tile covers every window size the format allows (2^sb <= 256)."""
     t = _skewed3(500_000, 23)
     ndims = t.ndims
     h = S.HiCOO(t, sb, 17)
