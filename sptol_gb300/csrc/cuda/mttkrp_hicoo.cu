@@ -10,6 +10,10 @@
 // atomics when the window continues in a neighbouring CTA.  Skewed (power-
 // law) rows thus cost shared-memory atomics, not contended global ones.
 //
+// Light kernel (k_hicoo_light, order 3): a schedule with no heavy window
+// runs the order-3 window kernel's light path over all its positions, without
+// the tile's shared memory and at a higher CTA count per SM.
+//
 // Block kernel (k_mttkrp_hicoo, any order; used without a schedule): a
 // worker (W lanes, one float4 column group per lane) owns one HiCOO block
 // at a time.  Element coordinates are rebuilt as (binds << sb_bits) + einds
@@ -254,11 +258,11 @@ struct Win2Ctx {
 // are gathered without a select (an empty record carries rows 0, in range).
 // AC (with FULL): the rank equals the stride, so no column is padding and the
 // row flushes need no column masks.
-template <int W, bool TILE, bool FULL, bool AC>
+template <int W, bool TILE, bool FULL, bool AC, int EB = 2>
 __device__ __forceinline__ void win2_range(const sptgb_hicoo_args &a, const Win2Ctx &x, uint4 *s_rec, float *tile,
                                            uint32_t row0, uint64_t klo, uint64_t khi, uint32_t r_beg,
                                            uint32_t r_end) {
-    constexpr int EB = 2;   // records per gather batch
+    // EB: records per gather batch
     uint32_t cur = NONE;
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     auto put = [&]() {
@@ -388,15 +392,10 @@ __device__ __forceinline__ void win2_range(const sptgb_hicoo_args &a, const Win2
     put();
 }
 
-template <int W, bool FULL, bool AC>
-__global__ void __launch_bounds__(BLOCK, 5) k_hicoo_win2(sptgb_hicoo_args a, uint32_t chunk, uint32_t total) {
-    extern __shared__ float tile[];   // [1 << sb][stride]
-    constexpr int NWARP = BLOCK / 32;
-    constexpr int NWK = 32 / W;              // workers per warp
-    constexpr uint32_t NWC = BLOCK / W;      // workers per CTA
-    __shared__ uint4 s_rec[NWARP][32];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    Win2Ctx x;
+// The per-lane constants of a worker (lane sl of worker wk in its warp).
+template <int W>
+__device__ __forceinline__ void win2_ctx(const sptgb_hicoo_args &a, Win2Ctx &x) {
+    const int lane = threadIdx.x & 31;
     x.sl = lane % W;
     x.wk = lane / W;
     x.rows_w = 1u << a.sb_bits;
@@ -424,6 +423,42 @@ __global__ void __launch_bounds__(BLOCK, 5) k_hicoo_win2(sptgb_hicoo_args a, uin
     x.Fa = reinterpret_cast<const char *>(a.fac[pa]) + (size_t)x.sl * 16;
     x.Fb = reinterpret_cast<const char *>(a.fac[pb]) + (size_t)x.sl * 16;
     x.rb = x.st * 4u;
+}
+
+// A schedule without heavy windows (no output window holds heavy_nnz
+// nonzeros, e.g. every window of a uniform mode) is one flat light range:
+// this kernel has no tile, so it needs no shared memory beyond the record
+// staging (the L1 keeps the rest) and fewer registers than k_hicoo_win2.
+constexpr int LIGHT_MINB = 6;   // CTAs per SM the register budget is set for
+constexpr int LIGHT_EB = 2;     // records per gather batch
+template <int W, bool FULL, bool AC>
+__global__ void __launch_bounds__(BLOCK, LIGHT_MINB) k_hicoo_light(sptgb_hicoo_args a, uint32_t chunk, uint32_t total) {
+    constexpr int NWARP = BLOCK / 32;
+    constexpr uint32_t NWC = BLOCK / W;   // workers per CTA
+    __shared__ uint4 s_rec[NWARP][32];
+    const int warp = threadIdx.x >> 5;
+    Win2Ctx x;
+    win2_ctx<W>(a, x);
+    const uint32_t gw = (uint32_t)(warp * (32 / W) + x.wk);
+    const uint64_t lo64 = (uint64_t)blockIdx.x * chunk;
+    if (lo64 >= total) return;
+    const uint32_t lo = (uint32_t)lo64, hi = (uint32_t)min((uint64_t)total, lo64 + chunk);
+    const uint32_t per = (hi - lo + NWC - 1) / NWC;
+    const uint32_t r_beg = lo + min(hi - lo, gw * per);
+    win2_range<W, false, FULL, AC, LIGHT_EB>(a, x, s_rec[warp], nullptr, 0u, 0u, a.nb, r_beg, min(hi, r_beg + per));
+}
+
+template <int W, bool FULL, bool AC>
+__global__ void __launch_bounds__(BLOCK, 5) k_hicoo_win2(sptgb_hicoo_args a, uint32_t chunk, uint32_t total) {
+    extern __shared__ float tile[];   // [1 << sb][stride]
+    constexpr int NWARP = BLOCK / 32;
+    constexpr int NWK = 32 / W;              // workers per warp
+    constexpr uint32_t NWC = BLOCK / W;      // workers per CTA
+    __shared__ uint4 s_rec[NWARP][32];
+    const int warp = threadIdx.x >> 5;
+    Win2Ctx x;
+    win2_ctx<W>(a, x);
+    const uint32_t mode = a.mode;
     const uint32_t st4 = x.st / 4;
     const uint32_t gw = (uint32_t)(warp * NWK + x.wk);
 
@@ -523,8 +558,32 @@ cudaError_t launch_win2_k(const sptgb_hicoo_args &a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+template <int W, bool FULL, bool AC>
+cudaError_t launch_light_k(const sptgb_hicoo_args &a, cudaStream_t s) {
+    static int nsm = 0, per = 0;
+    if (nsm == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_hicoo_light<W, FULL, AC>, BLOCK, 0);
+        if (per < 1) per = 1;
+    }
+    if (a.nnz == 0 || a.nnz >= 0xffffffffull) return a.nnz ? cudaErrorInvalidValue : cudaSuccess;
+    const uint32_t total = (uint32_t)a.nnz;
+    const uint64_t grid = (uint64_t)nsm * per * 2;
+    const uint32_t chunk = (uint32_t)((total + grid - 1) / grid);
+    const uint32_t ngrid = (total + chunk - 1) / chunk;
+    k_hicoo_light<W, FULL, AC><<<ngrid, BLOCK, 0, s>>>(a, chunk, total);
+    sptgb_count_launch(1);
+    return cudaGetLastError();
+}
+
 template <int W>
 cudaError_t launch_win2(const sptgb_hicoo_args &a, cudaStream_t s) {
+    if (a.nheavy == 0) {
+        if (a.stride != 4u * W) return launch_light_k<W, false, false>(a, s);
+        return a.rank == a.stride ? launch_light_k<W, true, true>(a, s) : launch_light_k<W, true, false>(a, s);
+    }
     if (a.stride != 4u * W) return launch_win2_k<W, false, false>(a, s);
     return a.rank == a.stride ? launch_win2_k<W, true, true>(a, s) : launch_win2_k<W, true, false>(a, s);
 }
