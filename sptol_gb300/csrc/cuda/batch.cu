@@ -209,36 +209,37 @@ unsigned grid_for(uint64_t n, unsigned cap) {
     return b ? (unsigned)b : 1u;
 }
 
-int g_nsm = 0;
 int g_mt_blocks[4][2][2];   // [group][deep][occupancy 2 / 3]: grid of each MTTKRP kernel
 
 template <int W, bool DEEP, int MINB>
-void size_mttkrp(int g) {
+void size_mttkrp(int g, int n) {
     int per = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_b_mttkrp<W, DEEP, MINB>, BT, 0);
-    g_mt_blocks[g][DEEP][MINB - 2] = (per < 1 ? 1 : per) * g_nsm;
+    g_mt_blocks[g][DEEP][MINB - 2] = (per < 1 ? 1 : per) * n;
 }
 template <int W>
-void size_group(int g) {
-    size_mttkrp<W, false, 2>(g);
-    size_mttkrp<W, true, 2>(g);
-    size_mttkrp<W, false, 3>(g);
-    size_mttkrp<W, true, 3>(g);
+void size_group(int g, int n) {
+    size_mttkrp<W, false, 2>(g, n);
+    size_mttkrp<W, true, 2>(g, n);
+    size_mttkrp<W, false, 3>(g, n);
+    size_mttkrp<W, true, 3>(g, n);
 }
 
+// SM count; the first call also sets the kernels' shared-memory limits and
+// sizes the MTTKRP grids.  A function-local static is initialised by one
+// thread while the others wait, so no caller sees the grids half sized.
 int nsm() {
-    if (!g_nsm) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&g_nsm, cudaDevAttrMultiProcessorCount, dev);
+    static const int n = [] {
+        const int c = sptgb_sm_count();
         cudaFuncSetAttribute(k_b_prepare, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PREP_SMEM);
         cudaFuncSetAttribute(k_b_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SOLVE_SMEM);
-        size_group<2>(0);
-        size_group<4>(1);
-        size_group<8>(2);
-        size_group<16>(3);
-    }
-    return g_nsm;
+        size_group<2>(0, c);
+        size_group<4>(1, c);
+        size_group<8>(2, c);
+        size_group<16>(3, c);
+        return c;
+    }();
+    return n;
 }
 
 template <int W>

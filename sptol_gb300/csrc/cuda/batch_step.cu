@@ -143,7 +143,23 @@ __global__ void k_bar_selftest(sptgb_grid_bar *bar, int missing, uint32_t max_sp
     }
 }
 
-int g_blocks = 0;   // resident blocks of k_b_step (0: not yet sized, <0: unsupported)
+// Resident blocks of k_b_step (< 0: cooperative launch unsupported), sized on
+// first use; a function-local static is initialised by one thread while the
+// others wait.
+int step_blocks() {
+    static const int blocks = [] {
+        int dev = 0, coop = 0, per = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) == cudaSuccess && coop &&
+            cudaFuncSetAttribute(k_b_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SOLVE_SMEM) ==
+                cudaSuccess &&
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_b_step, BT, SOLVE_SMEM) == cudaSuccess && per >= 1)
+            return (per < 2 ? per : 2) * sptgb_sm_count();
+        cudaGetLastError();
+        return -1;
+    }();
+    return blocks;
+}
 
 }  // namespace
 
@@ -152,23 +168,13 @@ int g_blocks = 0;   // resident blocks of k_b_step (0: not yet sized, <0: unsupp
 // cooperative launch that does not fit rather than running it.
 extern "C" cudaError_t sptgb_batch_step_persistent(const sptgb_slot *slots, const sptgb_step_lists *L,
                                                    sptgb_grid_bar *bar, cudaStream_t s) {
-    // sized once; two threads sizing it at the same time store the same value
-    if (g_blocks == 0) {
-        int dev = 0, coop = 0, per = 0, blocks = -1;
-        if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) ==
-                                                      cudaSuccess && coop &&
-            cudaFuncSetAttribute(k_b_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SOLVE_SMEM) ==
-                cudaSuccess &&
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_b_step, BT, SOLVE_SMEM) == cudaSuccess && per >= 1)
-            blocks = (per < 2 ? per : 2) * sptgb_sm_count();
-        g_blocks = blocks;
-    }
-    if (g_blocks < 0) return cudaErrorNotSupported;
+    const int blocks = step_blocks();
+    if (blocks < 0) return cudaErrorNotSupported;
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;
     attr[0].val.cooperative = 1;
-    cfg.gridDim = dim3((unsigned)g_blocks);
+    cfg.gridDim = dim3((unsigned)blocks);
     cfg.blockDim = dim3(BT);
     cfg.dynamicSmemBytes = SOLVE_SMEM;
     cfg.stream = s;

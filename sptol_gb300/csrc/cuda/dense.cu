@@ -65,11 +65,11 @@ extern "C" cudaError_t sptgb_gram(const float *A, uint32_t nrows, int rank, int 
 extern "C" cudaError_t sptgb_solve_prepare(const double *const *grams, int nmodes, int mode, int rank,
                                            double *Hinv, int *status, cudaStream_t s) {
     if (rank < 1 || rank > RMAX) return cudaErrorInvalidValue;
-    static int configured = 0;
-    if (!configured) {
+    // once per process (a function-local static is initialised by one thread
+    // while the others wait; a failure shows up as the launch's error)
+    static const cudaError_t attr =
         cudaFuncSetAttribute(k_solve_prepare, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PREP_SMEM);
-        configured = 1;
-    }
+    (void)attr;
     GramPtrs gp;
     for (int m = 0; m < SPTGB_MAX_MODES; ++m) gp.g[m] = m < nmodes ? grams[m] : nullptr;
     k_solve_prepare<<<1, DT, PREP_SMEM, s>>>(gp, nmodes, mode, rank, Hinv, status);
@@ -80,11 +80,9 @@ extern "C" cudaError_t sptgb_solve_prepare(const double *const *grams, int nmode
 extern "C" cudaError_t sptgb_solve_rows(const float *M, float *X, uint32_t nrows, int rank, int stride,
                                         const double *Hinv, const int *status, double *ws, cudaStream_t s) {
     if (rank < 1 || rank > RMAX) return cudaErrorInvalidValue;
-    static int configured = 0;
-    if (!configured) {
+    static const cudaError_t attr =
         cudaFuncSetAttribute(k_solve_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SOLVE_SMEM);
-        configured = 1;
-    }
+    (void)attr;   // once per process, as in sptgb_solve_prepare
     const int nb = nblocks_for_solve(nrows, rank);
     const size_t P = (size_t)rank * (rank + 1) / 2;
     k_solve_rows<<<nb, DT, SOLVE_SMEM, s>>>(M, X, nrows, rank, stride, Hinv, status, ws, ws + NBLK * P);

@@ -252,17 +252,15 @@ __global__ void k_zero_shared(const uint32_t *__restrict__ rows, uint64_t nnz, u
 
 template <int W, int NP, bool BF16>
 cudaError_t launch(const sptgb_mttkrp_args &a, cudaStream_t s) {
-    static int max_blocks = 0;
-    static int nsm = 0;
-    if (max_blocks == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        int per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mttkrp_seg<W, NP, BF16>, BLOCK, 0);
-        if (per_sm < 1) per_sm = 1;
-        max_blocks = per_sm * nsm;
-    }
+    // once per process (function-local statics are initialised by one thread
+    // while the others wait)
+    static const int per_sm = [] {
+        int p = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p, k_mttkrp_seg<W, NP, BF16>, BLOCK, 0);
+        return p < 1 ? 1 : p;
+    }();
+    const int nsm = sptgb_sm_count();
+    const int max_blocks = per_sm * nsm;
     const uint64_t workers_per_block = BLOCK / W;
     const uint64_t concurrent = workers_per_block * (uint64_t)max_blocks;
     // Units: about four per concurrent worker, between 64 and 4096 nonzeros.
@@ -287,17 +285,15 @@ cudaError_t launch(const sptgb_mttkrp_args &a, cudaStream_t s) {
 template <int W, bool BF16, bool FULL, int NF>
 cudaError_t launch_rec_k(const sptgb_mttkrp_args &a, cudaStream_t s) {
     constexpr int NB = 2;   // order-4 records per batch (3: register spills at 3 CTAs/SM)
-    static int max_blocks = 0;
-    if (max_blocks == 0) {
-        int dev = 0, nsm = 0, per_sm = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    static const int per_sm = [] {
+        int p = 0;
         if (NF == 2)
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mttkrp_rec<W, BF16, FULL>, BLOCK, 0);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p, k_mttkrp_rec<W, BF16, FULL>, BLOCK, 0);
         else
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mttkrp_rec4<W, BF16, FULL, NB>, BLOCK, 0);
-        max_blocks = (per_sm < 1 ? 1 : per_sm) * nsm;
-    }
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p, k_mttkrp_rec4<W, BF16, FULL, NB>, BLOCK, 0);
+        return p < 1 ? 1 : p;
+    }();
+    const int max_blocks = per_sm * sptgb_sm_count();
     // 256-nonzero units: enough of them to balance a power-law row distribution
     const uint32_t ul = SPTGB_REC_UNIT;
     const uint64_t nunits = (a.nnz + ul - 1) / ul;

@@ -536,15 +536,14 @@ __global__ void k_block_sizes(const uint32_t *__restrict__ perm, const uint64_t 
 
 template <int W, bool FULL, bool AC>
 cudaError_t launch_win2_k(const sptgb_hicoo_args &a, cudaStream_t s) {
-    static int nsm = 0;
     const size_t smem = ((size_t)1 << a.sb_bits) * a.stride * sizeof(float);
     if (smem > 180 * 1024) return cudaErrorInvalidValue;
-    if (nsm == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    // once per process: a function-local static is initialised by one thread
+    // while the others wait (a failure shows up as the launch's error)
+    static const cudaError_t attr =
         cudaFuncSetAttribute(k_hicoo_win2<W, FULL, AC>, cudaFuncAttributeMaxDynamicSharedMemorySize, 180 * 1024);
-    }
+    (void)attr;
+    const int nsm = sptgb_sm_count();
     int per = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_hicoo_win2<W, FULL, AC>, BLOCK, smem);
     if (per < 1) per = 1;
@@ -560,14 +559,12 @@ cudaError_t launch_win2_k(const sptgb_hicoo_args &a, cudaStream_t s) {
 
 template <int W, bool FULL, bool AC>
 cudaError_t launch_light_k(const sptgb_hicoo_args &a, cudaStream_t s) {
-    static int nsm = 0, per = 0;
-    if (nsm == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_hicoo_light<W, FULL, AC>, BLOCK, 0);
-        if (per < 1) per = 1;
-    }
+    static const int per = [] {
+        int p = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p, k_hicoo_light<W, FULL, AC>, BLOCK, 0);
+        return p < 1 ? 1 : p;
+    }();
+    const int nsm = sptgb_sm_count();
     if (a.nnz == 0 || a.nnz >= 0xffffffffull) return a.nnz ? cudaErrorInvalidValue : cudaSuccess;
     const uint32_t total = (uint32_t)a.nnz;
     const uint64_t grid = (uint64_t)nsm * per * 2;
@@ -590,15 +587,12 @@ cudaError_t launch_win2(const sptgb_hicoo_args &a, cudaStream_t s) {
 
 template <int W, int NP>
 cudaError_t launch_win(const sptgb_hicoo_args &a, cudaStream_t s) {
-    static int nsm = 0;
     const size_t smem = ((size_t)1 << a.sb_bits) * a.stride * sizeof(float);
     if (smem > 200 * 1024) return cudaErrorInvalidValue;
-    if (nsm == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    static const cudaError_t attr =
         cudaFuncSetAttribute(k_hicoo_win<W, NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    }
+    (void)attr;   // once per process, as in launch_win2_k
+    const int nsm = sptgb_sm_count();
     int per = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_hicoo_win<W, NP>, BLOCK, smem);
     if (per < 1) per = 1;
@@ -629,14 +623,12 @@ __global__ void k_hicoo_check(const uint64_t *__restrict__ bptr, sptgb_hicoo_arg
 
 template <int W>
 cudaError_t launch(const sptgb_hicoo_args &a, cudaStream_t s) {
-    static int max_blocks = 0;
-    if (max_blocks == 0) {
-        int dev = 0, nsm = 0, per_sm = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mttkrp_hicoo<W>, BLOCK, 0);
-        max_blocks = (per_sm < 1 ? 1 : per_sm) * nsm;
-    }
+    static const int per_sm = [] {
+        int p = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p, k_mttkrp_hicoo<W>, BLOCK, 0);
+        return p < 1 ? 1 : p;
+    }();
+    const int max_blocks = per_sm * sptgb_sm_count();
     const uint64_t wpb = BLOCK / W;
     uint64_t blocks = (a.nb + wpb - 1) / wpb;
     if (blocks > (uint64_t)max_blocks) blocks = max_blocks;
