@@ -24,7 +24,9 @@ Workload (one "step" = MTTKRP of every mode, 0, 1, 2, on one GPU):
           and sptMTTKRPHiCOO per mode (kernel time from CUDA events); its
           cpu_baseline is the oracle port of
           sptOmpMTTKRPHiCOO_MatrixTiling_Scheduled_Reduce (all host threads)
-          on the HiCOO form of the 10M-nonzero sample.
+          on the HiCOO form of the 10M-nonzero sample.  With --hicoo4,
+          hicoo.order4 adds order-4 HiCOO against the order-4 record kernel on
+          two 50M-draw tensors (uniform and power-law), kernel times per mode.
   serve   the batched / served CP-ALS stream: 4,096 requests of order 3 or 4
           (50/50), mode sizes log-uniform in [64, 100,000], nnz log-uniform in
           [1e3, 1e6] (at most half the index space, unique uniform
@@ -77,6 +79,7 @@ def parse():
     p.add_argument("--serve-cpu-sample", type=int, default=32)
     p.add_argument("--skip-serve", action="store_true")
     p.add_argument("--skip-hicoo", action="store_true")
+    p.add_argument("--hicoo4", action="store_true", help="also time order-4 HiCOO against order-4 COO")
     p.add_argument("--skip-registered", action="store_true")
     p.add_argument("--skip-c1", action="store_true")
     p.add_argument("--skip-cpals", action="store_true")
@@ -314,6 +317,66 @@ def hicoo_leg(t, mats, ndims, nnz, reps):
             "algorithmic_bytes_per_mttkrp": hb,
             "kernel_gbs": round(N * hb / (sum(kern) / 1e3) / 1e9, 1),
             "coo_bytes_gbs": round(N * algo_bytes(ndims, nnz, RANK) / (sum(kern) / 1e3) / 1e9, 1)}
+
+
+def hicoo4_leg(reps=3):
+    """Order-4 HiCOO (blocks 2^7, kernels 2^17) against the order-4 record
+    kernel on the same tensors: a uniform 10K x 5K x 2K x 500 and a power-law
+    2M x 1M x 50K x 500 (Zipf(1.2) in the first two modes), 50M draws each,
+    values U[-1,1), rank 16.  Kernel times (output memset included) from CUDA
+    events, median of `reps` calls per mode after one warm-up call."""
+    import torch
+    import sptol_gb300 as S
+    L = S.lib()
+    rank = stride = 16
+    out = {}
+    for name, dims, zipf in (("uniform_10Kx5Kx2Kx500", [10_000, 5_000, 2_000, 500], [0, 0, 0, 0]),
+                             ("zipf_2Mx1Mx50Kx500", [2_000_000, 1_000_000, 50_000, 500], [1.2, 1.2, 0, 0])):
+        spec = S.GenSpec()
+        spec.seed = SEED + 4
+        spec.nmodes = 4
+        for m, d in enumerate(dims):
+            spec.ndims[m] = d
+            spec.coord_dist[m] = S.DIST_ZIPF if zipf[m] else S.DIST_UNIFORM
+            spec.zipf_s[m] = zipf[m]
+        spec.count = 50_000_000
+        spec.value_dist = S.VAL_UPM1
+        t = S.Tensor.generate(spec)
+        nd = t.ndims
+        mats = S.new_factors(nd, rank, seed=3)
+        h = S.HiCOO(t, 7, 17)
+        nb = int(h.s.bptr.len) - 1
+        L.sptgbHiCOOSetTiming(1)
+        hk = []
+        for m in range(4):
+            S.mttkrp_hicoo(h, mats, m)
+            ks = []
+            for _ in range(reps):
+                S.mttkrp_hicoo(h, mats, m)
+                ks.append(float(L.sptgbHiCOOLastKernelMs()))
+            hk.append(round(float(np.median(ks)), 3))
+        L.sptgbHiCOOSetTiming(0)
+        h.free()
+        dc = S.DeviceCoo(t)
+        facs = [torch.from_numpy(mats[m].array()[: nd[m]].copy()).cuda() for m in range(4)]
+        ptrs = [f.data_ptr() for f in facs]
+        dout = torch.zeros((max(nd), stride), dtype=torch.float32, device="cuda")
+        dc.set_timing(True)
+        ck = []
+        for m in range(4):
+            order = [m] + [(m + j) % 4 for j in (1, 2, 3)]
+            dc.prepare(m)
+            dc.mttkrp(m, order, ptrs, rank, stride, dout.data_ptr())
+            ks = []
+            for _ in range(reps):
+                dc.mttkrp(m, order, ptrs, rank, stride, dout.data_ptr())
+                ks.append(dc.last_ms())
+            ck.append(round(float(np.median(ks)), 3))
+        dc.free()
+        del facs, dout
+        out[name] = {"nnz": int(t.nnz), "blocks": nb, "hicoo_kernel_ms_by_mode": hk, "coo_kernel_ms_by_mode": ck}
+        t.free()
+    return out
 
 
 def hicoo_cpu_leg(sample_nnz, reps):
@@ -1101,6 +1164,8 @@ def run_ours(args, world, rank, local):
         hicoo = hicoo_leg(t, mats, ndims, nnz, 3)
         if not args.skip_cpu:
             hicoo["cpu_baseline"] = hicoo_cpu_leg(args.cpu_sample, 2)
+        if args.hicoo4:
+            hicoo["order4"] = hicoo4_leg()
 
     # CP-ALS before the serve leg: after that leg (a 120 GB arena and ~10 GB of
     # request tensors allocated and freed) the first upload of this tensor

@@ -1,18 +1,19 @@
 // HiCOO MTTKRP for sm_103a (sptMTTKRPHiCOO, src/sptensor/hicoo/mttkrp.c:53-144).
 //
-// Window kernel (k_hicoo_win, orders 3 and 4): the blocks are visited in the
-// order of their block index in the output mode (a stable device sort of
+// Window kernel (k_hicoo_win2, orders 3 and 4): the blocks are visited in
+// the order of their block index in the output mode (a stable device sort of
 // binds[mode], sptgb_hicoo_schedule), so all blocks writing one output window
 // of 2^sb rows are consecutive.  The nonzeros, in that order, are split
-// evenly over persistent CTAs; a CTA accumulates the products of each window
-// it visits in a shared-memory tile (2^sb rows x stride, shared atomics) and
-// writes the tile once: plain stores when it covers the whole window, vector
-// atomics when the window continues in a neighbouring CTA.  Skewed (power-
-// law) rows thus cost shared-memory atomics, not contended global ones.
+// evenly over persistent CTAs.  A window holding a large share of the tensor
+// (a heavy window: the head of a power-law mode) is summed in a shared-memory
+// tile (2^sb rows x stride, shared atomics) that is written once: plain
+// stores when the CTA covers the whole window, vector atomics when the window
+// continues in a neighbouring CTA, so skewed rows cost shared-memory atomics,
+// not contended global ones.  Light windows go straight to the output.
 //
-// Light kernel (k_hicoo_light, order 3): a schedule with no heavy window
-// runs the order-3 window kernel's light path over all its positions, without
-// the tile's shared memory and at a higher CTA count per SM.
+// Light kernel (k_hicoo_light, orders 3 and 4): a schedule with no heavy
+// window runs the window kernel's light path over all its positions, without
+// the tile's shared memory and, for order 3, at a higher CTA count per SM.
 //
 // Block kernel (k_mttkrp_hicoo, any order; used without a schedule): a
 // worker (W lanes, one float4 column group per lane) owns one HiCOO block
@@ -100,138 +101,14 @@ __device__ __forceinline__ uint64_t block_at(const uint32_t *pnnz, uint64_t lo, 
     return lo;
 }
 
-template <int W, int NP>
-__global__ void __launch_bounds__(BLOCK) k_hicoo_win(sptgb_hicoo_args a, uint32_t chunk, uint32_t total) {
-    extern __shared__ float tile[];   // [1 << sb][stride]
-    const int sl = (threadIdx.x & 31) % W;
-    const int wk = threadIdx.x / W;          // worker in this CTA
-    constexpr int NW = BLOCK / W;
-    const uint32_t rows_w = 1u << a.sb_bits;
-    const uint32_t st = a.stride, st4 = st / 4;
-    const bool col_ok = (uint32_t)(sl * 4) < st;
-    const int c0 = sl * 4;
-    const bool m0 = c0 + 0 < (int)a.rank, m1 = c0 + 1 < (int)a.rank;
-    const bool m2 = c0 + 2 < (int)a.rank, m3 = c0 + 3 < (int)a.rank;
-    const uint32_t mode = a.mode;
-    uint32_t pm[NP];
-#pragma unroll
-    for (int i = 0; i < NP; ++i) pm[i] = a.order[i + 1];
-
-    const uint64_t lo64 = (uint64_t)blockIdx.x * chunk;
-    if (lo64 >= total) return;
-    const uint32_t lo = (uint32_t)lo64, hi = (uint32_t)min((uint64_t)total, lo64 + chunk);
-    for (uint32_t i = threadIdx.x; i < rows_w * st; i += BLOCK) tile[i] = 0.f;
-    // first window: last w with pnnz[wst[w]] <= lo
-    uint32_t wlo = 0, whi = a.nwin;
-    while (whi - wlo > 1) {
-        const uint32_t mid = (wlo + whi) >> 1;
-        if (a.pnnz[a.wst[mid]] <= lo) wlo = mid;
-        else whi = mid;
-    }
-    uint32_t w = wlo;
-    uint32_t q = lo;
-    __syncthreads();
-    while (q < hi) {
-        const uint64_t k0 = a.wst[w], k1 = a.wst[w + 1];
-        const uint32_t wbeg = a.pnnz[k0], wend = a.pnnz[k1];
-        const uint32_t s0 = q > wbeg ? q : wbeg, s1 = hi < wend ? hi : wend;
-        const uint32_t per = (s1 - s0 + NW - 1) / NW;
-        uint32_t p = s0 + wk * per;
-        const uint32_t pend = min(p + per, s1);
-        if (p < pend) {
-            uint64_t k = block_at(a.pnnz, k0, k1, p);
-            uint32_t b = a.perm[k];
-            uint64_t e = a.bptr[b] + (p - a.pnnz[k]);
-            uint32_t kend = a.pnnz[k + 1];
-            uint32_t base_m = a.binds[mode][b] << a.sb_bits, base[NP];
-#pragma unroll
-            for (int i = 0; i < NP; ++i) base[i] = a.binds[pm[i]][b] << a.sb_bits;
-            // consecutive elements of one output row are summed in registers
-            // and added to the tile when the row changes
-            uint32_t cur = NONE;
-            float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-            auto put = [&]() {
-                if (cur == NONE || !col_ok) return;
-                float *t = tile + cur * st + c0;
-                if (m0) atomicAdd(t + 0, acc.x);
-                if (m1) atomicAdd(t + 1, acc.y);
-                if (m2) atomicAdd(t + 2, acc.z);
-                if (m3) atomicAdd(t + 3, acc.w);
-            };
-            for (; p < pend; ++p, ++e) {
-                while (p == kend) {   // next non-empty block
-                    ++k;
-                    b = a.perm[k];
-                    e = a.bptr[b];
-                    kend = a.pnnz[k + 1];
-                    base_m = a.binds[mode][b] << a.sb_bits;
-#pragma unroll
-                    for (int i = 0; i < NP; ++i) base[i] = a.binds[pm[i]][b] << a.sb_bits;
-                }
-                const uint32_t rl = a.einds[mode][e];
-                uint32_t ri[NP];
-                bool inside = base_m + rl < a.out_rows && rl < rows_w;
-#pragma unroll
-                for (int i = 0; i < NP; ++i) {
-                    ri[i] = base[i] + a.einds[pm[i]][e];
-                    inside &= ri[i] < a.ndims[pm[i]];
-                }
-                if (!inside) {
-                    if (sl == 0) atomicOr(a.err, 1u);
-                    continue;
-                }
-                if (!col_ok) continue;
-                const float v = a.vals[e];
-                float4 pr = make_float4(v, v, v, v);
-#pragma unroll
-                for (int i = 0; i < NP; ++i) {
-                    const float4 f = __ldg(reinterpret_cast<const float4 *>(a.fac[pm[i]] + (size_t)ri[i] * st) + sl);
-                    pr.x *= f.x;
-                    pr.y *= f.y;
-                    pr.z *= f.z;
-                    pr.w *= f.w;
-                }
-                if (rl != cur) {
-                    put();
-                    cur = rl;
-                    acc = make_float4(0.f, 0.f, 0.f, 0.f);
-                }
-                acc.x += pr.x;
-                acc.y += pr.y;
-                acc.z += pr.z;
-                acc.w += pr.w;
-            }
-            put();
-        }
-        __syncthreads();
-        // one write of the window: plain when this CTA covered all of it
-        const bool owned = s0 == wbeg && s1 == wend;
-        const uint32_t row0 = a.binds[mode][a.perm[k0]] << a.sb_bits;
-        float4 *t4 = reinterpret_cast<float4 *>(tile);
-        for (uint32_t i = threadIdx.x; i < rows_w * st4; i += BLOCK) {
-            const uint32_t r = i / st4, c = i % st4;
-            const float4 v = t4[i];
-            t4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (row0 + r >= a.out_rows) continue;
-            float4 *o = reinterpret_cast<float4 *>(a.out + (size_t)(row0 + r) * st) + c;
-            if (owned) *o = v;
-            else if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f) atomicAdd(o, v);
-        }
-        __syncthreads();
-        q = s1;
-        ++w;
-    }
-}
-
-// Order 3 (k_hicoo_win2).  Same schedule and equal-nonzero CTA ranges as
-// k_hicoo_win, with two changes.
+// The window kernels' work, per worker:
 //  * Decoding: each worker owns a contiguous share of its positions, and its
 //    W lanes decode W consecutive schedule positions together: they load the
 //    next W block boundaries (pnnz) at once and each lane finds its block
 //    with a log2(W)-step search over them through shuffles (exact with empty
 //    blocks), so the block and element loads of the 32 positions of a warp
 //    are in flight together instead of one dependent chain per element.  The
-//    decoded records {row, row of factor a, row of factor b, value} go through
+//    decoded records (output row, the product modes' rows, value) go through
 //    shared memory to the worker, which issues the factor-row gathers of a
 //    batch of them before using any.
 //  * Windows: only heavy windows (at least heavy_nnz nonzeros, the
@@ -240,26 +117,30 @@ __global__ void __launch_bounds__(BLOCK) k_hicoo_win(sptgb_hicoo_args a, uint32_
 //    running row sum of a worker goes to the output with a vector atomic when
 //    the row changes, with no per-window barrier or tile write, so the many
 //    small windows of a long tail cost no more than their nonzeros.
+// Product modes a, b (mats_order[1], [2]) and, for order 4, c ([3]).
 struct Win2Ctx {
-    const uint8_t *e_m, *e_a, *e_b;
-    const uint32_t *b_m, *b_a, *b_b;
-    const char *Fa, *Fb;
+    const uint8_t *e_m, *e_a, *e_b, *e_c;
+    const uint32_t *b_m, *b_a, *b_b, *b_c;
+    const char *Fa, *Fb, *Fc;   // factor rows, offset to this lane's columns
     uint32_t rb;      // bytes per factor row (stride * 4 <= 512)
-    uint32_t lim_a, lim_b, rows_w, st;
+    uint32_t lim_a, lim_b, lim_c, rows_w, st;
     int sl, wk, c0;
     bool col_ok, m0, m1, m2, m3;
     uint32_t mrot;    // column mask m0 | m1 << 1 | m2 << 2 | m3 << 3 rotated right by wk mod 4
 };
 
 // One worker's positions [r_beg, r_end) of the blocks [klo, khi) of the
-// schedule.  TILE: rows are window rows (row0 + r) summed in `tile`;
+// schedule, for NP product modes (2: order 3, 3: order 4).  Records are
+// staged as {row, row of a, row of b, value} (NP = 2) or as {row of a, row of
+// b, row of c, value} with the output row in s_row (NP = 3).  TILE: rows are window rows (row0 + r) summed in `tile`;
 // otherwise output rows, flushed with vector atomics.  FULL: the stride is
 // exactly 4W columns, so every lane holds stored columns and the factor rows
 // are gathered without a select (an empty record carries rows 0, in range).
 // AC (with FULL): the rank equals the stride, so no column is padding and the
 // row flushes need no column masks.
-template <int W, bool TILE, bool FULL, bool AC, int EB = 2>
-__device__ __forceinline__ void win2_range(const sptgb_hicoo_args &a, const Win2Ctx &x, uint4 *s_rec, float *tile,
+template <int W, int NP, bool TILE, bool FULL, bool AC, int EB = 2>
+__device__ __forceinline__ void win2_range(const sptgb_hicoo_args &a, const Win2Ctx &x, uint4 *s_rec,
+                                           uint32_t *s_row, float *tile,
                                            uint32_t row0, uint64_t klo, uint64_t khi, uint32_t r_beg,
                                            uint32_t r_end) {
     // EB: records per gather batch
@@ -331,7 +212,10 @@ __device__ __forceinline__ void win2_range(const sptgb_hicoo_args &a, const Win2
             bstart = last;
             base += W;
         }
-        uint4 r = make_uint4(NONE, 0u, 0u, 0u);
+        // an empty record: row NONE, product rows 0 (in range for the
+        // unconditional gathers)
+        uint4 r = make_uint4(NP == 2 ? NONE : 0u, 0u, 0u, 0u);
+        uint32_t rrow = NONE;
         if (valid && !todo) {
             const uint32_t b = a.perm[myk];
             const uint32_t e = (uint32_t)a.bptr[b] + (p - mystart);
@@ -341,8 +225,18 @@ __device__ __forceinline__ void win2_range(const sptgb_hicoo_args &a, const Win2
                 const uint32_t row = TILE ? rl : (x.b_m[b] << a.sb_bits) + rl;
                 const uint32_t ra = (x.b_a[b] << a.sb_bits) + x.e_a[e];
                 const uint32_t rr = (x.b_b[b] << a.sb_bits) + x.e_b[e];
-                ok = rl < x.rows_w && (TILE ? row0 + rl : row) < a.out_rows && ra < x.lim_a && rr < x.lim_b;
-                if (ok) r = make_uint4(row, ra, rr, __float_as_uint(a.vals[e]));
+                if constexpr (NP == 2) {
+                    ok = rl < x.rows_w && (TILE ? row0 + rl : row) < a.out_rows && ra < x.lim_a && rr < x.lim_b;
+                    if (ok) r = make_uint4(row, ra, rr, __float_as_uint(a.vals[e]));
+                } else {
+                    const uint32_t rc = (x.b_c[b] << a.sb_bits) + x.e_c[e];
+                    ok = rl < x.rows_w && (TILE ? row0 + rl : row) < a.out_rows && ra < x.lim_a && rr < x.lim_b &&
+                         rc < x.lim_c;
+                    if (ok) {
+                        r = make_uint4(ra, rr, rc, __float_as_uint(a.vals[e]));
+                        rrow = row;
+                    }
+                }
             }
             if (!ok) atomicOr(a.err, 1u);
         } else if (valid) {
@@ -352,39 +246,76 @@ __device__ __forceinline__ void win2_range(const sptgb_hicoo_args &a, const Win2
         kb = __shfl_sync(0xffffffffu, myk, W - 1, W);
         kst = __shfl_sync(0xffffffffu, mystart, W - 1, W);
         s_rec[threadIdx.x & 31] = r;
+        if constexpr (NP == 3) s_row[threadIdx.x & 31] = rrow;
         __syncwarp();
 #pragma unroll
         for (int j0 = 0; j0 < W; j0 += EB) {
-            uint4 q4[EB];
-            float4 fa[EB], fb[EB];
+            if constexpr (NP == 2) {
+                uint4 q4[EB];
+                float4 fa[EB], fb[EB];
 #pragma unroll
-            for (int t = 0; t < EB; ++t) q4[t] = s_rec[x.wk * W + j0 + t];
+                for (int t = 0; t < EB; ++t) q4[t] = s_rec[x.wk * W + j0 + t];
 #pragma unroll
-            for (int t = 0; t < EB; ++t) {
-                if (FULL) {
-                    fa[t] = __ldg(reinterpret_cast<const float4 *>(x.Fa + (size_t)q4[t].y * x.rb));
-                    fb[t] = __ldg(reinterpret_cast<const float4 *>(x.Fb + (size_t)q4[t].z * x.rb));
-                } else {
-                    const bool use = q4[t].x != NONE && x.col_ok;
-                    fa[t] = use ? __ldg(reinterpret_cast<const float4 *>(x.Fa + (size_t)q4[t].y * x.rb))
+                for (int t = 0; t < EB; ++t) {
+                    if (FULL) {
+                        fa[t] = __ldg(reinterpret_cast<const float4 *>(x.Fa + (size_t)q4[t].y * x.rb));
+                        fb[t] = __ldg(reinterpret_cast<const float4 *>(x.Fb + (size_t)q4[t].z * x.rb));
+                    } else {
+                        const bool use = q4[t].x != NONE && x.col_ok;
+                        fa[t] = use ? __ldg(reinterpret_cast<const float4 *>(x.Fa + (size_t)q4[t].y * x.rb))
+                                    : make_float4(0.f, 0.f, 0.f, 0.f);
+                        fb[t] = use ? __ldg(reinterpret_cast<const float4 *>(x.Fb + (size_t)q4[t].z * x.rb))
+                                    : make_float4(0.f, 0.f, 0.f, 0.f);
+                    }
+                }
+#pragma unroll
+                for (int t = 0; t < EB; ++t) {
+                    if (q4[t].x == NONE) continue;
+                    if (q4[t].x != cur) {
+                        put();
+                        cur = q4[t].x;
+                        acc = make_float4(0.f, 0.f, 0.f, 0.f);
+                    }
+                    const float v = __uint_as_float(q4[t].w);
+                    acc.x += v * fa[t].x * fb[t].x;
+                    acc.y += v * fa[t].y * fb[t].y;
+                    acc.z += v * fa[t].z * fb[t].z;
+                    acc.w += v * fa[t].w * fb[t].w;
+                }
+            } else {
+                // order 4: v * U_a * U_b * U_c in mats_order
+                uint4 q4[EB];
+                uint32_t qr[EB];
+                float4 fa[EB], fb[EB], fc[EB];
+#pragma unroll
+                for (int t = 0; t < EB; ++t) {
+                    q4[t] = s_rec[x.wk * W + j0 + t];
+                    qr[t] = s_row[x.wk * W + j0 + t];
+                }
+#pragma unroll
+                for (int t = 0; t < EB; ++t) {
+                    const bool use = FULL || (qr[t] != NONE && x.col_ok);
+                    fa[t] = use ? __ldg(reinterpret_cast<const float4 *>(x.Fa + (size_t)q4[t].x * x.rb))
                                 : make_float4(0.f, 0.f, 0.f, 0.f);
-                    fb[t] = use ? __ldg(reinterpret_cast<const float4 *>(x.Fb + (size_t)q4[t].z * x.rb))
+                    fb[t] = use ? __ldg(reinterpret_cast<const float4 *>(x.Fb + (size_t)q4[t].y * x.rb))
+                                : make_float4(0.f, 0.f, 0.f, 0.f);
+                    fc[t] = use ? __ldg(reinterpret_cast<const float4 *>(x.Fc + (size_t)q4[t].z * x.rb))
                                 : make_float4(0.f, 0.f, 0.f, 0.f);
                 }
-            }
 #pragma unroll
-            for (int t = 0; t < EB; ++t) {
-                if (q4[t].x == NONE) continue;
-                if (q4[t].x != cur) {
-                    put();
-                    cur = q4[t].x;
-                    acc = make_float4(0.f, 0.f, 0.f, 0.f);
+                for (int t = 0; t < EB; ++t) {
+                    if (qr[t] == NONE) continue;
+                    if (qr[t] != cur) {
+                        put();
+                        cur = qr[t];
+                        acc = make_float4(0.f, 0.f, 0.f, 0.f);
+                    }
+                    const float v = __uint_as_float(q4[t].w);
+                    acc.x += v * fa[t].x * fb[t].x * fc[t].x;
+                    acc.y += v * fa[t].y * fb[t].y * fc[t].y;
+                    acc.z += v * fa[t].z * fb[t].z * fc[t].z;
+                    acc.w += v * fa[t].w * fb[t].w * fc[t].w;
                 }
-                const float v = __uint_as_float(q4[t].w);
-                acc.x += v * fa[t].x * fb[t].x;
-                acc.y += v * fa[t].y * fb[t].y;
-                acc.z += v * fa[t].z * fb[t].z;
-                acc.w += v * fa[t].w * fb[t].w;
             }
         }
         __syncwarp();
@@ -393,7 +324,7 @@ __device__ __forceinline__ void win2_range(const sptgb_hicoo_args &a, const Win2
 }
 
 // The per-lane constants of a worker (lane sl of worker wk in its warp).
-template <int W>
+template <int W, int NP>
 __device__ __forceinline__ void win2_ctx(const sptgb_hicoo_args &a, Win2Ctx &x) {
     const int lane = threadIdx.x & 31;
     x.sl = lane % W;
@@ -422,6 +353,13 @@ __device__ __forceinline__ void win2_ctx(const sptgb_hicoo_args &a, Win2Ctx &x) 
     x.lim_b = a.ndims[pb];
     x.Fa = reinterpret_cast<const char *>(a.fac[pa]) + (size_t)x.sl * 16;
     x.Fb = reinterpret_cast<const char *>(a.fac[pb]) + (size_t)x.sl * 16;
+    if constexpr (NP == 3) {
+        const uint32_t pc = a.order[3];
+        x.e_c = a.einds[pc];
+        x.b_c = a.binds[pc];
+        x.lim_c = a.ndims[pc];
+        x.Fc = reinterpret_cast<const char *>(a.fac[pc]) + (size_t)x.sl * 16;
+    }
     x.rb = x.st * 4u;
 }
 
@@ -429,35 +367,43 @@ __device__ __forceinline__ void win2_ctx(const sptgb_hicoo_args &a, Win2Ctx &x) 
 // nonzeros, e.g. every window of a uniform mode) is one flat light range:
 // this kernel has no tile, so it needs no shared memory beyond the record
 // staging (the L1 keeps the rest) and fewer registers than k_hicoo_win2.
-constexpr int LIGHT_MINB = 6;   // CTAs per SM the register budget is set for
+constexpr int LIGHT_MINB = 6;   // CTAs per SM the register budget is set for (order 3)
 constexpr int LIGHT_EB = 2;     // records per gather batch
-template <int W, bool FULL, bool AC>
-__global__ void __launch_bounds__(BLOCK, LIGHT_MINB) k_hicoo_light(sptgb_hicoo_args a, uint32_t chunk, uint32_t total) {
+// CTAs per SM of the window kernels: order 4 gathers a third factor row per
+// record and gets the registers of 4 CTAs per SM
+constexpr int win_minb(int np, bool light) { return np == 2 ? (light ? LIGHT_MINB : 5) : 4; }
+template <int W, int NP, bool FULL, bool AC>
+__global__ void __launch_bounds__(BLOCK, win_minb(NP, true))
+    k_hicoo_light(sptgb_hicoo_args a, uint32_t chunk, uint32_t total) {
     constexpr int NWARP = BLOCK / 32;
     constexpr uint32_t NWC = BLOCK / W;   // workers per CTA
     __shared__ uint4 s_rec[NWARP][32];
+    __shared__ uint32_t s_row[NP == 3 ? NWARP : 1][32];   // output rows of the staged order-4 records
     const int warp = threadIdx.x >> 5;
     Win2Ctx x;
-    win2_ctx<W>(a, x);
+    win2_ctx<W, NP>(a, x);
     const uint32_t gw = (uint32_t)(warp * (32 / W) + x.wk);
     const uint64_t lo64 = (uint64_t)blockIdx.x * chunk;
     if (lo64 >= total) return;
     const uint32_t lo = (uint32_t)lo64, hi = (uint32_t)min((uint64_t)total, lo64 + chunk);
     const uint32_t per = (hi - lo + NWC - 1) / NWC;
     const uint32_t r_beg = lo + min(hi - lo, gw * per);
-    win2_range<W, false, FULL, AC, LIGHT_EB>(a, x, s_rec[warp], nullptr, 0u, 0u, a.nb, r_beg, min(hi, r_beg + per));
+    win2_range<W, NP, false, FULL, AC, LIGHT_EB>(a, x, s_rec[warp], s_row[NP == 3 ? warp : 0], nullptr, 0u, 0u,
+                                                 a.nb, r_beg, min(hi, r_beg + per));
 }
 
-template <int W, bool FULL, bool AC>
-__global__ void __launch_bounds__(BLOCK, 5) k_hicoo_win2(sptgb_hicoo_args a, uint32_t chunk, uint32_t total) {
+template <int W, int NP, bool FULL, bool AC>
+__global__ void __launch_bounds__(BLOCK, win_minb(NP, false))
+    k_hicoo_win2(sptgb_hicoo_args a, uint32_t chunk, uint32_t total) {
     extern __shared__ float tile[];   // [1 << sb][stride]
     constexpr int NWARP = BLOCK / 32;
     constexpr int NWK = 32 / W;              // workers per warp
     constexpr uint32_t NWC = BLOCK / W;      // workers per CTA
     __shared__ uint4 s_rec[NWARP][32];
+    __shared__ uint32_t s_row[NP == 3 ? NWARP : 1][32];   // output rows of the staged order-4 records
     const int warp = threadIdx.x >> 5;
     Win2Ctx x;
-    win2_ctx<W>(a, x);
+    win2_ctx<W, NP>(a, x);
     const uint32_t mode = a.mode;
     const uint32_t st4 = x.st / 4;
     const uint32_t gw = (uint32_t)(warp * NWK + x.wk);
@@ -492,7 +438,8 @@ __global__ void __launch_bounds__(BLOCK, 5) k_hicoo_win2(sptgb_hicoo_args a, uin
             const uint32_t s0 = q, s1 = hi < rend ? hi : rend;
             const uint32_t per = (s1 - s0 + NWC - 1) / NWC;
             const uint32_t r_beg = s0 + min(s1 - s0, gw * per);
-            win2_range<W, false, FULL, AC>(a, x, s_rec[warp], tile, 0u, k0, kend, r_beg, min(s1, r_beg + per));
+            win2_range<W, NP, false, FULL, AC>(a, x, s_rec[warp], s_row[NP == 3 ? warp : 0], tile, 0u, k0, kend,
+                                               r_beg, min(s1, r_beg + per));
             q = s1;
             w = wh;
             continue;
@@ -501,7 +448,8 @@ __global__ void __launch_bounds__(BLOCK, 5) k_hicoo_win2(sptgb_hicoo_args a, uin
         const uint32_t row0 = a.binds[mode][a.perm[k0]] << a.sb_bits;
         const uint32_t per = (s1 - s0 + NWC - 1) / NWC;
         const uint32_t r_beg = s0 + min(s1 - s0, gw * per);
-        win2_range<W, true, FULL, AC>(a, x, s_rec[warp], tile, row0, k0, k1, r_beg, min(s1, r_beg + per));
+        win2_range<W, NP, true, FULL, AC>(a, x, s_rec[warp], s_row[NP == 3 ? warp : 0], tile, row0, k0, k1, r_beg,
+                                          min(s1, r_beg + per));
         __syncthreads();
         // one write of the window: plain when this CTA covered all of it
         const bool owned = s0 == wbeg && s1 == wend;
@@ -534,34 +482,34 @@ __global__ void k_block_sizes(const uint32_t *__restrict__ perm, const uint64_t 
         sizes[k] = (uint32_t)(bptr[perm[k] + 1] - bptr[perm[k]]);
 }
 
-template <int W, bool FULL, bool AC>
+template <int W, int NP, bool FULL, bool AC>
 cudaError_t launch_win2_k(const sptgb_hicoo_args &a, cudaStream_t s) {
     const size_t smem = ((size_t)1 << a.sb_bits) * a.stride * sizeof(float);
     if (smem > 180 * 1024) return cudaErrorInvalidValue;
     // once per process: a function-local static is initialised by one thread
     // while the others wait (a failure shows up as the launch's error)
     static const cudaError_t attr =
-        cudaFuncSetAttribute(k_hicoo_win2<W, FULL, AC>, cudaFuncAttributeMaxDynamicSharedMemorySize, 180 * 1024);
+        cudaFuncSetAttribute(k_hicoo_win2<W, NP, FULL, AC>, cudaFuncAttributeMaxDynamicSharedMemorySize, 180 * 1024);
     (void)attr;
     const int nsm = sptgb_sm_count();
     int per = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_hicoo_win2<W, FULL, AC>, BLOCK, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_hicoo_win2<W, NP, FULL, AC>, BLOCK, smem);
     if (per < 1) per = 1;
     if (a.nnz == 0 || a.nnz >= 0xffffffffull) return a.nnz ? cudaErrorInvalidValue : cudaSuccess;
     const uint32_t total = (uint32_t)a.nnz;
     const uint64_t grid = (uint64_t)nsm * per * 2;
     const uint32_t chunk = (uint32_t)((total + grid - 1) / grid);
     const uint32_t ngrid = (total + chunk - 1) / chunk;
-    k_hicoo_win2<W, FULL, AC><<<ngrid, BLOCK, smem, s>>>(a, chunk, total);
+    k_hicoo_win2<W, NP, FULL, AC><<<ngrid, BLOCK, smem, s>>>(a, chunk, total);
     sptgb_count_launch(1);
     return cudaGetLastError();
 }
 
-template <int W, bool FULL, bool AC>
+template <int W, int NP, bool FULL, bool AC>
 cudaError_t launch_light_k(const sptgb_hicoo_args &a, cudaStream_t s) {
     static const int per = [] {
         int p = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p, k_hicoo_light<W, FULL, AC>, BLOCK, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p, k_hicoo_light<W, NP, FULL, AC>, BLOCK, 0);
         return p < 1 ? 1 : p;
     }();
     const int nsm = sptgb_sm_count();
@@ -570,41 +518,19 @@ cudaError_t launch_light_k(const sptgb_hicoo_args &a, cudaStream_t s) {
     const uint64_t grid = (uint64_t)nsm * per * 2;
     const uint32_t chunk = (uint32_t)((total + grid - 1) / grid);
     const uint32_t ngrid = (total + chunk - 1) / chunk;
-    k_hicoo_light<W, FULL, AC><<<ngrid, BLOCK, 0, s>>>(a, chunk, total);
+    k_hicoo_light<W, NP, FULL, AC><<<ngrid, BLOCK, 0, s>>>(a, chunk, total);
     sptgb_count_launch(1);
     return cudaGetLastError();
-}
-
-template <int W>
-cudaError_t launch_win2(const sptgb_hicoo_args &a, cudaStream_t s) {
-    if (a.nheavy == 0) {
-        if (a.stride != 4u * W) return launch_light_k<W, false, false>(a, s);
-        return a.rank == a.stride ? launch_light_k<W, true, true>(a, s) : launch_light_k<W, true, false>(a, s);
-    }
-    if (a.stride != 4u * W) return launch_win2_k<W, false, false>(a, s);
-    return a.rank == a.stride ? launch_win2_k<W, true, true>(a, s) : launch_win2_k<W, true, false>(a, s);
 }
 
 template <int W, int NP>
-cudaError_t launch_win(const sptgb_hicoo_args &a, cudaStream_t s) {
-    const size_t smem = ((size_t)1 << a.sb_bits) * a.stride * sizeof(float);
-    if (smem > 200 * 1024) return cudaErrorInvalidValue;
-    static const cudaError_t attr =
-        cudaFuncSetAttribute(k_hicoo_win<W, NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    (void)attr;   // once per process, as in launch_win2_k
-    const int nsm = sptgb_sm_count();
-    int per = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_hicoo_win<W, NP>, BLOCK, smem);
-    if (per < 1) per = 1;
-    if (a.nnz == 0 || a.nnz >= 0xffffffffull) return a.nnz ? cudaErrorInvalidValue : cudaSuccess;
-    const uint32_t total = (uint32_t)a.nnz;
-    // about two waves of CTAs with equal numbers of nonzeros
-    const uint64_t grid = (uint64_t)nsm * per * 2;
-    const uint32_t chunk = (uint32_t)((total + grid - 1) / grid);
-    const uint32_t ngrid = (total + chunk - 1) / chunk;
-    k_hicoo_win<W, NP><<<ngrid, BLOCK, smem, s>>>(a, chunk, total);
-    sptgb_count_launch(1);
-    return cudaGetLastError();
+cudaError_t launch_win2(const sptgb_hicoo_args &a, cudaStream_t s) {
+    if (a.nheavy == 0) {
+        if (a.stride != 4u * W) return launch_light_k<W, NP, false, false>(a, s);
+        return a.rank == a.stride ? launch_light_k<W, NP, true, true>(a, s) : launch_light_k<W, NP, true, false>(a, s);
+    }
+    if (a.stride != 4u * W) return launch_win2_k<W, NP, false, false>(a, s);
+    return a.rank == a.stride ? launch_win2_k<W, NP, true, true>(a, s) : launch_win2_k<W, NP, true, false>(a, s);
 }
 
 // *err = 1 when an element's coordinate is outside its mode or its element
@@ -649,17 +575,17 @@ extern "C" cudaError_t sptgb_mttkrp_hicoo(const sptgb_hicoo_args *a, cudaStream_
     // the window kernels count positions and blocks in 32 bits
     if (a->perm && (a->nmodes == 3 || a->nmodes == 4) && a->nnz < 0xfffff000ull) {
         if (a->nmodes == 3) {
-            if (c4 <= 2) return launch_win2<2>(*a, s);
-            if (c4 <= 4) return launch_win2<4>(*a, s);
-            if (c4 <= 8) return launch_win2<8>(*a, s);
-            if (c4 <= 16) return launch_win2<16>(*a, s);
-            return launch_win2<32>(*a, s);
+            if (c4 <= 2) return launch_win2<2, 2>(*a, s);
+            if (c4 <= 4) return launch_win2<4, 2>(*a, s);
+            if (c4 <= 8) return launch_win2<8, 2>(*a, s);
+            if (c4 <= 16) return launch_win2<16, 2>(*a, s);
+            return launch_win2<32, 2>(*a, s);
         }
-        if (c4 <= 2) return launch_win<2, 3>(*a, s);
-        if (c4 <= 4) return launch_win<4, 3>(*a, s);
-        if (c4 <= 8) return launch_win<8, 3>(*a, s);
-        if (c4 <= 16) return launch_win<16, 3>(*a, s);
-        return launch_win<32, 3>(*a, s);
+        if (c4 <= 2) return launch_win2<2, 3>(*a, s);
+        if (c4 <= 4) return launch_win2<4, 3>(*a, s);
+        if (c4 <= 8) return launch_win2<8, 3>(*a, s);
+        if (c4 <= 16) return launch_win2<16, 3>(*a, s);
+        return launch_win2<32, 3>(*a, s);
     }
     if (c4 <= 2) return launch<2>(*a, s);
     if (c4 <= 4) return launch<4>(*a, s);
