@@ -117,7 +117,9 @@ __device__ __forceinline__ uint64_t block_at(const uint32_t *pnnz, uint64_t lo, 
 //    running row sum of a worker goes to the output with a vector atomic when
 //    the row changes, with no per-window barrier or tile write, so the many
 //    small windows of a long tail cost no more than their nonzeros.
-// Product modes a, b (mats_order[1], [2]) and, for order 4, c ([3]).
+//
+// Per-lane constants; product modes a, b (mats_order[1], [2]) and, for
+// order 4, c ([3]).
 struct Win2Ctx {
     const uint8_t *e_m, *e_a, *e_b, *e_c;
     const uint32_t *b_m, *b_a, *b_b, *b_c;
@@ -131,19 +133,19 @@ struct Win2Ctx {
 
 // One worker's positions [r_beg, r_end) of the blocks [klo, khi) of the
 // schedule, for NP product modes (2: order 3, 3: order 4).  Records are
-// staged as {row, row of a, row of b, value} (NP = 2) or as {row of a, row of
-// b, row of c, value} with the output row in s_row (NP = 3).  TILE: rows are window rows (row0 + r) summed in `tile`;
-// otherwise output rows, flushed with vector atomics.  FULL: the stride is
+// staged as {row, row of a, row of b, value} (NP = 2) or as {row of a, row
+// of b, row of c, value} with the output row in s_row (NP = 3).  TILE: rows
+// are window rows (row0 + r) summed in `tile`; otherwise output rows,
+// flushed with vector atomics.  FULL: the stride is
 // exactly 4W columns, so every lane holds stored columns and the factor rows
 // are gathered without a select (an empty record carries rows 0, in range).
 // AC (with FULL): the rank equals the stride, so no column is padding and the
-// row flushes need no column masks.
+// row flushes need no column masks.  EB: records per gather batch.
 template <int W, int NP, bool TILE, bool FULL, bool AC, int EB = 2>
 __device__ __forceinline__ void win2_range(const sptgb_hicoo_args &a, const Win2Ctx &x, uint4 *s_rec,
                                            uint32_t *s_row, float *tile,
                                            uint32_t row0, uint64_t klo, uint64_t khi, uint32_t r_beg,
                                            uint32_t r_end) {
-    // EB: records per gather batch
     uint32_t cur = NONE;
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     auto put = [&]() {
