@@ -27,7 +27,7 @@ constexpr int TR = 32;           // rows per tile
 constexpr int RMAX = 64;
 constexpr int PMAX = RMAX * (RMAX + 1) / 2;
 constexpr int PPT = (PMAX + DT - 1) / DT;   // pairs per thread (9)
-constexpr int NBLK = 2 * 152;    // partial-reduction blocks
+constexpr int NBLK = SPTGB_NPART;   // partial-reduction blocks (fixed, device-independent)
 
 __device__ __forceinline__ void pair_of(int idx, int rank, int *p, int *q) {
     // idx enumerates (p, q), p <= q, row by row.

@@ -30,7 +30,7 @@
 #include "../../../include/sptgb.h"
 
 #define NA_MAX_VALUES (4u * 1024u * 1024u)
-#define NA_BLOCKS 304
+#define NA_BLOCKS SPTGB_NPART
 #define NA_THREADS 256
 #define NA_VALUES_BYTES ((size_t)NA_MAX_VALUES * sizeof(float))
 #define NA_PART_OFFSET NA_VALUES_BYTES

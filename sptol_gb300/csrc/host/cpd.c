@@ -326,10 +326,10 @@ static double sumsq_host(const float *v, uint64_t n) {
     double *ws = NULL;
     if (n == 0) return 0.0;
     if (cudaMalloc((void **)&d, n * sizeof(float)) != cudaSuccess) goto done;
-    if (cudaMalloc((void **)&ws, 2 * 152 * sizeof(double) + 64) != cudaSuccess) goto done;
+    if (cudaMalloc((void **)&ws, SPTGB_NPART * sizeof(double) + 64) != cudaSuccess) goto done;
     if (cudaMemcpyAsync(d, v, n * sizeof(float), cudaMemcpyHostToDevice, s) != cudaSuccess) goto done;
-    if (sptgb_sumsq(d, n, ws + 2 * 152, ws, s) != cudaSuccess) goto done;
-    if (cudaMemcpyAsync(&out, ws + 2 * 152, sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess) goto done;
+    if (sptgb_sumsq(d, n, ws + SPTGB_NPART, ws, s) != cudaSuccess) goto done;
+    if (cudaMemcpyAsync(&out, ws + SPTGB_NPART, sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess) goto done;
     cudaStreamSynchronize(s);
 done:
     if (d) cudaFree(d);

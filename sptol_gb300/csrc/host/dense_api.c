@@ -138,7 +138,7 @@ int sptMatrixSolveNormals(sptIndex const mode, sptIndex const nmodes, sptMatrix 
         double *d64 = (double *)dalloc(&l, (size_t)nmodes * rank * rank * sizeof(double));
         double *Hinv = (double *)dalloc(&l, (size_t)2 * rank * rank * sizeof(double));
         int *status = (int *)dalloc(&l, 16);
-        double *ws = (double *)dalloc(&l, sptgb_dense_ws_bytes((int)rank, 2 * 152));
+        double *ws = (double *)dalloc(&l, sptgb_dense_ws_bytes((int)rank, SPTGB_NPART));
         float *dM = (float *)dalloc(&l, (size_t)nrows * stride * sizeof(float));
         float *dX = (float *)dalloc(&l, (size_t)nrows * stride * sizeof(float));
         NEED(d64);
@@ -178,7 +178,7 @@ static int col_norm(sptMatrix *A, sptValue *lambda, int use_max, int lambda_io, 
     {
         float *dA = (float *)dalloc(&l, (size_t)nrows * stride * sizeof(float));
         float *dl = (float *)dalloc(&l, DMAX * sizeof(float));
-        double *ws = (double *)dalloc(&l, sptgb_dense_ws_bytes((int)rank, 2 * 152) + 2 * 152 * DMAX * 4);
+        double *ws = (double *)dalloc(&l, sptgb_dense_ws_bytes((int)rank, SPTGB_NPART) + SPTGB_NPART * DMAX * 4);
         NEED(dA);
         NEED(dl);
         NEED(ws);
@@ -269,7 +269,7 @@ double sptSparseKruskalTensorInnerProduct(sptIndex const nmodes, sptValue const 
         float *dA = (float *)dalloc(&l, (size_t)I * stride * sizeof(float));
         float *dB = (float *)dalloc(&l, (size_t)I * stride * sizeof(float));
         float *dl = (float *)dalloc(&l, DMAX * sizeof(float));
-        double *ws = (double *)dalloc(&l, (size_t)2 * 152 * DMAX * sizeof(double) + 64);
+        double *ws = (double *)dalloc(&l, (size_t)SPTGB_NPART * DMAX * sizeof(double) + 64);
         NEED(dA);
         NEED(dB);
         NEED(dl);
@@ -281,7 +281,7 @@ double sptSparseKruskalTensorInnerProduct(sptIndex const nmodes, sptValue const 
                                s));
         }
         CK(cudaMemcpyAsync(dl, lambda, rank * sizeof(float), cudaMemcpyHostToDevice, s));
-        double *dout = ws + 2 * 152 * DMAX;
+        double *dout = ws + SPTGB_NPART * DMAX;
         CK(sptgb_rowdot(dA, dB, I, (int)rank, (int)stride, dl, dout, ws, s));
         CK(cudaMemcpyAsync(&result, dout, sizeof(double), cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));

@@ -219,6 +219,11 @@ typedef struct {
     int      stride;
     double  *ws;        /* device workspace, sptgb_dense_ws_bytes() */
 } sptgb_dense_ctx;
+/* Blocks of the dense reductions (Grams, norms, fit terms, ||X||^2): a fixed
+ * count, two per SM of a GB300, so the partial sums and the order in which
+ * they are combined do not depend on the device; workspaces hold this many
+ * partials. */
+#define SPTGB_NPART 304
 size_t      sptgb_dense_ws_bytes(int rank, int max_blocks);
 /* G = A^T A in FP64 (full symmetric) over rows [0, nrows). */
 cudaError_t sptgb_gram(const float *A, uint32_t nrows, int rank, int stride, double *G, double *ws,
